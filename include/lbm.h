@@ -1,0 +1,185 @@
+/*
+ * lbm.h - C ABI of the GB300 lattice Boltzmann engine (D3Q19 MRT with
+ * finite-size moving spheres).
+ *
+ * The engine replaces the no-argument Fortran subroutines that the
+ * reference main loop calls once per time step
+ * (3DBox_Forced_HI_Turbulence_Moving_Particles_LBM/main.f90:172-188 and
+ * 3DChannel_Decaying_HIT_Finite_Size_Moving_Particles/main.f90:187-204):
+ *
+ *   FORCING -> collision_MRT -> beads_collision -> streaming ->
+ *   beads_lubforce -> beads_move -> beads_redistribute -> beads_links ->
+ *   beads_filling -> macrovar
+ *
+ * The state that module var_inc shares between those subroutines
+ * (3DBox.../var_inc.f90:70-103) lives on the GPU inside an lbm_ctx.  Every
+ * entry point below takes plain host pointers and sizes; host arrays use the
+ * reference's Fortran memory order, so a Fortran caller passes its own
+ * arrays through ISO_C_BINDING without copying them first.
+ *
+ * Conventions shared by every entry point:
+ *  - return 0 (LBM_OK) on success, a negative LBM_ERR_* code on failure;
+ *    lbm_last_error() then describes the failure.  Nothing aborts the
+ *    process (the reference's `stop` statements become error codes).
+ *  - calls on one context are serialised on the context's CUDA stream and
+ *    are not thread-safe; different contexts may be driven from different
+ *    host threads.
+ *  - no host pointer is retained after a call returns.
+ *  - particle ids are 0-based here; the reference's ids are 1-based
+ *    (isnodes = ip in 3DBox.../partlib.f90:992), so isnodes(i,j,k) = ip-1.
+ */
+#ifndef LBM_GB300_LBM_H
+#define LBM_GB300_LBM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  LBM_OK = 0,
+  LBM_ERR_ARG = -1,       /* bad argument or unsupported configuration       */
+  LBM_ERR_CUDA = -2,      /* a CUDA runtime call failed                      */
+  LBM_ERR_OVERLAP = -3,   /* particles overlap after a move (partlib.f90:2641) */
+  LBM_ERR_CAPACITY = -4,  /* a fixed-capacity device list overflowed         */
+  LBM_ERR_ALPHA = -5,     /* link fraction outside [0,1] (partlib.f90:1026)  */
+  LBM_ERR_NONFINITE = -6, /* non-finite value detected in the state          */
+  LBM_ERR_TIMEOUT = -7,   /* a bounded device-side wait ran out              */
+  LBM_ERR_STATE = -8,     /* call out of order (e.g. no particles uploaded)  */
+  LBM_ERR_NOMEM = -9      /* device allocation failed                        */
+};
+
+/* ---- configuration ------------------------------------------------------ */
+enum { LBM_PREC_F64 = 0, LBM_PREC_F32 = 1 };
+/* LBM_BC_XWALLS: halfway bounce-back walls at x = 0 and x = nx, periodic in
+ * y and z (3DChannel.../streaming.f90:11-13,175-187). */
+enum { LBM_BC_PERIODIC = 0, LBM_BC_XWALLS = 1 };
+/* LBM_FORCING_STOCHASTIC: low-wavenumber Ornstein-Uhlenbeck forcing
+ * (3DBox.../gaussian.f90:182-372); LBM_FORCING_CONSTANT: uniform body force
+ * (0, force_y, 0) (3DChannel.../collision.f90:335-347). */
+enum { LBM_FORCING_NONE = 0, LBM_FORCING_STOCHASTIC = 1, LBM_FORCING_CONSTANT = 2 };
+/* preset selector for lbm_config_init */
+enum { LBM_PRESET_BOX = 0, LBM_PRESET_CHANNEL = 1 };
+
+typedef struct lbm_config {
+  int32_t nx, ny, nz;     /* lattice nodes per axis (lx = nx, ly = ny, lz = nz) */
+  int32_t npart_max;      /* particle capacity (0: no particles)               */
+  int32_t mrt_type;       /* 1, 2 or 3 as in para.f90:96-135                   */
+  int32_t boundary;       /* LBM_BC_*                                          */
+  int32_t forcing;        /* LBM_FORCING_*                                     */
+  int32_t precision;      /* LBM_PREC_*                                        */
+  int32_t iseedf;         /* forcing RNG seed, para.f90:20 (232300)           */
+  int32_t iseedp;         /* particle position RNG seed, para.f90:247 (12345) */
+  int32_t link_capacity;  /* links per particle (0: derived from rad)         */
+  int32_t reserved_i[5];
+  double visc;            /* kinematic viscosity; tau = 3 visc + 0.5          */
+  double rho0;            /* reference density (1)                            */
+  double rhopart;         /* particle density (var_inc.f90:27)                */
+  double rad;             /* particle radius (var_inc.f90:28)                 */
+  double mingap;          /* particle-particle lubrication range              */
+  double mingap_w;        /* particle-wall lubrication range (channel)        */
+  double vscale;          /* forcing velocity scale, para.f90:37              */
+  double force_y;         /* constant body force per volume (channel)         */
+  double fpc;             /* lubrication scale: volp*rho0*9.8/gscale (box,
+                             partlib.f90:2260) or volp*rho0*g_lbm (channel)   */
+  double stf0, stf1;      /* particle-particle stiffness, para.f90:244-245    */
+  double stf0_w, stf1_w;  /* particle-wall stiffness (channel para.f90)       */
+  double body_force_y;    /* extra y force added in beads_move:
+                             -volp*rhog (box, partlib.f90:2332) or
+                             +volp*force_in_y (channel partlib.f90:2409)     */
+  double reserved_d[6];
+} lbm_config;
+
+/* Fill `cfg` with the reference's values for an n^3 box (para.f90) or an
+ * nx*ny*nz x-walled channel (channel para.f90) holding `npart` spheres of
+ * radius `rad` and density `rhopart`.  visc defaults to 0.0036. */
+int lbm_config_init(lbm_config* cfg, int preset, int nx, int ny, int nz,
+                    int npart, double rad, double rhopart);
+
+/* ---- context ------------------------------------------------------------ */
+typedef struct lbm_ctx lbm_ctx;
+
+int lbm_create(const lbm_config* cfg, lbm_ctx** out);  /* allocates all device state */
+int lbm_destroy(lbm_ctx* ctx);
+const char* lbm_last_error(const lbm_ctx* ctx);         /* never NULL */
+int lbm_version(void);                                  /* ABI version (1) */
+/* bytes of device memory a context with this configuration allocates */
+int lbm_footprint(const lbm_config* cfg, uint64_t* bytes);
+/* Use `stream` (a cudaStream_t) for all work of this context; NULL = the
+ * context's own stream. */
+int lbm_set_stream(lbm_ctx* ctx, void* stream);
+int lbm_synchronize(lbm_ctx* ctx);
+
+/* ---- populations and macroscopic fields (var_inc.f90:89-92) ------------- */
+/* f(0:18, lx, ly, lz) in Fortran order (population index fastest), FP64.
+ * Replaces reading/writing var_inc's f. */
+int lbm_upload_f(lbm_ctx* ctx, const double* f);
+int lbm_download_f(lbm_ctx* ctx, double* f);
+/* structure-of-arrays form f[q][z][y][x], q = 0..18, FP64 */
+int lbm_upload_f_soa(lbm_ctx* ctx, const double* f);
+int lbm_download_f_soa(lbm_ctx* ctx, double* f);
+/* initpop (3DBox.../initial.f90:3-28): f = feq(rho' = 0, u) for a velocity
+ * field given as three (lx, ly, lz) Fortran-order arrays. */
+int lbm_initpop(lbm_ctx* ctx, const double* ux, const double* uy, const double* uz);
+/* rho, ux, uy, uz as left by the last macrovar (each lx*ly*lz, Fortran order) */
+int lbm_download_macro(lbm_ctx* ctx, double* rho, double* ux, double* uy, double* uz);
+/* the body force field force_real{x,y,z} last produced by lbm_forcing */
+int lbm_download_force(lbm_ctx* ctx, double* fx, double* fy, double* fz);
+
+/* ---- particles (var_inc.f90:95-103) -------------------------------------- */
+/* Release `npart` particles: ypglb, wp, omgp as (3, npart) Fortran arrays
+ * (x,y,z fastest).  Equivalent to the `istep == irelease` block of
+ * main.f90:149-165 with given positions and velocities; builds the links
+ * (beads_links) and marks the next beads_move as the first one. */
+int lbm_upload_particles(lbm_ctx* ctx, int npart, const double* ypglb,
+                         const double* wp, const double* omgp);
+/* any pointer may be NULL; each is a (3, npart) array */
+int lbm_download_particles(lbm_ctx* ctx, double* ypglb, double* wp, double* omgp,
+                           double* fHIp, double* flubp, double* torqp);
+/* ibnodes (1 solid, -1 fluid) and isnodes (particle id, -1 fluid); each
+ * lx*ly*lz int32 in Fortran order; either may be NULL */
+int lbm_download_flags(lbm_ctx* ctx, int32_t* ibnodes, int32_t* isnodes);
+/* The current boundary links (the nonzero entries of ilink/mlink/alink,
+ * partlib.f90:1013-1024), grouped by particle and in (z, y, x, ipop) order
+ * inside each particle.  node = i + lx*(j + ly*k) (0-based), ipop = 1..18.
+ * Returns the link count in *nlinks; arrays may be NULL to query the count. */
+int lbm_download_links(lbm_ctx* ctx, int64_t capacity, int64_t* nlinks,
+                       int32_t* node, int32_t* ipop, int32_t* particle,
+                       double* alpha);
+
+/* ---- forcing state (gaussian.f90:182-215, saveload.f90:217-274) --------- */
+/* dir = 0: read (iseedf, iyf, ivf[32], b[3*150]) from the context;
+ * dir = 1: write them.  b holds b1r, b2r, b3r, each (6,5,5) Fortran order. */
+int lbm_forcing_state(lbm_ctx* ctx, int dir, int32_t* iseedf, int32_t* iyf,
+                      int32_t* ivf, double* b);
+
+/* ---- the reference subroutines, one entry each --------------------------- */
+int lbm_forcing(lbm_ctx* ctx);            /* gaussian.f90:182  FORCING        */
+int lbm_collision_mrt(lbm_ctx* ctx);      /* collision.f90:8   collision_MRT  */
+int lbm_beads_collision(lbm_ctx* ctx);    /* partlib.f90:1064  beads_collision*/
+int lbm_streaming(lbm_ctx* ctx);          /* streaming.f90:2   streaming      */
+int lbm_beads_lubforce(lbm_ctx* ctx);     /* partlib.f90:2211  beads_lubforce */
+int lbm_beads_move(lbm_ctx* ctx);         /* partlib.f90:2295  beads_move     */
+int lbm_beads_redistribute(lbm_ctx* ctx); /* partlib.f90:2397  (wrap+overlap) */
+int lbm_beads_links(lbm_ctx* ctx);        /* partlib.f90:934   beads_links    */
+int lbm_beads_filling(lbm_ctx* ctx);      /* partlib.f90:2793  beads_filling  */
+int lbm_macrovar(lbm_ctx* ctx);           /* collision.f90:232 macrovar       */
+int lbm_rhoupdat(lbm_ctx* ctx);           /* collision.f90:213 rhoupdat       */
+
+/* The whole time step of main.f90:172-188, `nsteps` times, fused into a
+ * short chain of kernels per step.  Leaves the same state as calling the
+ * entries above in that order. */
+int lbm_step(lbm_ctx* ctx, int nsteps);
+
+/* ---- diagnostics --------------------------------------------------------- */
+/* FP64 totals over all nodes: out[0] = sum f (mass), out[1..3] = momentum
+ * sum c f. */
+int lbm_mass_momentum(lbm_ctx* ctx, double out[4]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LBM_GB300_LBM_H */

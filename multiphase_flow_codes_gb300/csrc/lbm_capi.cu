@@ -1,0 +1,967 @@
+// lbm_capi.cu - the C ABI (include/lbm.h) over the GB300 kernels.
+//
+// A context owns every device buffer of one box.  Populations are kept in
+// the "plain" post-streaming layout between calls, which is the state the
+// reference holds between its subroutines, so the per-subroutine entries and
+// the fused lbm_step can be mixed freely.  lbm_step performs a whole time
+// step as: forcing update -> fused collide+stream -> bounce-back ->
+// particle update -> links -> refill, and leaves macrovar's output to be
+// materialised lazily (only when something reads it).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "lbm_internal.cuh"
+
+using namespace lbm;
+
+namespace {
+
+constexpr int kStagingDoubles = 1 << 25;  // 256 MB chunk for host transfers
+
+struct ForceState {
+  int mode;  // FM_NONE / FM_TABLE / FM_CONST
+  int slot;  // table slot for FM_TABLE
+};
+
+}  // namespace
+
+struct lbm_ctx {
+  lbm_config cfg;
+  Geometry g;
+  Rates r;
+  PartParams pp;
+  bool f32 = false;
+  size_t esz = 8;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+
+  void* f[2] = {nullptr, nullptr};
+  int cur = 0;
+  void* macro = nullptr;  // rho, ux, uy, uz (4*N of T)
+  bool macro_pending = false;  // macrovar of the current f not yet materialised
+  bool macro_derived = true;   // macro arrays equal macrovar(f) (or pending)
+  int32_t* flags[2] = {nullptr, nullptr};
+  int fcur = 0;
+
+  // forcing
+  ForcingDev* d_forcing = nullptr;
+  double* d_kxr6 = nullptr;
+  double* d_kyr5 = nullptr;
+  double* d_kzr5 = nullptr;
+  double* ztab = nullptr;
+  void* rowtab[3] = {nullptr, nullptr, nullptr};
+  void* xtw = nullptr;
+  ForceState latest{FM_NONE, 0}, fmacro{FM_NONE, 0};
+  double var = 0, tf = 0, pi2 = 0;
+
+  // particles
+  int npmax = 0, npart = 0;
+  bool particles_on = false;
+  double* pbuf = nullptr;  // 15 vectors of 3*npmax
+  double *ypglb, *ypglbp, *wp, *wpp, *omgp, *omgpp, *dwdt, *domgdt, *forcep, *forcepp, *torqp,
+      *torqpp, *thetap, *fHIp, *flubp;
+  int* first_move = nullptr;
+  LinkSlab links{};
+
+  DevStatus* status = nullptr;
+  DevStatus* status_host = nullptr;
+  double* staging = nullptr;
+  double* partial = nullptr;
+  double* partial_host = nullptr;
+};
+
+namespace {
+
+int fail(lbm_ctx* c, int code, const std::string& m) {
+  if (c) c->err = m;
+  return code;
+}
+
+#define CK(call)                                                                       \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess)                                                             \
+      return fail(ctx, LBM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+ParticleView pview(lbm_ctx* c) {
+  ParticleView v;
+  v.npart = c->npart;
+  v.cap = c->links.cap;
+  v.rad = c->cfg.rad;
+  v.rhopart = c->cfg.rhopart;
+  v.ypglb = c->ypglb;
+  v.wp = c->wp;
+  v.omgp = c->omgp;
+  return v;
+}
+
+MoveState mstate(lbm_ctx* c) {
+  MoveState m;
+  m.ypglb = c->ypglb; m.ypglbp = c->ypglbp; m.ypold = nullptr;
+  m.wp = c->wp; m.wpp = c->wpp; m.omgp = c->omgp; m.omgpp = c->omgpp;
+  m.dwdt = c->dwdt; m.domgdt = c->domgdt; m.forcep = c->forcep; m.forcepp = c->forcepp;
+  m.torqp = c->torqp; m.torqpp = c->torqpp; m.thetap = c->thetap; m.fHIp = c->fHIp;
+  m.flubp = c->flubp; m.first_move = c->first_move;
+  return m;
+}
+
+template <typename T>
+ForceView<T> fview(lbm_ctx* c, const ForceState& s) {
+  ForceView<T> v;
+  v.mode = s.mode;
+  v.rowtab = s.mode == FM_TABLE ? static_cast<const T*>(c->rowtab[s.slot]) : nullptr;
+  v.xtw = static_cast<const T*>(c->xtw);
+  v.cfx = T(0);
+  v.cfy = T(c->cfg.force_y);
+  v.cfz = T(0);
+  return v;
+}
+
+template <typename T>
+T* fbuf(lbm_ctx* c, int i) { return static_cast<T*>(c->f[i]); }
+template <typename T>
+T* mbuf(lbm_ctx* c, int comp) { return static_cast<T*>(c->macro) + comp * c->g.N; }
+
+int check_status(lbm_ctx* ctx) {
+  CK(cudaMemcpyAsync(ctx->status_host, ctx->status, sizeof(DevStatus), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  DevStatus s = *ctx->status_host;
+  if (s.code != 0) {
+    CK(cudaMemsetAsync(ctx->status, 0, sizeof(DevStatus), ctx->stream));
+    char buf[160];
+    const char* what = s.code == LBM_ERR_OVERLAP    ? "particles overlap after a move"
+                       : s.code == LBM_ERR_CAPACITY ? "link or geometry capacity exceeded"
+                       : s.code == LBM_ERR_STATE    ? "particle image sweep not at a fixed point"
+                                                    : "device error";
+    snprintf(buf, sizeof buf, "%s (particle %d)", what, s.where);
+    return fail(ctx, s.code, buf);
+  }
+  return 0;
+}
+
+template <typename T>
+void materialize_macro_t(lbm_ctx* c) {
+  launch_macrovar<T>(c->g, fbuf<T>(c, c->cur), c->flags[c->fcur], fview<T>(c, c->fmacro),
+                     pview(c), mbuf<T>(c, 0), mbuf<T>(c, 1), mbuf<T>(c, 2), mbuf<T>(c, 3),
+                     c->stream);
+}
+void materialize_macro(lbm_ctx* c) {
+  if (!c->macro_pending) return;
+  if (c->f32) materialize_macro_t<float>(c); else materialize_macro_t<double>(c);
+  c->macro_pending = false;
+  c->macro_derived = true;
+}
+
+int pick_slot(lbm_ctx* c) {
+  for (int s = 0; s < 3; ++s) {
+    bool used = (c->latest.mode == FM_TABLE && c->latest.slot == s) ||
+                (c->fmacro.mode == FM_TABLE && c->fmacro.slot == s);
+    if (!used) return s;
+  }
+  return 0;
+}
+
+// FORCING: advance the stochastic state and tabulate the new field
+void do_forcing(lbm_ctx* c) {
+  if (c->cfg.forcing == LBM_FORCING_STOCHASTIC) {
+    int s = pick_slot(c);
+    launch_forcing_update(c->d_forcing, c->var, c->tf, c->pi2, c->d_kxr6, c->d_kyr5, c->d_kzr5,
+                          c->stream);
+    if (c->f32)
+      launch_forcing_tables<float>(c->g, c->d_forcing, c->d_kyr5, c->d_kzr5,
+                                   static_cast<float*>(c->rowtab[s]), c->ztab, c->stream);
+    else
+      launch_forcing_tables<double>(c->g, c->d_forcing, c->d_kyr5, c->d_kzr5,
+                                    static_cast<double*>(c->rowtab[s]), c->ztab, c->stream);
+    c->latest = {FM_TABLE, s};
+  } else if (c->cfg.forcing == LBM_FORCING_CONSTANT) {
+    c->latest = {FM_CONST, 0};
+  } else {
+    c->latest = {FM_NONE, 0};
+  }
+}
+
+template <typename T>
+void particle_phase(lbm_ctx* c, T* f_plain) {
+  // beads_lubforce, beads_move, beads_redistribute, beads_links, beads_filling
+  launch_lubforce(c->g, c->npart, c->pp, mstate(c), c->stream);
+  launch_move(c->g, c->npart, c->pp, mstate(c), c->stream);
+  launch_redistribute(c->g, c->npart, c->pp, mstate(c), c->status, c->stream);
+  int nf = 1 - c->fcur;
+  cudaMemsetAsync(c->flags[nf], 0xff, sizeof(int32_t) * c->g.N, c->stream);
+  launch_links(c->g, pview(c), c->flags[nf], c->links, c->status, c->stream);
+  launch_filling<T>(c->g, pview(c), c->pp, c->ypglbp, c->wpp, c->omgpp, c->flags[nf],
+                    c->flags[c->fcur], f_plain, c->stream);
+  c->fcur = nf;
+}
+
+template <typename T>
+void fused_step_t(lbm_ctx* c) {
+  do_forcing(c);
+  T* fin = fbuf<T>(c, c->cur);
+  T* fout = fbuf<T>(c, 1 - c->cur);
+  launch_fused_step<T>(c->g, c->r, fin, fout, c->flags[c->fcur], fview<T>(c, c->fmacro),
+                       fview<T>(c, c->latest), c->stream);
+  if (c->particles_on) {
+    launch_bounce_back<T>(c->g, pview(c), fout, 1, c->flags[c->fcur], c->links, c->fHIp,
+                          c->torqp, c->stream);
+    launch_bounce_scatter<T>(c->g, pview(c), fout, 1, c->links, c->stream);
+    particle_phase<T>(c, fout);
+  }
+  c->cur = 1 - c->cur;
+  c->fmacro = c->latest;
+  c->macro_pending = true;
+  c->macro_derived = true;
+}
+
+// the unfused sequence of main.f90:172-188, used when the stored macro
+// arrays are not macrovar's output of the current populations
+template <typename T>
+void unfused_step_t(lbm_ctx* c) {
+  materialize_macro(c);
+  do_forcing(c);
+  launch_collision<T>(c->g, c->r, fbuf<T>(c, c->cur), c->flags[c->fcur], fview<T>(c, c->latest),
+                      mbuf<T>(c, 0), mbuf<T>(c, 1), mbuf<T>(c, 2), mbuf<T>(c, 3), c->stream);
+  if (c->particles_on) {
+    launch_bounce_back<T>(c->g, pview(c), fbuf<T>(c, c->cur), 0, c->flags[c->fcur], c->links,
+                          c->fHIp, c->torqp, c->stream);
+    launch_bounce_scatter<T>(c->g, pview(c), fbuf<T>(c, c->cur), 0, c->links, c->stream);
+  }
+  launch_streaming<T>(c->g, fbuf<T>(c, c->cur), fbuf<T>(c, 1 - c->cur), c->stream);
+  c->cur = 1 - c->cur;
+  if (c->particles_on) particle_phase<T>(c, fbuf<T>(c, c->cur));
+  c->fmacro = c->latest;
+  c->macro_pending = true;
+  c->macro_derived = true;
+}
+
+int64_t default_link_capacity(double rad) {
+  const double pi = 4.0 * std::atan(1.0);
+  double ro = rad + 2.0, ri = rad > 1.0 ? rad - 1.0 : 0.0;
+  double shell = 4.0 / 3.0 * pi * (ro * ro * ro - ri * ri * ri);
+  int64_t cap = (int64_t)std::ceil(shell * 10.0);
+  if (cap < 256) cap = 256;
+  return (cap + 31) / 32 * 32;
+}
+
+uint64_t footprint(const lbm_config& c, int64_t* cap_out) {
+  uint64_t N = (uint64_t)c.nx * c.ny * c.nz;
+  uint64_t es = c.precision == LBM_PREC_F32 ? 4 : 8;
+  uint64_t b = 0;
+  b += 2 * 19 * N * es;   // populations
+  b += 4 * N * es;        // macro
+  b += 2 * N * 4;         // flags
+  uint64_t np = c.npart_max > 0 ? c.npart_max : 0;
+  int64_t cap = c.link_capacity > 0 ? c.link_capacity : default_link_capacity(c.rad);
+  if (cap_out) *cap_out = cap;
+  b += np * 15 * 3 * 8;
+  b += np * (uint64_t)cap * (4 + 8 + 8) + np * 4;
+  if (c.forcing == LBM_FORCING_STOCHASTIC) {
+    b += 3 * 9ull * c.ny * c.nz * 2 * es + 45ull * c.nz * 2 * 8;
+  }
+  b += 4ull * c.nx * es;
+  uint64_t stage = std::min<uint64_t>(19 * N, kStagingDoubles) * 8;
+  b += stage;
+  return b;
+}
+
+template <typename T>
+int upload_soa_t(lbm_ctx* ctx, const double* h, bool aos) {
+  const long long N = ctx->g.N;
+  T* f = fbuf<T>(ctx, ctx->cur);
+  if (aos) {
+    long long chunk = kStagingDoubles / 19;
+    for (long long n0 = 0; n0 < N; n0 += chunk) {
+      long long nn = std::min(chunk, N - n0);
+      CK(cudaMemcpyAsync(ctx->staging, h + n0 * 19, nn * 19 * sizeof(double),
+                         cudaMemcpyHostToDevice, ctx->stream));
+      launch_aos_to_soa<T>(ctx->g, ctx->staging, f, n0, nn, ctx->stream);
+    }
+  } else if (!ctx->f32) {
+    CK(cudaMemcpyAsync(f, h, 19 * N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  } else {
+    long long total = 19 * N;
+    for (long long o = 0; o < total; o += kStagingDoubles) {
+      long long nn = std::min<long long>(kStagingDoubles, total - o);
+      CK(cudaMemcpyAsync(ctx->staging, h + o, nn * sizeof(double), cudaMemcpyHostToDevice,
+                         ctx->stream));
+      launch_convert<T>(ctx->staging, f + o, nn, ctx->stream);
+    }
+  }
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return 0;
+}
+
+template <typename T>
+int download_soa_t(lbm_ctx* ctx, double* h, bool aos) {
+  const long long N = ctx->g.N;
+  T* f = fbuf<T>(ctx, ctx->cur);
+  if (aos) {
+    long long chunk = kStagingDoubles / 19;
+    for (long long n0 = 0; n0 < N; n0 += chunk) {
+      long long nn = std::min(chunk, N - n0);
+      launch_soa_to_aos<T>(ctx->g, f, ctx->staging, n0, nn, ctx->stream);
+      CK(cudaMemcpyAsync(h + n0 * 19, ctx->staging, nn * 19 * sizeof(double),
+                         cudaMemcpyDeviceToHost, ctx->stream));
+      CK(cudaStreamSynchronize(ctx->stream));
+    }
+  } else if (!ctx->f32) {
+    CK(cudaMemcpyAsync(h, f, 19 * N * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  } else {
+    long long total = 19 * N;
+    for (long long o = 0; o < total; o += kStagingDoubles) {
+      long long nn = std::min<long long>(kStagingDoubles, total - o);
+      launch_convert_back<T>(f + o, ctx->staging, nn, ctx->stream);
+      CK(cudaMemcpyAsync(h + o, ctx->staging, nn * sizeof(double), cudaMemcpyDeviceToHost,
+                         ctx->stream));
+      CK(cudaStreamSynchronize(ctx->stream));
+    }
+  }
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return 0;
+}
+
+// copy a host double array of n values into T device array (via staging)
+template <typename T>
+int h2d_field(lbm_ctx* ctx, const double* h, T* d, long long n) {
+  for (long long o = 0; o < n; o += kStagingDoubles) {
+    long long nn = std::min<long long>(kStagingDoubles, n - o);
+    CK(cudaMemcpyAsync(ctx->staging, h + o, nn * sizeof(double), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    launch_convert<T>(ctx->staging, d + o, nn, ctx->stream);
+  }
+  return 0;
+}
+template <typename T>
+int d2h_field(lbm_ctx* ctx, const T* d, double* h, long long n) {
+  for (long long o = 0; o < n; o += kStagingDoubles) {
+    long long nn = std::min<long long>(kStagingDoubles, n - o);
+    launch_convert_back<T>(d + o, ctx->staging, nn, ctx->stream);
+    CK(cudaMemcpyAsync(h + o, ctx->staging, nn * sizeof(double), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  return 0;
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+int lbm_version(void) { return 1; }
+
+int lbm_config_init(lbm_config* cfg, int preset, int nx, int ny, int nz, int npart, double rad,
+                    double rhopart) {
+  if (!cfg || nx < 4 || ny < 4 || nz < 4 || npart < 0) return LBM_ERR_ARG;
+  std::memset(cfg, 0, sizeof(*cfg));
+  const double pi = 4.0 * std::atan(1.0);
+  cfg->nx = nx; cfg->ny = ny; cfg->nz = nz;
+  cfg->npart_max = npart;
+  cfg->precision = LBM_PREC_F64;
+  cfg->iseedf = 232300;                 // B/para.f90:20
+  cfg->iseedp = 12345;                  // B/para.f90:247
+  cfg->visc = 0.0036;
+  cfg->rho0 = 1.0;
+  cfg->rhopart = rhopart;
+  cfg->rad = rad;
+  cfg->mingap = 2.0;
+  cfg->mingap_w = 2.0;
+  cfg->vscale = 2.037183272e-3;         // B/para.f90:37
+  cfg->stf0 = 0.025; cfg->stf1 = 0.002; // B/para.f90:244-245
+  cfg->stf0_w = 0.025; cfg->stf1_w = 0.002;
+  const double volp = 4.0 / 3.0 * pi * (rad * rad * rad);
+  if (preset == LBM_PRESET_BOX) {
+    cfg->mrt_type = 1;                  // B/para.f90:96
+    cfg->boundary = LBM_BC_PERIODIC;
+    cfg->forcing = LBM_FORCING_STOCHASTIC;
+    const double gscale = 10000.0 / 4.0;  // B/para.f90:237
+    cfg->fpc = volp * cfg->rho0 * 9.8 / gscale;
+    const double rhog = 0.0;              // B/para.f90:239
+    cfg->body_force_y = -(volp * rhog);
+  } else if (preset == LBM_PRESET_CHANNEL) {
+    cfg->mrt_type = 2;                  // C/para.f90:67
+    cfg->boundary = LBM_BC_XWALLS;
+    cfg->forcing = LBM_FORCING_CONSTANT;
+    const double Rstar = 180.0;         // C/para.f90:14-19
+    const double ustar = 2.0 * Rstar * cfg->visc / (double)nx;
+    const double force_in_y = 2. * cfg->rho0 * ustar * ustar / (double)nx;
+    const double ystar = cfg->visc / ustar;
+    const double force_mag = 1.0;
+    cfg->force_y = force_in_y * force_mag;
+    const double g_lbm = ustar * ustar / ystar;
+    cfg->fpc = volp * cfg->rho0 * g_lbm;
+    cfg->body_force_y = volp * force_in_y;  // C/partlib.f90:2409
+  } else {
+    return LBM_ERR_ARG;
+  }
+  return LBM_OK;
+}
+
+int lbm_footprint(const lbm_config* cfg, uint64_t* bytes) {
+  if (!cfg || !bytes) return LBM_ERR_ARG;
+  *bytes = footprint(*cfg, nullptr);
+  return LBM_OK;
+}
+
+const char* lbm_last_error(const lbm_ctx* ctx) {
+  if (!ctx) return "null context";
+  return ctx->err.c_str();
+}
+
+int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
+  if (!cfg || !out) return LBM_ERR_ARG;
+  *out = nullptr;
+  if (cfg->nx < 4 || cfg->ny < 4 || cfg->nz < 4) return LBM_ERR_ARG;
+  if ((long long)cfg->nx * cfg->ny * cfg->nz >= (1LL << 26)) return LBM_ERR_ARG;  // link code
+  if (cfg->precision != LBM_PREC_F64 && cfg->precision != LBM_PREC_F32) return LBM_ERR_ARG;
+  if (cfg->boundary != LBM_BC_PERIODIC && cfg->boundary != LBM_BC_XWALLS) return LBM_ERR_ARG;
+  if (cfg->mrt_type < 1 || cfg->mrt_type > 3) return LBM_ERR_ARG;
+  if (cfg->npart_max > 0 && !(cfg->rad > 0.0)) return LBM_ERR_ARG;
+  if (cfg->forcing == LBM_FORCING_STOCHASTIC && (cfg->ny < 6 || cfg->nz < 6)) return LBM_ERR_ARG;
+  lbm_ctx* ctx = new lbm_ctx();
+  ctx->cfg = *cfg;
+  Geometry& g = ctx->g;
+  g.nx = cfg->nx; g.ny = cfg->ny; g.nz = cfg->nz;
+  g.nxh = g.nx / 2; g.nyh = g.ny / 2; g.nzh = g.nz / 2;
+  g.N = (long long)g.nx * g.ny * g.nz;
+  g.channel = cfg->boundary == LBM_BC_XWALLS;
+  ctx->f32 = cfg->precision == LBM_PREC_F32;
+  ctx->esz = ctx->f32 ? 4 : 8;
+  // MRT rates, B/para.f90:91-135
+  const double tau = 3.0 * cfg->visc + 0.5;
+  Rates& r = ctx->r;
+  if (cfg->mrt_type == 1) { r.omegepsl = 0.0; r.omegepslj = -475.0 / 63.0; r.omegxx = 0.0; }
+  else { r.omegepsl = 3.0; r.omegepslj = -11.0 / 2.0; r.omegxx = -1.0 / 2.0; }
+  r.s9 = 1.0 / tau; r.s13 = r.s9;
+  if (cfg->mrt_type == 1) { r.s1 = 1.19; r.s2 = 1.4; r.s4 = 1.2; r.s10 = 1.4; r.s16 = 1.98; }
+  else if (cfg->mrt_type == 2) { r.s1 = r.s9; r.s2 = r.s9; r.s4 = r.s9; r.s10 = r.s9; r.s16 = r.s9; }
+  else { r.s1 = 1.8; r.s2 = r.s1; r.s4 = r.s9; r.s10 = r.s1; r.s16 = r.s1; }
+  const double pi = 4.0 * std::atan(1.0);
+  const double volp = 4.0 / 3.0 * pi * (cfg->rad * cfg->rad * cfg->rad);
+  PartParams& pp = ctx->pp;
+  pp.rad = cfg->rad; pp.mingap = cfg->mingap; pp.mingap_w = cfg->mingap_w; pp.fpc = cfg->fpc;
+  pp.stf0 = cfg->stf0; pp.stf1 = cfg->stf1; pp.stf0_w = cfg->stf0_w; pp.stf1_w = cfg->stf1_w;
+  pp.body_force_y = cfg->body_force_y;
+  pp.amp = cfg->rhopart * volp;
+  pp.aip = 0.4 * pp.amp * (cfg->rad * cfg->rad);
+  pp.rho0 = cfg->rho0; pp.rhopart = cfg->rhopart;
+  ctx->pi2 = 2.0 * pi;
+  const double tscale = ctx->pi2 * cfg->vscale / (double)g.ny;  // B/para.f90:60
+  ctx->var = 447.31 * ((cfg->vscale * tscale) * (cfg->vscale * tscale));  // gaussian.f90:197
+  ctx->tf = 0.038 / tscale;
+
+  int rc = 0;
+  auto al = [&](void** p, size_t bytes) -> bool {
+    if (rc) return false;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+      rc = fail(ctx, LBM_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+      return false;
+    }
+    return true;
+  };
+  const long long N = g.N;
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return LBM_ERR_CUDA;
+  }
+  ctx->own_stream = true;
+  al(&ctx->f[0], 19 * N * ctx->esz);
+  al(&ctx->f[1], 19 * N * ctx->esz);
+  al(&ctx->macro, 4 * N * ctx->esz);
+  al((void**)&ctx->flags[0], N * sizeof(int32_t));
+  al((void**)&ctx->flags[1], N * sizeof(int32_t));
+  al((void**)&ctx->status, sizeof(DevStatus));
+  al((void**)&ctx->staging, std::min<long long>(19 * N, kStagingDoubles) * sizeof(double));
+  al((void**)&ctx->partial, 4 * 1024 * sizeof(double));
+  al(&ctx->xtw, 4 * g.nx * ctx->esz);
+  if (!rc && cudaMallocHost((void**)&ctx->status_host, sizeof(DevStatus)) != cudaSuccess)
+    rc = fail(ctx, LBM_ERR_NOMEM, "cudaMallocHost");
+  if (!rc && cudaMallocHost((void**)&ctx->partial_host, 4 * 1024 * sizeof(double)) != cudaSuccess)
+    rc = fail(ctx, LBM_ERR_NOMEM, "cudaMallocHost");
+  if (cfg->forcing == LBM_FORCING_STOCHASTIC) {
+    al((void**)&ctx->d_forcing, sizeof(ForcingDev));
+    al((void**)&ctx->d_kxr6, 16 * sizeof(double));
+    al((void**)&ctx->d_kyr5, 8 * sizeof(double));
+    al((void**)&ctx->d_kzr5, 8 * sizeof(double));
+    al((void**)&ctx->ztab, 45LL * g.nz * 2 * sizeof(double));
+    for (int s = 0; s < 3; ++s) al(&ctx->rowtab[s], 9LL * g.ny * g.nz * 2 * ctx->esz);
+  }
+  ctx->npmax = cfg->npart_max > 0 ? cfg->npart_max : 0;
+  if (ctx->npmax > 0) {
+    int64_t cap = cfg->link_capacity > 0 ? cfg->link_capacity : default_link_capacity(cfg->rad);
+    ctx->links.cap = (int)cap;
+    al((void**)&ctx->pbuf, 15ULL * 3 * ctx->npmax * sizeof(double));
+    al((void**)&ctx->first_move, sizeof(int));
+    al((void**)&ctx->links.code, (size_t)ctx->npmax * cap * sizeof(int32_t));
+    al((void**)&ctx->links.alpha, (size_t)ctx->npmax * cap * sizeof(double));
+    al((void**)&ctx->links.f9, (size_t)ctx->npmax * cap * sizeof(double));
+    al((void**)&ctx->links.count, (size_t)ctx->npmax * sizeof(int32_t));
+  }
+  if (rc) {
+    lbm_destroy(ctx);
+    return rc;
+  }
+  if (ctx->npmax > 0) {
+    double* b = ctx->pbuf;
+    size_t v = 3 * (size_t)ctx->npmax;
+    double** vecs[15] = {&ctx->ypglb, &ctx->ypglbp, &ctx->wp, &ctx->wpp, &ctx->omgp,
+                         &ctx->omgpp, &ctx->dwdt, &ctx->domgdt, &ctx->forcep, &ctx->forcepp,
+                         &ctx->torqp, &ctx->torqpp, &ctx->thetap, &ctx->fHIp, &ctx->flubp};
+    for (int i = 0; i < 15; ++i) *vecs[i] = b + i * v;
+    cudaMemsetAsync(ctx->pbuf, 0, 15 * v * sizeof(double), ctx->stream);
+    cudaMemsetAsync(ctx->links.count, 0, ctx->npmax * sizeof(int32_t), ctx->stream);
+    cudaMemsetAsync(ctx->first_move, 0, sizeof(int), ctx->stream);
+  }
+  cudaMemsetAsync(ctx->f[0], 0, 19 * N * ctx->esz, ctx->stream);
+  cudaMemsetAsync(ctx->f[1], 0, 19 * N * ctx->esz, ctx->stream);
+  cudaMemsetAsync(ctx->macro, 0, 4 * N * ctx->esz, ctx->stream);
+  cudaMemsetAsync(ctx->flags[0], 0xff, N * sizeof(int32_t), ctx->stream);
+  cudaMemsetAsync(ctx->flags[1], 0xff, N * sizeof(int32_t), ctx->stream);
+  cudaMemsetAsync(ctx->status, 0, sizeof(DevStatus), ctx->stream);
+  // x twiddles for the forcing: cos/sin of 2 pi kx x / nx, kx = 1, 2
+  {
+    std::vector<double> tw(4 * g.nx);
+    for (int x = 0; x < g.nx; ++x) {
+      for (int kx = 1; kx <= 2; ++kx) {
+        long long m = ((long long)kx * x) % g.nx;
+        double ang = ctx->pi2 * (double)m / (double)g.nx;
+        tw[4 * x + 2 * (kx - 1)] = std::cos(ang);
+        tw[4 * x + 2 * (kx - 1) + 1] = std::sin(ang);
+      }
+    }
+    if (ctx->f32) {
+      std::vector<float> twf(tw.begin(), tw.end());
+      cudaMemcpy(ctx->xtw, twf.data(), twf.size() * sizeof(float), cudaMemcpyHostToDevice);
+    } else {
+      cudaMemcpy(ctx->xtw, tw.data(), tw.size() * sizeof(double), cudaMemcpyHostToDevice);
+    }
+  }
+  if (cfg->forcing == LBM_FORCING_STOCHASTIC) {
+    // wavenumbers of the 6x5x5 block, B/para.f90:260-286; state 281-286
+    double kx6[16] = {0}, ky5[8] = {0}, kz5[8] = {0};
+    for (int i = 1; i <= 6; ++i) kx6[i - 1] = (double)(i / 2);
+    for (int j = 1; j <= 5; ++j) {
+      int jj = (j > 3) ? j + g.ny - 5 : j;
+      ky5[j - 1] = (jj < g.ny / 2 + 2) ? (double)(jj - 1) : (double)(-(g.ny + 1 - jj));
+      int kk = (j > 3) ? j + g.nz - 5 : j;
+      kz5[j - 1] = (kk < g.nz / 2 + 2) ? (double)(kk - 1) : (double)(-(g.nz + 1 - kk));
+    }
+    cudaMemcpy(ctx->d_kxr6, kx6, sizeof kx6, cudaMemcpyHostToDevice);
+    cudaMemcpy(ctx->d_kyr5, ky5, sizeof ky5, cudaMemcpyHostToDevice);
+    cudaMemcpy(ctx->d_kzr5, kz5, sizeof kz5, cudaMemcpyHostToDevice);
+    ForcingDev st;
+    std::memset(&st, 0, sizeof st);
+    st.iseedf = -cfg->iseedf;
+    cudaMemcpy(ctx->d_forcing, &st, sizeof st, cudaMemcpyHostToDevice);
+    ctx->latest = {FM_NONE, 0};
+    ctx->fmacro = {FM_NONE, 0};
+  } else if (cfg->forcing == LBM_FORCING_CONSTANT) {
+    ctx->latest = {FM_CONST, 0};
+    ctx->fmacro = {FM_CONST, 0};
+  }
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    lbm_destroy(ctx);
+    return LBM_ERR_CUDA;
+  }
+  *out = ctx;
+  return LBM_OK;
+}
+
+int lbm_destroy(lbm_ctx* ctx) {
+  if (!ctx) return LBM_OK;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  void* ptrs[] = {ctx->f[0], ctx->f[1], ctx->macro, ctx->flags[0], ctx->flags[1], ctx->status,
+                  ctx->staging, ctx->partial, ctx->xtw, ctx->d_forcing, ctx->d_kxr6,
+                  ctx->d_kyr5, ctx->d_kzr5, ctx->ztab, ctx->rowtab[0], ctx->rowtab[1],
+                  ctx->rowtab[2], ctx->pbuf, ctx->first_move, ctx->links.code,
+                  ctx->links.alpha, ctx->links.f9, ctx->links.count};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (ctx->status_host) cudaFreeHost(ctx->status_host);
+  if (ctx->partial_host) cudaFreeHost(ctx->partial_host);
+  if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return LBM_OK;
+}
+
+int lbm_set_stream(lbm_ctx* ctx, void* stream) {
+  if (!ctx) return LBM_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (stream) {
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    ctx->stream = static_cast<cudaStream_t>(stream);
+    ctx->own_stream = false;
+  }
+  return LBM_OK;
+}
+
+int lbm_synchronize(lbm_ctx* ctx) {
+  if (!ctx) return LBM_ERR_ARG;
+  CK(cudaGetLastError());
+  return check_status(ctx);
+}
+
+int lbm_upload_f(lbm_ctx* ctx, const double* f) {
+  if (!ctx || !f) return LBM_ERR_ARG;
+  int rc = ctx->f32 ? upload_soa_t<float>(ctx, f, true) : upload_soa_t<double>(ctx, f, true);
+  ctx->macro_pending = false;
+  ctx->macro_derived = false;
+  return rc;
+}
+int lbm_download_f(lbm_ctx* ctx, double* f) {
+  if (!ctx || !f) return LBM_ERR_ARG;
+  return ctx->f32 ? download_soa_t<float>(ctx, f, true) : download_soa_t<double>(ctx, f, true);
+}
+int lbm_upload_f_soa(lbm_ctx* ctx, const double* f) {
+  if (!ctx || !f) return LBM_ERR_ARG;
+  int rc = ctx->f32 ? upload_soa_t<float>(ctx, f, false) : upload_soa_t<double>(ctx, f, false);
+  ctx->macro_pending = false;
+  ctx->macro_derived = false;
+  return rc;
+}
+int lbm_download_f_soa(lbm_ctx* ctx, double* f) {
+  if (!ctx || !f) return LBM_ERR_ARG;
+  return ctx->f32 ? download_soa_t<float>(ctx, f, false) : download_soa_t<double>(ctx, f, false);
+}
+
+int lbm_initpop(lbm_ctx* ctx, const double* ux, const double* uy, const double* uz) {
+  if (!ctx || !ux || !uy || !uz) return LBM_ERR_ARG;
+  const long long N = ctx->g.N;
+  double* dv = nullptr;
+  CK(cudaMalloc((void**)&dv, 3 * N * sizeof(double)));
+  cudaMemcpyAsync(dv, ux, N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+  cudaMemcpyAsync(dv + N, uy, N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+  cudaMemcpyAsync(dv + 2 * N, uz, N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+  if (ctx->f32) {
+    launch_initpop<float>(ctx->g, dv, dv + N, dv + 2 * N, fbuf<float>(ctx, ctx->cur),
+                          mbuf<float>(ctx, 0), ctx->stream);
+    for (int c = 0; c < 3; ++c) launch_convert<float>(dv + c * N, mbuf<float>(ctx, 1 + c), N, ctx->stream);
+  } else {
+    launch_initpop<double>(ctx->g, dv, dv + N, dv + 2 * N, fbuf<double>(ctx, ctx->cur),
+                           mbuf<double>(ctx, 0), ctx->stream);
+    cudaMemcpyAsync(mbuf<double>(ctx, 1), dv, 3 * N * sizeof(double), cudaMemcpyDeviceToDevice,
+                    ctx->stream);
+  }
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(dv);
+  if (e != cudaSuccess) return fail(ctx, LBM_ERR_CUDA, cudaGetErrorString(e));
+  CK(cudaGetLastError());
+  ctx->macro_pending = false;
+  ctx->macro_derived = false;
+  return LBM_OK;
+}
+
+int lbm_download_macro(lbm_ctx* ctx, double* rho, double* ux, double* uy, double* uz) {
+  if (!ctx) return LBM_ERR_ARG;
+  materialize_macro(ctx);
+  double* outs[4] = {rho, ux, uy, uz};
+  for (int c = 0; c < 4; ++c) {
+    if (!outs[c]) continue;
+    int rc = ctx->f32 ? d2h_field<float>(ctx, mbuf<float>(ctx, c), outs[c], ctx->g.N)
+                      : d2h_field<double>(ctx, mbuf<double>(ctx, c), outs[c], ctx->g.N);
+    if (rc) return rc;
+  }
+  CK(cudaGetLastError());
+  return LBM_OK;
+}
+
+int lbm_download_force(lbm_ctx* ctx, double* fx, double* fy, double* fz) {
+  if (!ctx || !fx || !fy || !fz) return LBM_ERR_ARG;
+  const long long N = ctx->g.N;
+  double* d = nullptr;
+  CK(cudaMalloc((void**)&d, 3 * N * sizeof(double)));
+  if (ctx->f32)
+    launch_force_field<float>(ctx->g, fview<float>(ctx, ctx->latest), d, d + N, d + 2 * N, ctx->stream);
+  else
+    launch_force_field<double>(ctx->g, fview<double>(ctx, ctx->latest), d, d + N, d + 2 * N, ctx->stream);
+  cudaMemcpyAsync(fx, d, N * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  cudaMemcpyAsync(fy, d + N, N * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  cudaMemcpyAsync(fz, d + 2 * N, N * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(ctx, LBM_ERR_CUDA, cudaGetErrorString(e));
+  return LBM_OK;
+}
+
+int lbm_upload_particles(lbm_ctx* ctx, int npart, const double* ypglb, const double* wp,
+                         const double* omgp) {
+  if (!ctx || npart < 0 || npart > ctx->npmax) return LBM_ERR_ARG;
+  if (npart > 0 && (!ypglb || !wp || !omgp)) return LBM_ERR_ARG;
+  materialize_macro(ctx);
+  size_t v = 3 * (size_t)ctx->npmax;
+  if (ctx->npmax > 0) CK(cudaMemsetAsync(ctx->pbuf, 0, 15 * v * sizeof(double), ctx->stream));
+  ctx->npart = npart;
+  if (npart > 0) {
+    size_t b = 3 * (size_t)npart * sizeof(double);
+    CK(cudaMemcpyAsync(ctx->ypglb, ypglb, b, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->ypglbp, ypglb, b, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->wp, wp, b, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->omgp, omgp, b, cudaMemcpyHostToDevice, ctx->stream));
+    int one = 1;
+    CK(cudaMemcpyAsync(ctx->first_move, &one, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  }
+  CK(cudaMemsetAsync(ctx->flags[0], 0xff, ctx->g.N * sizeof(int32_t), ctx->stream));
+  CK(cudaMemsetAsync(ctx->flags[1], 0xff, ctx->g.N * sizeof(int32_t), ctx->stream));
+  ctx->particles_on = npart > 0;
+  if (npart > 0) launch_links(ctx->g, pview(ctx), ctx->flags[ctx->fcur], ctx->links, ctx->status, ctx->stream);
+  CK(cudaGetLastError());
+  return check_status(ctx);
+}
+
+int lbm_download_particles(lbm_ctx* ctx, double* ypglb, double* wp, double* omgp, double* fHIp,
+                           double* flubp, double* torqp) {
+  if (!ctx) return LBM_ERR_ARG;
+  size_t b = 3 * (size_t)ctx->npart * sizeof(double);
+  if (b == 0) return LBM_OK;
+  double* outs[6] = {ypglb, wp, omgp, fHIp, flubp, torqp};
+  double* srcs[6] = {ctx->ypglb, ctx->wp, ctx->omgp, ctx->fHIp, ctx->flubp, ctx->torqp};
+  for (int i = 0; i < 6; ++i)
+    if (outs[i]) CK(cudaMemcpyAsync(outs[i], srcs[i], b, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return LBM_OK;
+}
+
+int lbm_download_flags(lbm_ctx* ctx, int32_t* ibnodes, int32_t* isnodes) {
+  if (!ctx) return LBM_ERR_ARG;
+  const long long N = ctx->g.N;
+  std::vector<int32_t> tmp;
+  int32_t* dst = isnodes;
+  if (!dst) { tmp.resize(N); dst = tmp.data(); }
+  CK(cudaMemcpyAsync(dst, ctx->flags[ctx->fcur], N * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (ibnodes)
+    for (long long n = 0; n < N; ++n) ibnodes[n] = dst[n] >= 0 ? 1 : -1;
+  return LBM_OK;
+}
+
+int lbm_download_links(lbm_ctx* ctx, int64_t capacity, int64_t* nlinks, int32_t* node,
+                       int32_t* ipop, int32_t* particle, double* alpha) {
+  if (!ctx || !nlinks) return LBM_ERR_ARG;
+  *nlinks = 0;
+  if (ctx->npart <= 0) return LBM_OK;
+  std::vector<int32_t> cnt(ctx->npart);
+  CK(cudaMemcpyAsync(cnt.data(), ctx->links.count, ctx->npart * sizeof(int32_t),
+                     cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  int64_t total = 0;
+  for (int p = 0; p < ctx->npart; ++p) total += cnt[p];
+  *nlinks = total;
+  if (!node && !ipop && !particle && !alpha) return LBM_OK;
+  if (capacity < total) return fail(ctx, LBM_ERR_CAPACITY, "link buffer too small");
+  const int cap = ctx->links.cap;
+  std::vector<int32_t> code((size_t)ctx->npart * cap);
+  std::vector<double> al((size_t)ctx->npart * cap);
+  CK(cudaMemcpyAsync(code.data(), ctx->links.code, code.size() * sizeof(int32_t),
+                     cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(al.data(), ctx->links.alpha, al.size() * sizeof(double),
+                     cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  int64_t w = 0;
+  for (int p = 0; p < ctx->npart; ++p)
+    for (int l = 0; l < cnt[p]; ++l, ++w) {
+      int32_t cd = code[(size_t)p * cap + l];
+      if (node) node[w] = cd >> 5;
+      if (ipop) ipop[w] = cd & 31;
+      if (particle) particle[w] = p;
+      if (alpha) alpha[w] = al[(size_t)p * cap + l];
+    }
+  return LBM_OK;
+}
+
+int lbm_forcing_state(lbm_ctx* ctx, int dir, int32_t* iseedf, int32_t* iyf, int32_t* ivf,
+                      double* b) {
+  if (!ctx) return LBM_ERR_ARG;
+  if (ctx->cfg.forcing != LBM_FORCING_STOCHASTIC) return fail(ctx, LBM_ERR_STATE, "no stochastic forcing");
+  ForcingDev st;
+  CK(cudaMemcpyAsync(&st, ctx->d_forcing, sizeof st, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (dir == 0) {
+    if (iseedf) *iseedf = st.iseedf;
+    if (iyf) *iyf = st.iyf;
+    if (ivf) std::memcpy(ivf, st.ivf, sizeof st.ivf);
+    if (b) std::memcpy(b, st.b, sizeof st.b);
+  } else {
+    if (iseedf) st.iseedf = *iseedf;
+    if (iyf) st.iyf = *iyf;
+    if (ivf) std::memcpy(st.ivf, ivf, sizeof st.ivf);
+    if (b) std::memcpy(st.b, b, sizeof st.b);
+    CK(cudaMemcpyAsync(ctx->d_forcing, &st, sizeof st, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  return LBM_OK;
+}
+
+// ---- per-subroutine entries ----------------------------------------------
+int lbm_forcing(lbm_ctx* ctx) {
+  if (!ctx) return LBM_ERR_ARG;
+  materialize_macro(ctx);
+  do_forcing(ctx);
+  CK(cudaGetLastError());
+  return LBM_OK;
+}
+
+int lbm_collision_mrt(lbm_ctx* ctx) {
+  if (!ctx) return LBM_ERR_ARG;
+  materialize_macro(ctx);
+  if (ctx->f32)
+    launch_collision<float>(ctx->g, ctx->r, fbuf<float>(ctx, ctx->cur), ctx->flags[ctx->fcur],
+                            fview<float>(ctx, ctx->latest), mbuf<float>(ctx, 0), mbuf<float>(ctx, 1),
+                            mbuf<float>(ctx, 2), mbuf<float>(ctx, 3), ctx->stream);
+  else
+    launch_collision<double>(ctx->g, ctx->r, fbuf<double>(ctx, ctx->cur), ctx->flags[ctx->fcur],
+                             fview<double>(ctx, ctx->latest), mbuf<double>(ctx, 0),
+                             mbuf<double>(ctx, 1), mbuf<double>(ctx, 2), mbuf<double>(ctx, 3),
+                             ctx->stream);
+  ctx->macro_derived = false;
+  CK(cudaGetLastError());
+  return LBM_OK;
+}
+
+int lbm_beads_collision(lbm_ctx* ctx) {
+  if (!ctx) return LBM_ERR_ARG;
+  if (!ctx->particles_on) return LBM_OK;
+  materialize_macro(ctx);
+  if (ctx->f32) {
+    launch_bounce_back<float>(ctx->g, pview(ctx), fbuf<float>(ctx, ctx->cur), 0, ctx->flags[ctx->fcur],
+                              ctx->links, ctx->fHIp, ctx->torqp, ctx->stream);
+    launch_bounce_scatter<float>(ctx->g, pview(ctx), fbuf<float>(ctx, ctx->cur), 0, ctx->links, ctx->stream);
+  } else {
+    launch_bounce_back<double>(ctx->g, pview(ctx), fbuf<double>(ctx, ctx->cur), 0, ctx->flags[ctx->fcur],
+                               ctx->links, ctx->fHIp, ctx->torqp, ctx->stream);
+    launch_bounce_scatter<double>(ctx->g, pview(ctx), fbuf<double>(ctx, ctx->cur), 0, ctx->links, ctx->stream);
+  }
+  ctx->macro_derived = false;
+  CK(cudaGetLastError());
+  return LBM_OK;
+}
+
+int lbm_streaming(lbm_ctx* ctx) {
+  if (!ctx) return LBM_ERR_ARG;
+  materialize_macro(ctx);
+  if (ctx->f32)
+    launch_streaming<float>(ctx->g, fbuf<float>(ctx, ctx->cur), fbuf<float>(ctx, 1 - ctx->cur), ctx->stream);
+  else
+    launch_streaming<double>(ctx->g, fbuf<double>(ctx, ctx->cur), fbuf<double>(ctx, 1 - ctx->cur), ctx->stream);
+  ctx->cur = 1 - ctx->cur;
+  ctx->macro_derived = false;
+  CK(cudaGetLastError());
+  return LBM_OK;
+}
+
+int lbm_beads_lubforce(lbm_ctx* ctx) {
+  if (!ctx) return LBM_ERR_ARG;
+  if (!ctx->particles_on) return LBM_OK;
+  launch_lubforce(ctx->g, ctx->npart, ctx->pp, mstate(ctx), ctx->stream);
+  CK(cudaGetLastError());
+  return LBM_OK;
+}
+
+int lbm_beads_move(lbm_ctx* ctx) {
+  if (!ctx) return LBM_ERR_ARG;
+  if (!ctx->particles_on) return LBM_OK;
+  launch_move(ctx->g, ctx->npart, ctx->pp, mstate(ctx), ctx->stream);
+  CK(cudaGetLastError());
+  return LBM_OK;
+}
+
+int lbm_beads_redistribute(lbm_ctx* ctx) {
+  if (!ctx) return LBM_ERR_ARG;
+  if (!ctx->particles_on) return LBM_OK;
+  launch_redistribute(ctx->g, ctx->npart, ctx->pp, mstate(ctx), ctx->status, ctx->stream);
+  CK(cudaGetLastError());
+  return check_status(ctx);
+}
+
+int lbm_beads_links(lbm_ctx* ctx) {
+  if (!ctx) return LBM_ERR_ARG;
+  if (!ctx->particles_on) return LBM_OK;
+  int nf = 1 - ctx->fcur;
+  CK(cudaMemsetAsync(ctx->flags[nf], 0xff, ctx->g.N * sizeof(int32_t), ctx->stream));
+  launch_links(ctx->g, pview(ctx), ctx->flags[nf], ctx->links, ctx->status, ctx->stream);
+  ctx->fcur = nf;
+  CK(cudaGetLastError());
+  return check_status(ctx);
+}
+
+int lbm_beads_filling(lbm_ctx* ctx) {
+  if (!ctx) return LBM_ERR_ARG;
+  if (!ctx->particles_on) return LBM_OK;
+  materialize_macro(ctx);
+  if (ctx->f32)
+    launch_filling<float>(ctx->g, pview(ctx), ctx->pp, ctx->ypglbp, ctx->wpp, ctx->omgpp,
+                          ctx->flags[ctx->fcur], ctx->flags[1 - ctx->fcur],
+                          fbuf<float>(ctx, ctx->cur), ctx->stream);
+  else
+    launch_filling<double>(ctx->g, pview(ctx), ctx->pp, ctx->ypglbp, ctx->wpp, ctx->omgpp,
+                           ctx->flags[ctx->fcur], ctx->flags[1 - ctx->fcur],
+                           fbuf<double>(ctx, ctx->cur), ctx->stream);
+  ctx->macro_derived = false;
+  CK(cudaGetLastError());
+  return LBM_OK;
+}
+
+int lbm_macrovar(lbm_ctx* ctx) {
+  if (!ctx) return LBM_ERR_ARG;
+  ctx->fmacro = ctx->latest;
+  ctx->macro_pending = true;
+  materialize_macro(ctx);
+  CK(cudaGetLastError());
+  return LBM_OK;
+}
+
+int lbm_rhoupdat(lbm_ctx* ctx) {
+  if (!ctx) return LBM_ERR_ARG;
+  materialize_macro(ctx);
+  if (ctx->f32)
+    launch_rhoupdat<float>(ctx->g, fbuf<float>(ctx, ctx->cur), mbuf<float>(ctx, 0), ctx->stream);
+  else
+    launch_rhoupdat<double>(ctx->g, fbuf<double>(ctx, ctx->cur), mbuf<double>(ctx, 0), ctx->stream);
+  ctx->macro_derived = false;
+  CK(cudaGetLastError());
+  return LBM_OK;
+}
+
+int lbm_step(lbm_ctx* ctx, int nsteps) {
+  if (!ctx || nsteps < 0) return LBM_ERR_ARG;
+  for (int s = 0; s < nsteps; ++s) {
+    if (!ctx->macro_derived) {
+      if (ctx->f32) unfused_step_t<float>(ctx); else unfused_step_t<double>(ctx);
+    } else {
+      if (ctx->f32) fused_step_t<float>(ctx); else fused_step_t<double>(ctx);
+    }
+  }
+  CK(cudaGetLastError());
+  if (ctx->particles_on) return check_status(ctx);
+  return LBM_OK;
+}
+
+int lbm_mass_momentum(lbm_ctx* ctx, double out[4]) {
+  if (!ctx || !out) return LBM_ERR_ARG;
+  const int nb = 1024;
+  if (ctx->f32)
+    launch_mass_momentum<float>(ctx->g, fbuf<float>(ctx, ctx->cur), ctx->partial, nb, ctx->stream);
+  else
+    launch_mass_momentum<double>(ctx->g, fbuf<double>(ctx, ctx->cur), ctx->partial, nb, ctx->stream);
+  CK(cudaMemcpyAsync(ctx->partial_host, ctx->partial, 4 * nb * sizeof(double),
+                     cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (int c = 0; c < 4; ++c) out[c] = 0.0;
+  for (int b = 0; b < nb; ++b)
+    for (int c = 0; c < 4; ++c) out[c] += ctx->partial_host[4 * b + c];
+  return LBM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,612 @@
+// lbm_fluid.cu - fluid kernels of the GB300 lattice Boltzmann engine.
+//
+// The hot kernel is k_fused: one pass over the box that, per node,
+//   1. loads the 19 post-streaming populations (coalesced, x fastest),
+//   2. forms rho and u exactly as macrovar does (B/collision.f90:249-271),
+//      with the previous step's body force,
+//   3. evaluates the current step's body force at the node directly from
+//      the low-wavenumber forcing modes (replacing the three inverse FFTs of
+//      FORCING, B/gaussian.f90:595-601),
+//   4. applies the MRT collision with Guo-type forcing of collision_MRT
+//      (B/collision.f90:31-208) at fluid nodes,
+//   5. pushes every population to its neighbour (the cshift streaming of
+//      B/streaming.f90:13-166), bouncing it back at x walls in the channel
+//      (C/streaming.f90:175-187).
+// It reads and writes each population once: 2*19*sizeof(T) bytes per node
+// plus a 4-byte flag.  In FP64 the MRT arithmetic, not HBM, bounds it on
+// GB300, whose FP64 rate is a small fraction of its FP32 rate.
+#include "lbm_internal.cuh"
+
+namespace lbm {
+
+namespace {
+
+template <typename T>
+struct Vec2 { T x, y; };
+
+// MRT collision of one fluid node, B/collision.f90:36-203.  f holds the
+// node's 19 populations on entry and the post-collision populations on
+// exit.  rho9/ux9.. are the macroscopic values of macrovar, fx9.. the body
+// force of the current step.  The arithmetic follows the reference term by
+// term (the compiler may fuse multiply-adds).
+template <typename T>
+__device__ __forceinline__ void collide_mrt(T (&f)[NPOP], T rho9, T ux9, T uy9, T uz9,
+                                            T fx9, T fy9, T fz9, const Rates& r) {
+  const T ww1 = T(1.0 / 18.0), ww2 = T(1.0 / 36.0);
+  const T coef1 = T(-2.0 / 3.0), coef2 = T(-11.0), coef3 = T(8.0), coef4 = T(-4.0), coef5 = T(2.0);
+  const T coef3i = T(1.0 / 8.0), coef4i = T(1.0 / -4.0);
+  const T val1i = T(1.0 / 19.0), val2i = T(1.0 / 2394.0), val3i = T(1.0 / 252.0);
+  const T val4i = T(1.0 / 10.0), val5i = T(1.0 / 40.0), val6i = T(1.0 / 36.0);
+  const T val7i = T(1.0 / 72.0), val8i = T(1.0 / 12.0), val9i = T(1.0 / 24.0), val8 = T(12.0);
+  const T s1 = T(r.s1), s2 = T(r.s2), s4 = T(r.s4), s9 = T(r.s9), s10 = T(r.s10);
+  const T s13 = T(r.s13), s16 = T(r.s16);
+
+  T ux9s = ux9 * ux9, uy9s = uy9 * uy9, uz9s = uz9 * uz9;
+  T G3 = ux9 * fx9 + uy9 * fy9 + uz9 * fz9;
+  T Fbar[NPOP];
+  Fbar[0] = -G3;
+#pragma unroll
+  for (int ip = 1; ip < NPOP; ++ip) {
+    T G1 = T(cix(ip)) * fx9 + T(ciy(ip)) * fy9 + T(ciz(ip)) * fz9;
+    T G2 = T(cix(ip)) * ux9 + T(ciy(ip)) * uy9 + T(ciz(ip)) * uz9;
+    T w = ip <= 6 ? ww1 : ww2;
+    Fbar[ip] = w * (T(3.) * G1 + T(9.) * G1 * G2 - T(3.) * G3);
+  }
+  T f9[NPOP];
+#pragma unroll
+  for (int ip = 0; ip < NPOP; ++ip) f9[ip] = f[ip] + Fbar[ip] / T(2.);
+
+  T t1 = ux9s + uy9s + uz9s;
+  T eqm1 = T(-11.0) * rho9 + T(19.0) * t1;
+  T eqm2 = T(r.omegepsl) * rho9 + T(r.omegepslj) * t1;
+  T eqm3 = coef1 * ux9, eqm4 = coef1 * uy9, eqm5 = coef1 * uz9;
+  T eqm6 = T(2.0) * ux9s - uy9s - uz9s;
+  T eqm7 = T(r.omegxx) * eqm6;
+  T eqm8 = uy9s - uz9s;
+  T eqm9 = T(r.omegxx) * eqm8;
+  T eqm10 = ux9 * uy9, eqm11 = uy9 * uz9, eqm12 = ux9 * uz9;
+
+  T sum1 = f9[1] + f9[2] + f9[3] + f9[4] + f9[5] + f9[6];
+  T sum2 = f9[7] + f9[8] + f9[9] + f9[10] + f9[11] + f9[12] + f9[13] + f9[14] + f9[15] +
+           f9[16] + f9[17] + f9[18];
+  T sum3 = f9[7] - f9[8] + f9[9] - f9[10] + f9[11] - f9[12] + f9[13] - f9[14];
+  T sum4 = f9[7] + f9[8] - f9[9] - f9[10] + f9[15] - f9[16] + f9[17] - f9[18];
+  T sum5 = f9[11] + f9[12] - f9[13] - f9[14] + f9[15] + f9[16] - f9[17] - f9[18];
+  T sum6 = f9[1] + f9[2];
+  T sum7 = f9[3] + f9[4] + f9[5] + f9[6];
+  T sum8 = f9[7] + f9[8] + f9[9] + f9[10] + f9[11] + f9[12] + f9[13] + f9[14];
+  T sum9 = f9[15] + f9[16] + f9[17] + f9[18];
+  T sum10 = f9[3] + f9[4] - f9[5] - f9[6];
+  T sum11 = f9[7] + f9[8] + f9[9] + f9[10] - f9[11] - f9[12] - f9[13] - f9[14];
+
+  T evlm1 = T(-30.0) * f9[0] + coef2 * sum1 + coef3 * sum2;
+  T evlm2 = T(12.0) * f9[0] + coef4 * sum1 + sum2;
+  T evlm3 = coef4 * (f9[1] - f9[2]) + sum3;
+  T evlm4 = coef4 * (f9[3] - f9[4]) + sum4;
+  T evlm5 = coef4 * (f9[5] - f9[6]) + sum5;
+  T evlm6 = coef5 * sum6 - sum7 + sum8 - coef5 * sum9;
+  T evlm7 = coef4 * sum6 + coef5 * sum7 + sum8 - coef5 * sum9;
+  T evlm8 = sum10 + sum11;
+  T evlm9 = -coef5 * sum10 + sum11;
+  T evlm10 = f9[7] - f9[8] - f9[9] + f9[10];
+  T evlm11 = f9[15] - f9[16] - f9[17] + f9[18];
+  T evlm12 = f9[11] - f9[12] - f9[13] + f9[14];
+  T evlm13 = f9[7] - f9[8] + f9[9] - f9[10] - f9[11] + f9[12] - f9[13] + f9[14];
+  T evlm14 = -f9[7] - f9[8] + f9[9] + f9[10] + f9[15] - f9[16] + f9[17] - f9[18];
+  T evlm15 = f9[11] + f9[12] - f9[13] - f9[14] - f9[15] - f9[16] + f9[17] + f9[18];
+
+  T eqmc1 = evlm1 - s1 * (evlm1 - eqm1);
+  T eqmc2 = evlm2 - s2 * (evlm2 - eqm2);
+  T eqmc3 = evlm3 - s4 * (evlm3 - eqm3);
+  T eqmc4 = evlm4 - s4 * (evlm4 - eqm4);
+  T eqmc5 = evlm5 - s4 * (evlm5 - eqm5);
+  T eqmc6 = evlm6 - s9 * (evlm6 - eqm6);
+  T eqmc7 = evlm7 - s10 * (evlm7 - eqm7);
+  T eqmc8 = evlm8 - s9 * (evlm8 - eqm8);
+  T eqmc9 = evlm9 - s10 * (evlm9 - eqm9);
+  T eqmc10 = evlm10 - s13 * (evlm10 - eqm10);
+  T eqmc11 = evlm11 - s13 * (evlm11 - eqm11);
+  T eqmc12 = evlm12 - s13 * (evlm12 - eqm12);
+  T eqmc13 = evlm13 - s16 * evlm13;
+  T eqmc14 = evlm14 - s16 * evlm14;
+  T eqmc15 = evlm15 - s16 * evlm15;
+
+  T tl1 = val1i * rho9;
+  T tl2 = coef2 * val2i * eqmc1;
+  T tl3 = coef3 * val2i * eqmc1;
+  T tl4 = coef4 * val3i * eqmc2;
+  T tl5 = val3i * eqmc2;
+  T tl6 = val4i * ux9;
+  T tl7 = val5i * eqmc3;
+  T tl8 = val4i * uy9;
+  T tl9 = val5i * eqmc4;
+  T tl10 = val4i * uz9;
+  T tl11 = val5i * eqmc5;
+  T tl12 = val6i * eqmc6;
+  T tl13 = val7i * eqmc7;
+  T tl14 = val8i * eqmc8;
+  T tl15 = val9i * eqmc9;
+  T tl16 = -coef4i * eqmc10;
+  T tl17 = -coef4i * eqmc11;
+  T tl18 = -coef4i * eqmc12;
+  T tl19 = coef3i * eqmc13;
+  T tl20 = coef3i * eqmc14;
+  T tl21 = coef3i * eqmc15;
+
+  f9[0] = tl1 - T(30.0) * val2i * eqmc1 + val8 * val3i * eqmc2;
+  T suma = tl1 + tl2 + tl4;
+  T sumb = tl1 + tl3 + tl5;
+  T sumc = tl6 + coef4 * tl7;
+  T sumd = coef5 * tl12 + coef4 * tl13;
+  T sume = tl8 + coef4 * tl9;
+  T sumf = -tl12 + coef5 * tl13 + tl14 - coef5 * tl15;
+  T sumg = tl10 + coef4 * tl11;
+  T sumh = -tl12 + coef5 * tl13 - tl14 + coef5 * tl15;
+  T sumi = tl12 + tl13 + tl14 + tl15;
+  T sumk = tl12 + tl13 - tl14 - tl15;
+  T sump = -coef5 * tl12 - coef5 * tl13;
+  T sum67 = tl6 + tl7, sum89 = tl8 + tl9, sum1011 = tl10 + tl11;
+
+  f9[1] = suma + sumc + sumd;
+  f9[2] = suma - sumc + sumd;
+  f9[3] = suma + sume + sumf;
+  f9[4] = suma - sume + sumf;
+  f9[5] = suma + sumg + sumh;
+  f9[6] = suma - sumg + sumh;
+  f9[7] = sumb + sum67 + sum89 + sumi + tl16 + tl19 - tl20;
+  f9[8] = sumb - sum67 + sum89 + sumi - tl16 - tl19 - tl20;
+  f9[9] = sumb + sum67 - sum89 + sumi - tl16 + tl19 + tl20;
+  f9[10] = sumb - sum67 - sum89 + sumi + tl16 - tl19 + tl20;
+  f9[11] = sumb + sum67 + sum1011 + sumk + tl18 - tl19 + tl21;
+  f9[12] = sumb - sum67 + sum1011 + sumk - tl18 + tl19 + tl21;
+  f9[13] = sumb + sum67 - sum1011 + sumk - tl18 - tl19 - tl21;
+  f9[14] = sumb - sum67 - sum1011 + sumk + tl18 + tl19 - tl21;
+  f9[15] = sumb + sum89 + sum1011 + sump + tl17 + tl20 - tl21;
+  f9[16] = sumb - sum89 + sum1011 + sump - tl17 - tl20 - tl21;
+  f9[17] = sumb + sum89 - sum1011 + sump - tl17 + tl20 + tl21;
+  f9[18] = sumb - sum89 - sum1011 + sump + tl17 - tl20 + tl21;
+
+#pragma unroll
+  for (int ip = 0; ip < NPOP; ++ip) f[ip] = f9[ip] + T(0.5) * Fbar[ip];
+}
+
+// macrovar's fluid-node branch, B/collision.f90:249-271 (u without force)
+template <typename T>
+__device__ __forceinline__ void moments(const T (&f9)[NPOP], T& rho9, T& ux9, T& uy9, T& uz9) {
+  T sum1 = f9[7] - f9[10], sum2 = f9[9] - f9[8];
+  T sum3 = f9[11] - f9[14], sum4 = f9[13] - f9[12];
+  T sum5 = f9[15] - f9[18], sum6 = f9[17] - f9[16];
+  ux9 = f9[1] - f9[2] + sum1 + sum2 + sum3 + sum4;
+  uy9 = f9[3] - f9[4] + sum1 - sum2 + sum5 + sum6;
+  uz9 = f9[5] - f9[6] + sum3 - sum4 + sum5 - sum6;
+  rho9 = f9[0] + f9[1] + f9[2] + f9[3] + f9[4] + f9[5] + f9[6] + f9[7] + f9[8] + f9[9] +
+         f9[10] + f9[11] + f9[12] + f9[13] + f9[14] + f9[15] + f9[16] + f9[17] + f9[18];
+}
+
+// body force at node (x, y, z); see ForceView
+template <typename T>
+__device__ __forceinline__ void body_force(const ForceView<T>& fv, const Geometry& g, int x,
+                                           int y, int z, T& fx, T& fy, T& fz) {
+  if (fv.mode == FM_CONST) { fx = fv.cfx; fy = fv.cfy; fz = fv.cfz; return; }
+  if (fv.mode != FM_TABLE) { fx = T(0); fy = T(0); fz = T(0); return; }
+  const Vec2<T>* tab = reinterpret_cast<const Vec2<T>*>(fv.rowtab);
+  const T c1 = fv.xtw[4 * x], s1 = fv.xtw[4 * x + 1], c2 = fv.xtw[4 * x + 2], s2 = fv.xtw[4 * x + 3];
+  T out[3];
+  const long long plane = (long long)g.nz * g.ny;
+  const long long row = (long long)z * g.ny + y;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    Vec2<T> B0 = tab[(c * 3 + 0) * plane + row];
+    Vec2<T> B1 = tab[(c * 3 + 1) * plane + row];
+    Vec2<T> B2 = tab[(c * 3 + 2) * plane + row];
+    out[c] = B0.x + T(2.0) * (B1.x * c1 - B1.y * s1) + T(2.0) * (B2.x * c2 - B2.y * s2);
+  }
+  fx = out[0]; fy = out[1]; fz = out[2];
+}
+
+__device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+// --------------------------------------------------------------------------
+// fused stream + collide (push).  One thread per node, a block covers part
+// of an x-row; grid (ceil(nx/B), ny, nz).
+template <typename T, bool CHANNEL>
+__global__ void __launch_bounds__(128) k_fused(Geometry g, Rates r, const T* __restrict__ fin,
+                                               T* __restrict__ fout,
+                                               const int32_t* __restrict__ isnodes,
+                                               ForceView<T> fprev, ForceView<T> fnew) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y, z = blockIdx.z;
+  if (x >= g.nx) return;
+  const long long N = g.N;
+  const long long n = x + (long long)g.nx * (y + (long long)g.ny * z);
+  T f[NPOP];
+#pragma unroll
+  for (int q = 0; q < NPOP; ++q) f[q] = fin[q * N + n];
+  if (isnodes[n] < 0) {
+    T rho9, ux9, uy9, uz9, fx, fy, fz;
+    moments(f, rho9, ux9, uy9, uz9);
+    body_force(fprev, g, x, y, z, fx, fy, fz);
+    ux9 = ux9 + fx / T(2.);
+    uy9 = uy9 + fy / T(2.);
+    uz9 = uz9 + fz / T(2.);
+    body_force(fnew, g, x, y, z, fx, fy, fz);
+    collide_mrt(f, rho9, ux9, uy9, uz9, fx, fy, fz, r);
+  }
+  const int xm = x == 0 ? g.nx - 1 : x - 1, xp = x == g.nx - 1 ? 0 : x + 1;
+  const int ym = y == 0 ? g.ny - 1 : y - 1, yp = y == g.ny - 1 ? 0 : y + 1;
+  const int zm = z == 0 ? g.nz - 1 : z - 1, zp = z == g.nz - 1 ? 0 : z + 1;
+#pragma unroll
+  for (int q = 0; q < NPOP; ++q) {
+    int cx = cix(q), cy = ciy(q), cz = ciz(q);
+    if (CHANNEL && ((cx == -1 && x == 0) || (cx == 1 && x == g.nx - 1))) {
+      // halfway bounce-back at the wall: the outgoing population returns
+      // reversed at the same node (C/streaming.f90:175-187)
+      fout[ipopp(q) * N + n] = f[q];
+      continue;
+    }
+    int xd = cx == 0 ? x : (cx > 0 ? xp : xm);
+    int yd = cy == 0 ? y : (cy > 0 ? yp : ym);
+    int zd = cz == 0 ? z : (cz > 0 ? zp : zm);
+    fout[q * N + xd + (long long)g.nx * (yd + (long long)g.ny * zd)] = f[q];
+  }
+}
+
+// streaming alone (per-subroutine entry), B/streaming.f90:2-171
+template <typename T, bool CHANNEL>
+__global__ void k_stream(Geometry g, const T* __restrict__ fin, T* __restrict__ fout) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y, z = blockIdx.z;
+  if (x >= g.nx) return;
+  const long long N = g.N;
+  const long long n = x + (long long)g.nx * (y + (long long)g.ny * z);
+  fout[n] = fin[n];
+#pragma unroll
+  for (int q = 1; q < NPOP; ++q) {
+    int cx = cix(q), cy = ciy(q), cz = ciz(q);
+    T v = fin[q * N + n];
+    if (CHANNEL && ((cx == -1 && x == 0) || (cx == 1 && x == g.nx - 1))) {
+      fout[ipopp(q) * N + n] = v;
+      continue;
+    }
+    int xd = wrapi(x + cx, g.nx), yd = wrapi(y + cy, g.ny), zd = wrapi(z + cz, g.nz);
+    fout[q * N + xd + (long long)g.nx * (yd + (long long)g.ny * zd)] = v;
+  }
+}
+
+// collision_MRT alone (per-subroutine entry), in place, using the stored
+// macroscopic arrays as the reference does
+template <typename T>
+__global__ void k_collision(Geometry g, Rates r, T* __restrict__ f,
+                            const int32_t* __restrict__ isnodes, ForceView<T> fv,
+                            const T* __restrict__ rho, const T* __restrict__ ux,
+                            const T* __restrict__ uy, const T* __restrict__ uz) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y, z = blockIdx.z;
+  if (x >= g.nx) return;
+  const long long N = g.N;
+  const long long n = x + (long long)g.nx * (y + (long long)g.ny * z);
+  if (isnodes[n] >= 0) return;
+  T fl[NPOP];
+#pragma unroll
+  for (int q = 0; q < NPOP; ++q) fl[q] = f[q * N + n];
+  T fx, fy, fz;
+  body_force(fv, g, x, y, z, fx, fy, fz);
+  collide_mrt(fl, rho[n], ux[n], uy[n], uz[n], fx, fy, fz, r);
+#pragma unroll
+  for (int q = 0; q < NPOP; ++q) f[q * N + n] = fl[q];
+}
+
+// macrovar, B/collision.f90:232-332 (solid branch with nearest image; the
+// channel has no x image, C/collision.f90:294-295)
+template <typename T>
+__global__ void k_macrovar(Geometry g, const T* __restrict__ f,
+                           const int32_t* __restrict__ isnodes, ForceView<T> fv,
+                           ParticleView pv, T* __restrict__ rho, T* __restrict__ ux,
+                           T* __restrict__ uy, T* __restrict__ uz) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y, z = blockIdx.z;
+  if (x >= g.nx) return;
+  const long long N = g.N;
+  const long long n = x + (long long)g.nx * (y + (long long)g.ny * z);
+  T fl[NPOP];
+#pragma unroll
+  for (int q = 0; q < NPOP; ++q) fl[q] = f[q * N + n];
+  T rho9, ux9, uy9, uz9, fx, fy, fz;
+  moments(fl, rho9, ux9, uy9, uz9);
+  body_force(fv, g, x, y, z, fx, fy, fz);
+  T u1 = ux9 + fx / T(2.), u2 = uy9 + fy / T(2.), u3 = uz9 + fz / T(2.), rr = rho9;
+  int id = isnodes[n];
+  if (id >= 0 && pv.ypglb != nullptr) {
+    double xpnt = (double)(x + 1) - 0.5, ypnt = (double)(y + 1) - 0.5, zpnt = (double)(z + 1) - 0.5;
+    double xc = pv.ypglb[3 * id], yc = pv.ypglb[3 * id + 1], zc = pv.ypglb[3 * id + 2];
+    if (!g.channel) {
+      if ((xc - xpnt) > (double)g.nxh) xc = xc - (double)g.nx;
+      if ((xc - xpnt) < -(double)g.nxh) xc = xc + (double)g.nx;
+    }
+    if ((yc - ypnt) > (double)g.nyh) yc = yc - (double)g.ny;
+    if ((yc - ypnt) < -(double)g.nyh) yc = yc + (double)g.ny;
+    if ((zc - zpnt) > (double)g.nzh) zc = zc - (double)g.nz;
+    if ((zc - zpnt) < -(double)g.nzh) zc = zc + (double)g.nz;
+    double xx0 = xpnt - xc, yy0 = ypnt - yc, zz0 = zpnt - zc;
+    const double* w = pv.wp + 3 * id;
+    const double* o = pv.omgp + 3 * id;
+    u1 = T(w[0] + (o[1] * zz0 - o[2] * yy0));
+    u2 = T(w[1] + (o[2] * xx0 - o[0] * zz0));
+    u3 = T(w[2] + (o[0] * yy0 - o[1] * xx0));
+    rr = T(pv.rhopart);
+  }
+  rho[n] = rr; ux[n] = u1; uy[n] = u2; uz[n] = u3;
+}
+
+template <typename T>
+__global__ void k_rhoupdat(Geometry g, const T* __restrict__ f, T* __restrict__ rho) {
+  long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (n >= g.N) return;
+  T r = f[n];
+#pragma unroll
+  for (int q = 1; q < NPOP; ++q) r = r + f[q * g.N + n];
+  rho[n] = r;
+}
+
+// initpop, B/initial.f90:14-26 (rho' = 0)
+template <typename T>
+__global__ void k_initpop(Geometry g, const double* __restrict__ ux, const double* __restrict__ uy,
+                          const double* __restrict__ uz, T* __restrict__ f, T* __restrict__ rho) {
+  long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (n >= g.N) return;
+  double u1 = ux[n], u2 = uy[n], u3 = uz[n];
+  double usqr = u1 * u1 + u2 * u2 + u3 * u3;
+  usqr = 1.5 * usqr;
+  const double r0 = 0.0;
+  f[n] = T((1.0 / 3.0) * (r0 - usqr));
+#pragma unroll
+  for (int q = 1; q < NPOP; ++q) {
+    double G = cix(q) * u1 + ciy(q) * u2 + ciz(q) * u3;
+    double w = q <= 6 ? 1.0 / 18.0 : 1.0 / 36.0;
+    f[q * g.N + n] = T(w * (r0 + 3.0 * G + 4.5 * G * G - usqr));
+  }
+  rho[n] = T(0);
+}
+
+// Fortran-order f(0:18, lx, ly, lz) chunk <-> structure of arrays
+template <typename T>
+__global__ void k_aos_to_soa(Geometry g, const double* __restrict__ aos, T* __restrict__ soa,
+                             long long node0, long long nnodes) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= nnodes * NPOP) return;
+  long long nl = t / NPOP;
+  int q = (int)(t - nl * NPOP);
+  soa[q * g.N + node0 + nl] = T(aos[t]);
+}
+template <typename T>
+__global__ void k_soa_to_aos(Geometry g, const T* __restrict__ soa, double* __restrict__ aos,
+                             long long node0, long long nnodes) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= nnodes * NPOP) return;
+  long long nl = t / NPOP;
+  int q = (int)(t - nl * NPOP);
+  aos[t] = (double)soa[q * g.N + node0 + nl];
+}
+template <typename T>
+__global__ void k_convert(const double* __restrict__ in, T* __restrict__ out, long long n) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t < n) out[t] = T(in[t]);
+}
+template <typename T>
+__global__ void k_convert_back(const T* __restrict__ in, double* __restrict__ out, long long n) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t < n) out[t] = (double)in[t];
+}
+
+template <typename T>
+__global__ void k_force_field(Geometry g, ForceView<T> fv, double* fx, double* fy, double* fz) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y, z = blockIdx.z;
+  if (x >= g.nx) return;
+  long long n = x + (long long)g.nx * (y + (long long)g.ny * z);
+  T a, b, c;
+  body_force(fv, g, x, y, z, a, b, c);
+  fx[n] = (double)a; fy[n] = (double)b; fz[n] = (double)c;
+}
+
+// FP64 mass and momentum partial sums, one value set per block
+template <typename T>
+__global__ void k_mass_momentum(Geometry g, const T* __restrict__ f, double* partial) {
+  double m[4] = {0, 0, 0, 0};
+  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < g.N;
+       n += (long long)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int q = 0; q < NPOP; ++q) {
+      double v = (double)f[q * g.N + n];
+      m[0] += v;
+      m[1] += cix(q) * v;
+      m[2] += ciy(q) * v;
+      m[3] += ciz(q) * v;
+    }
+  }
+  __shared__ double sm[4][256];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) sm[c][threadIdx.x] = m[c];
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s)
+      for (int c = 0; c < 4; ++c) sm[c][threadIdx.x] += sm[c][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int c = 0; c < 4; ++c) partial[4 * blockIdx.x + c] = sm[c][0];
+}
+
+// Forcing tables.  Stage 1 (ztab): A(c, kx, jy, z) = sum_kz a(c,kx,jy,kz)
+// exp(+2 pi i kz z / nz); stage 2 (rowtab): B(c, kx, z, y) = sum_jy A
+// exp(+2 pi i ky y / ny).  Together with the per-x twiddles they evaluate
+// the inverse transform of gaussian.f90:557-601 at any node.
+__global__ void k_force_ztab(Geometry g, const ForcingDev* st, const double* kzr5, double* ztab) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;  // over (c, kx, jy, z)
+  int total = 3 * 3 * 5 * g.nz;
+  if (t >= total) return;
+  int z = t % g.nz;
+  int r = t / g.nz;
+  int jy = r % 5; r /= 5;
+  int kx = r % 3;
+  int c = r / 3;
+  const double* a = st->a + 150 * c;
+  double sr = 0.0, si = 0.0;
+  for (int kz = 0; kz < 5; ++kz) {
+    double cr = a[(2 * kx) + 6 * jy + 30 * kz];
+    double ci = a[(2 * kx + 1) + 6 * jy + 30 * kz];
+    long long m = ((long long)kzr5[kz] * z) % g.nz;
+    if (m < 0) m += g.nz;
+    double sn, cs;
+    sincospi(2.0 * (double)m / (double)g.nz, &sn, &cs);
+    sr += cr * cs - ci * sn;
+    si += cr * sn + ci * cs;
+  }
+  ztab[2 * t] = sr;
+  ztab[2 * t + 1] = si;
+}
+
+template <typename T>
+__global__ void k_force_rowtab(Geometry g, const double* __restrict__ ztab,
+                               const double* kyr5, T* __restrict__ rowtab) {
+  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;  // over (c,kx,z,y)
+  long long total = 9LL * g.nz * g.ny;
+  if (t >= total) return;
+  int y = (int)(t % g.ny);
+  long long r = t / g.ny;
+  int z = (int)(r % g.nz);
+  int ckx = (int)(r / g.nz);
+  T sr = T(0), si = T(0);
+  for (int jy = 0; jy < 5; ++jy) {
+    long long ai = ((long long)(ckx * 5 + jy)) * g.nz + z;
+    T ar = T(ztab[2 * ai]), aim = T(ztab[2 * ai + 1]);
+    long long m = ((long long)kyr5[jy] * y) % g.ny;
+    if (m < 0) m += g.ny;
+    double sn, cs;
+    sincospi(2.0 * (double)m / (double)g.ny, &sn, &cs);
+    sr += ar * T(cs) - aim * T(sn);
+    si += ar * T(sn) + aim * T(cs);
+  }
+  rowtab[2 * t] = sr;
+  rowtab[2 * t + 1] = si;
+}
+
+inline dim3 row_grid(const Geometry& g, int bx) { return dim3((g.nx + bx - 1) / bx, g.ny, g.nz); }
+inline unsigned blocks_for(long long n, int b) { return (unsigned)((n + b - 1) / b); }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+template <typename T>
+void launch_fused_step(const Geometry& g, const Rates& r, const T* fin, T* fout,
+                       const int32_t* isnodes, const ForceView<T>& fprev,
+                       const ForceView<T>& fnew, cudaStream_t s) {
+  const int B = 128;
+  if (g.channel)
+    k_fused<T, true><<<row_grid(g, B), B, 0, s>>>(g, r, fin, fout, isnodes, fprev, fnew);
+  else
+    k_fused<T, false><<<row_grid(g, B), B, 0, s>>>(g, r, fin, fout, isnodes, fprev, fnew);
+}
+
+template <typename T>
+void launch_macrovar(const Geometry& g, const T* f, const int32_t* isnodes,
+                     const ForceView<T>& fv, const ParticleView& pv, T* rho, T* ux, T* uy,
+                     T* uz, cudaStream_t s) {
+  k_macrovar<T><<<row_grid(g, 128), 128, 0, s>>>(g, f, isnodes, fv, pv, rho, ux, uy, uz);
+}
+
+template <typename T>
+void launch_collision(const Geometry& g, const Rates& r, T* f, const int32_t* isnodes,
+                      const ForceView<T>& fv, const T* rho, const T* ux, const T* uy,
+                      const T* uz, cudaStream_t s) {
+  k_collision<T><<<row_grid(g, 128), 128, 0, s>>>(g, r, f, isnodes, fv, rho, ux, uy, uz);
+}
+
+template <typename T>
+void launch_streaming(const Geometry& g, const T* fin, T* fout, cudaStream_t s) {
+  if (g.channel)
+    k_stream<T, true><<<row_grid(g, 128), 128, 0, s>>>(g, fin, fout);
+  else
+    k_stream<T, false><<<row_grid(g, 128), 128, 0, s>>>(g, fin, fout);
+}
+
+template <typename T>
+void launch_rhoupdat(const Geometry& g, const T* f, T* rho, cudaStream_t s) {
+  k_rhoupdat<T><<<blocks_for(g.N, 256), 256, 0, s>>>(g, f, rho);
+}
+
+template <typename T>
+void launch_initpop(const Geometry& g, const double* ux, const double* uy, const double* uz,
+                    T* f, T* rho, cudaStream_t s) {
+  k_initpop<T><<<blocks_for(g.N, 256), 256, 0, s>>>(g, ux, uy, uz, f, rho);
+}
+
+template <typename T>
+void launch_aos_to_soa(const Geometry& g, const double* aos, T* soa, long long node0,
+                       long long nnodes, cudaStream_t s) {
+  k_aos_to_soa<T><<<blocks_for(nnodes * NPOP, 256), 256, 0, s>>>(g, aos, soa, node0, nnodes);
+}
+template <typename T>
+void launch_soa_to_aos(const Geometry& g, const T* soa, double* aos, long long node0,
+                       long long nnodes, cudaStream_t s) {
+  k_soa_to_aos<T><<<blocks_for(nnodes * NPOP, 256), 256, 0, s>>>(g, soa, aos, node0, nnodes);
+}
+template <typename T>
+void launch_convert(const double* in, T* out, long long n, cudaStream_t s) {
+  k_convert<T><<<blocks_for(n, 256), 256, 0, s>>>(in, out, n);
+}
+template <typename T>
+void launch_convert_back(const T* in, double* out, long long n, cudaStream_t s) {
+  k_convert_back<T><<<blocks_for(n, 256), 256, 0, s>>>(in, out, n);
+}
+template <typename T>
+void launch_force_field(const Geometry& g, const ForceView<T>& fv, double* fx, double* fy,
+                        double* fz, cudaStream_t s) {
+  k_force_field<T><<<row_grid(g, 128), 128, 0, s>>>(g, fv, fx, fy, fz);
+}
+template <typename T>
+void launch_mass_momentum(const Geometry& g, const T* f, double* partial, int nblocks,
+                          cudaStream_t s) {
+  k_mass_momentum<T><<<nblocks, 256, 0, s>>>(g, f, partial);
+}
+
+template <typename T>
+void launch_forcing_tables(const Geometry& g, const ForcingDev* st, const double* kyr5,
+                           const double* kzr5, T* rowtab, double* ztab, cudaStream_t s) {
+  int nz_t = 45 * g.nz;
+  k_force_ztab<<<blocks_for(nz_t, 128), 128, 0, s>>>(g, st, kzr5, ztab);
+  long long nr = 9LL * g.nz * g.ny;
+  k_force_rowtab<T><<<blocks_for(nr, 256), 256, 0, s>>>(g, ztab, kyr5, rowtab);
+}
+
+#define LBM_INSTANTIATE(T)                                                                   \
+  template void launch_fused_step<T>(const Geometry&, const Rates&, const T*, T*,           \
+                                     const int32_t*, const ForceView<T>&,                   \
+                                     const ForceView<T>&, cudaStream_t);                    \
+  template void launch_macrovar<T>(const Geometry&, const T*, const int32_t*,               \
+                                   const ForceView<T>&, const ParticleView&, T*, T*, T*, T*, \
+                                   cudaStream_t);                                           \
+  template void launch_collision<T>(const Geometry&, const Rates&, T*, const int32_t*,      \
+                                    const ForceView<T>&, const T*, const T*, const T*,      \
+                                    const T*, cudaStream_t);                                \
+  template void launch_streaming<T>(const Geometry&, const T*, T*, cudaStream_t);           \
+  template void launch_rhoupdat<T>(const Geometry&, const T*, T*, cudaStream_t);            \
+  template void launch_initpop<T>(const Geometry&, const double*, const double*,            \
+                                  const double*, T*, T*, cudaStream_t);                     \
+  template void launch_aos_to_soa<T>(const Geometry&, const double*, T*, long long,         \
+                                     long long, cudaStream_t);                              \
+  template void launch_soa_to_aos<T>(const Geometry&, const T*, double*, long long,         \
+                                     long long, cudaStream_t);                              \
+  template void launch_convert<T>(const double*, T*, long long, cudaStream_t);              \
+  template void launch_convert_back<T>(const T*, double*, long long, cudaStream_t);         \
+  template void launch_force_field<T>(const Geometry&, const ForceView<T>&, double*,        \
+                                      double*, double*, cudaStream_t);                      \
+  template void launch_mass_momentum<T>(const Geometry&, const T*, double*, int,            \
+                                        cudaStream_t);                                      \
+  template void launch_forcing_tables<T>(const Geometry&, const ForcingDev*, const double*, \
+                                         const double*, T*, double*, cudaStream_t);
+
+LBM_INSTANTIATE(double)
+LBM_INSTANTIATE(float)
+
+}  // namespace lbm

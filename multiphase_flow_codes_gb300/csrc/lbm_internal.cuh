@@ -1,0 +1,201 @@
+// lbm_internal.cuh - device-side types shared by the engine's CUDA sources.
+//
+// Data layout in HBM (one context = one box):
+//   populations   f[q][z][y][x], q = 0..18, x fastest (structure of arrays),
+//                 double (plain path) or float (shifted FP32 path), two
+//                 buffers (current / next) of 19*N elements each;
+//   node flags    isnodes[z][y][x] int32: particle id (0-based) for solid
+//                 nodes, -1 for fluid; a second buffer keeps the flags of the
+//                 previous step (isnodes0 of the reference);
+//   forcing       for the low-wavenumber forcing, per-row coefficient tables
+//                 rowtab[comp][kx][z][y] (complex) from which the body force
+//                 at any node follows with five FMAs per component, plus a
+//                 per-x twiddle table; two slots (previous, current step);
+//   particles     (3, npart) FP64 vectors as in var_inc, plus per-particle
+//                 link slabs link_code[p][cap] (node*32 + ipop),
+//                 link_alpha[p][cap], link_f9[p][cap] and link_count[p].
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/lbm.h"
+
+namespace lbm {
+
+constexpr int NPOP = 19;
+
+// D3Q19 lattice of the reference, B/para.f90:171-175
+__host__ __device__ constexpr int cix(int q) {
+  return (q == 1 || q == 7 || q == 9 || q == 11 || q == 13) ? 1
+       : (q == 2 || q == 8 || q == 10 || q == 12 || q == 14) ? -1 : 0;
+}
+__host__ __device__ constexpr int ciy(int q) {
+  return (q == 3 || q == 7 || q == 8 || q == 15 || q == 17) ? 1
+       : (q == 4 || q == 9 || q == 10 || q == 16 || q == 18) ? -1 : 0;
+}
+__host__ __device__ constexpr int ciz(int q) {
+  return (q == 5 || q == 11 || q == 12 || q == 15 || q == 16) ? 1
+       : (q == 6 || q == 13 || q == 14 || q == 17 || q == 18) ? -1 : 0;
+}
+// opposite direction (ipopp, B/para.f90:175)
+__host__ __device__ constexpr int ipopp(int q) {
+  return q == 0 ? 0
+       : q <= 6 ? (q % 2 == 1 ? q + 1 : q - 1)
+       : q <= 10 ? 17 - q
+       : q <= 14 ? 25 - q
+       : 33 - q;
+}
+static_assert(ipopp(7) == 10 && ipopp(8) == 9 && ipopp(11) == 14 && ipopp(12) == 13 &&
+              ipopp(15) == 18 && ipopp(16) == 17 && ipopp(1) == 2 && ipopp(6) == 5,
+              "opposite-direction table");
+
+// MRT relaxation rates and constants (B/para.f90:96-169)
+struct Rates {
+  double s1, s2, s4, s9, s10, s13, s16;
+  double omegepsl, omegepslj, omegxx;
+};
+
+// forcing evaluation mode inside the fluid kernels
+enum ForceMode { FM_NONE = 0, FM_TABLE = 1, FM_CONST = 2 };
+
+// Per-row forcing tables: for node (x, y, z) and component c,
+//   F_c = Re B0 + 2 (Re B1 cos(2 pi x/nx) - Im B1 sin(..))
+//             + 2 (Re B2 cos(4 pi x/nx) - Im B2 sin(..)),
+// B_kx = rowtab[((c*3 + kx)*nz + z)*ny + y] (complex).
+template <typename T>
+struct ForceView {
+  int mode;                 // ForceMode
+  const T* rowtab;          // interleaved (re, im), 3*3*nz*ny complex
+  const T* xtw;             // per x: cos1, sin1, cos2, sin2
+  T cfx, cfy, cfz;          // constant force (FM_CONST)
+};
+
+struct Geometry {
+  int nx, ny, nz;
+  int nxh, nyh, nzh;
+  long long N;
+  int channel;
+};
+
+// Particle state on the device, (3, npart_max) FP64 vectors, 0-based ids.
+struct ParticleView {
+  int npart;
+  int cap;                  // link capacity per particle
+  double rad, rhopart;
+  const double* ypglb;
+  const double* wp;
+  const double* omgp;
+};
+
+// device error word values (first error wins)
+struct DevStatus {
+  int code;       // LBM_ERR_* or 0
+  int where;      // kernel-specific detail (particle id, node ...)
+};
+
+__device__ inline void raise_error(DevStatus* st, int code, int where) {
+  if (atomicCAS(&st->code, 0, code) == 0) st->where = where;
+}
+
+}  // namespace lbm
+
+// ---------------------------------------------------------------------------
+// launch wrappers implemented in lbm_fluid.cu / lbm_particles.cu, called by
+// the C ABI layer in lbm_capi.cu
+namespace lbm {
+
+struct Ctx;  // defined in lbm_capi.cu
+
+// fluid
+template <typename T>
+void launch_fused_step(const Geometry& g, const Rates& r, const T* fin, T* fout,
+                       const int32_t* isnodes, const ForceView<T>& fprev,
+                       const ForceView<T>& fnew, cudaStream_t s);
+template <typename T>
+void launch_macrovar(const Geometry& g, const T* f, const int32_t* isnodes,
+                     const ForceView<T>& fv, const ParticleView& pv, T* rho, T* ux,
+                     T* uy, T* uz, cudaStream_t s);
+template <typename T>
+void launch_collision(const Geometry& g, const Rates& r, T* f, const int32_t* isnodes,
+                      const ForceView<T>& fv, const T* rho, const T* ux, const T* uy,
+                      const T* uz, cudaStream_t s);
+template <typename T>
+void launch_streaming(const Geometry& g, const T* fin, T* fout, cudaStream_t s);
+template <typename T>
+void launch_rhoupdat(const Geometry& g, const T* f, T* rho, cudaStream_t s);
+template <typename T>
+void launch_initpop(const Geometry& g, const double* ux, const double* uy,
+                    const double* uz, T* f, T* rho, cudaStream_t s);
+template <typename T>
+void launch_aos_to_soa(const Geometry& g, const double* aos, T* soa, long long node0,
+                       long long nnodes, cudaStream_t s);
+template <typename T>
+void launch_soa_to_aos(const Geometry& g, const T* soa, double* aos, long long node0,
+                       long long nnodes, cudaStream_t s);
+template <typename T>
+void launch_convert(const double* in, T* out, long long n, cudaStream_t s);
+template <typename T>
+void launch_convert_back(const T* in, double* out, long long n, cudaStream_t s);
+template <typename T>
+void launch_force_field(const Geometry& g, const ForceView<T>& fv, double* fx, double* fy,
+                        double* fz, cudaStream_t s);
+template <typename T>
+void launch_mass_momentum(const Geometry& g, const T* f, double* partial, int nblocks,
+                          cudaStream_t s);
+
+// forcing: advance the Ornstein-Uhlenbeck state by one FORCING call and build
+// the per-row tables of the new force field
+struct ForcingDev {
+  int32_t iseedf, iyf, ivf[32];
+  double b[450];   // b1r, b2r, b3r, each (6,5,5)
+  double a[450];   // a1r, a2r, a3r
+};
+void launch_forcing_update(ForcingDev* st, double var, double tf, double pi2,
+                           const double* kxr6, const double* kyr5, const double* kzr5,
+                           cudaStream_t s);
+template <typename T>
+void launch_forcing_tables(const Geometry& g, const ForcingDev* st, const double* kyr5,
+                           const double* kzr5, T* rowtab, double* ztab, cudaStream_t s);
+
+// particles
+struct LinkSlab {
+  int32_t* code;     // node*32 + ipop
+  double* alpha;
+  double* f9;
+  int32_t* count;
+  int cap;
+};
+void launch_links(const Geometry& g, const ParticleView& pv, int32_t* isnodes,
+                  LinkSlab ls, DevStatus* st, cudaStream_t s);
+template <typename T>
+void launch_bounce_back(const Geometry& g, const ParticleView& pv, const T* f,
+                        int pushed_layout, const int32_t* isnodes, LinkSlab ls,
+                        double* fHIp, double* torqp, cudaStream_t s);
+template <typename T>
+void launch_bounce_scatter(const Geometry& g, const ParticleView& pv, T* f,
+                           int pushed_layout, LinkSlab ls, cudaStream_t s);
+struct MoveState {
+  double* ypglb; double* ypglbp; double* ypold;
+  double* wp; double* wpp; double* omgp; double* omgpp;
+  double* dwdt; double* domgdt; double* forcep; double* forcepp;
+  double* torqp; double* torqpp; double* thetap; double* fHIp; double* flubp;
+  int* first_move;  // device flag, cleared after the first beads_move
+};
+struct PartParams {
+  double rad, mingap, mingap_w, fpc, stf0, stf1, stf0_w, stf1_w;
+  double body_force_y, amp, aip, rho0, rhopart;
+};
+void launch_lubforce(const Geometry& g, int npart, const PartParams& pp, MoveState ms,
+                     cudaStream_t s);
+void launch_move(const Geometry& g, int npart, const PartParams& pp, MoveState ms,
+                 cudaStream_t s);
+void launch_redistribute(const Geometry& g, int npart, const PartParams& pp, MoveState ms,
+                         DevStatus* st, cudaStream_t s);
+template <typename T>
+void launch_filling(const Geometry& g, const ParticleView& pv, const PartParams& pp,
+                    const double* ypglbp, const double* wpp, const double* omgpp,
+                    const int32_t* isnodes, const int32_t* isnodes0, T* f,
+                    cudaStream_t s);
+
+}  // namespace lbm

@@ -1,0 +1,229 @@
+"""Host-side mirror of the reference's per-step call surface.
+
+``LBMBox`` wraps one ``lbm_ctx`` (one box on one GPU).  Its methods carry
+the names of the Fortran subroutines that the reference main loop calls
+(3DBox_Forced_HI_Turbulence_Moving_Particles_LBM/main.f90:172-188), each
+leaving the device state as that subroutine leaves var_inc's arrays:
+
+    FORCING  collision_MRT  beads_collision  streaming  beads_lubforce
+    beads_move  beads_redistribute  beads_links  beads_filling  macrovar
+
+``step(n)`` runs that whole sequence ``n`` times through the fused GPU
+path.  Errors that stop the reference (particle overlap, for instance)
+raise ``LBMError`` instead.
+
+Array conventions (numpy):
+  populations  ``(19, nz, ny, nx)`` float64 (structure of arrays); the
+               reference's own ``f(0:18, lx, ly, lz)`` is available through
+               ``get_f_fortran`` / ``set_f_fortran``
+  node fields  ``(nz, ny, nx)``
+  particles    ``(npart, 3)`` float64 (= the reference's ``(3, npart)``)
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _capi as capi
+from ._capi import LBMError, dptr, iptr
+
+
+class LBMBox:
+    def __init__(self, cfg: capi.lbm_config):
+        self.cfg = cfg
+        self.nx, self.ny, self.nz = cfg.nx, cfg.ny, cfg.nz
+        self.N = self.nx * self.ny * self.nz
+        self._L = capi.lib()
+        h = C.c_void_p()
+        rc = self._L.lbm_create(C.byref(cfg), C.byref(h))
+        if rc != capi.LBM_OK:
+            raise LBMError(rc, "lbm_create failed (is a CUDA device present?)")
+        self._h = h
+        self.npart = 0
+
+    # ---- lifetime ------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.lbm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def _ck(self, rc: int, what: str):
+        if rc != capi.LBM_OK:
+            msg = self._L.lbm_last_error(self._h)
+            raise LBMError(rc, f"{what}: {msg.decode() if msg else ''}")
+
+    def synchronize(self):
+        self._ck(self._L.lbm_synchronize(self._h), "lbm_synchronize")
+
+    # ---- populations -----------------------------------------------------
+    def set_f(self, f: np.ndarray):
+        f = np.ascontiguousarray(f, dtype=np.float64).reshape(19, self.nz, self.ny, self.nx)
+        self._ck(self._L.lbm_upload_f_soa(self._h, dptr(f)), "upload_f")
+
+    def get_f(self) -> np.ndarray:
+        out = np.empty((19, self.nz, self.ny, self.nx), dtype=np.float64)
+        self._ck(self._L.lbm_download_f_soa(self._h, dptr(out)), "download_f")
+        return out
+
+    def set_f_fortran(self, f: np.ndarray):
+        """f(0:18, lx, ly, lz) as the reference stores it (population fastest)."""
+        f = np.asfortranarray(f, dtype=np.float64)
+        assert f.shape == (19, self.nx, self.ny, self.nz)
+        self._ck(self._L.lbm_upload_f(self._h, dptr(f)), "upload_f")
+
+    def get_f_fortran(self) -> np.ndarray:
+        out = np.empty((19, self.nx, self.ny, self.nz), dtype=np.float64, order="F")
+        self._ck(self._L.lbm_download_f(self._h, dptr(out)), "download_f")
+        return out
+
+    def initpop(self, ux: np.ndarray, uy: np.ndarray, uz: np.ndarray):
+        """initpop (initial.f90:3-28) from a (nz, ny, nx) velocity field."""
+        a = [np.ascontiguousarray(u, dtype=np.float64).reshape(self.nz, self.ny, self.nx)
+             for u in (ux, uy, uz)]
+        self._ck(self._L.lbm_initpop(self._h, dptr(a[0]), dptr(a[1]), dptr(a[2])), "initpop")
+
+    def get_macro(self):
+        """(rho, ux, uy, uz) as left by the last macrovar, each (nz, ny, nx)."""
+        out = [np.empty((self.nz, self.ny, self.nx)) for _ in range(4)]
+        self._ck(self._L.lbm_download_macro(self._h, *map(dptr, out)), "download_macro")
+        return tuple(out)
+
+    def get_force(self):
+        out = [np.empty((self.nz, self.ny, self.nx)) for _ in range(3)]
+        self._ck(self._L.lbm_download_force(self._h, *map(dptr, out)), "download_force")
+        return tuple(out)
+
+    def mass_momentum(self) -> np.ndarray:
+        out = np.zeros(4)
+        self._ck(self._L.lbm_mass_momentum(self._h, dptr(out)), "mass_momentum")
+        return out
+
+    # ---- particles -------------------------------------------------------
+    def release_particles(self, ypglb: np.ndarray, wp: np.ndarray | None = None,
+                          omgp: np.ndarray | None = None):
+        y = np.ascontiguousarray(ypglb, dtype=np.float64).reshape(-1, 3)
+        n = y.shape[0]
+        w = np.zeros_like(y) if wp is None else np.ascontiguousarray(wp, dtype=np.float64).reshape(n, 3)
+        o = np.zeros_like(y) if omgp is None else np.ascontiguousarray(omgp, dtype=np.float64).reshape(n, 3)
+        self._ck(self._L.lbm_upload_particles(self._h, n, dptr(y), dptr(w), dptr(o)),
+                 "upload_particles")
+        self.npart = n
+
+    def get_particles(self) -> dict:
+        n = max(self.npart, 0)
+        arrs = {k: np.zeros((n, 3)) for k in ("ypglb", "wp", "omgp", "fHIp", "flubp", "torqp")}
+        if n:
+            self._ck(self._L.lbm_download_particles(
+                self._h, *(dptr(arrs[k]) for k in ("ypglb", "wp", "omgp", "fHIp", "flubp", "torqp"))),
+                "download_particles")
+        return arrs
+
+    def get_flags(self):
+        ib = np.empty((self.nz, self.ny, self.nx), dtype=np.int32)
+        isn = np.empty((self.nz, self.ny, self.nx), dtype=np.int32)
+        self._ck(self._L.lbm_download_flags(self._h, iptr(ib), iptr(isn)), "download_flags")
+        return ib, isn
+
+    def get_links(self):
+        """(node, ipop, particle, alpha) of every boundary link."""
+        n = C.c_int64(0)
+        self._ck(self._L.lbm_download_links(self._h, 0, C.byref(n), None, None, None, None), "links")
+        m = int(n.value)
+        node = np.empty(m, dtype=np.int32)
+        ipop = np.empty(m, dtype=np.int32)
+        part = np.empty(m, dtype=np.int32)
+        alpha = np.empty(m, dtype=np.float64)
+        if m:
+            self._ck(self._L.lbm_download_links(self._h, m, C.byref(n), iptr(node), iptr(ipop),
+                                                iptr(part), dptr(alpha)), "links")
+        return node, ipop, part, alpha
+
+    # ---- forcing state ---------------------------------------------------
+    def get_forcing_state(self):
+        iseed = C.c_int32(0)
+        iy = C.c_int32(0)
+        iv = np.zeros(32, dtype=np.int32)
+        b = np.zeros(450)
+        self._ck(self._L.lbm_forcing_state(self._h, 0, C.byref(iseed), C.byref(iy), iptr(iv), dptr(b)),
+                 "forcing_state")
+        return int(iseed.value), int(iy.value), iv, b
+
+    def set_forcing_state(self, iseedf: int, iyf: int, ivf: np.ndarray, b: np.ndarray):
+        iseed = C.c_int32(iseedf)
+        iy = C.c_int32(iyf)
+        iv = np.ascontiguousarray(ivf, dtype=np.int32)
+        bb = np.ascontiguousarray(b, dtype=np.float64)
+        self._ck(self._L.lbm_forcing_state(self._h, 1, C.byref(iseed), C.byref(iy), iptr(iv), dptr(bb)),
+                 "forcing_state")
+
+    # ---- the reference's subroutines ----------------------------------------
+    def FORCING(self):
+        self._ck(self._L.lbm_forcing(self._h), "FORCING")
+
+    def collision_MRT(self):
+        self._ck(self._L.lbm_collision_mrt(self._h), "collision_MRT")
+
+    def beads_collision(self):
+        self._ck(self._L.lbm_beads_collision(self._h), "beads_collision")
+
+    def streaming(self):
+        self._ck(self._L.lbm_streaming(self._h), "streaming")
+
+    def beads_lubforce(self):
+        self._ck(self._L.lbm_beads_lubforce(self._h), "beads_lubforce")
+
+    def beads_move(self):
+        self._ck(self._L.lbm_beads_move(self._h), "beads_move")
+
+    def beads_redistribute(self):
+        self._ck(self._L.lbm_beads_redistribute(self._h), "beads_redistribute")
+
+    def beads_links(self):
+        self._ck(self._L.lbm_beads_links(self._h), "beads_links")
+
+    def beads_filling(self):
+        self._ck(self._L.lbm_beads_filling(self._h), "beads_filling")
+
+    def macrovar(self):
+        self._ck(self._L.lbm_macrovar(self._h), "macrovar")
+
+    def rhoupdat(self):
+        self._ck(self._L.lbm_rhoupdat(self._h), "rhoupdat")
+
+    def step(self, nsteps: int = 1):
+        """The time step of main.f90:172-188, ``nsteps`` times (fused path)."""
+        self._ck(self._L.lbm_step(self._h, int(nsteps)), "step")
+
+    def step_unfused(self, nsteps: int = 1):
+        """The same sequence, one reference subroutine per call."""
+        for _ in range(nsteps):
+            self.FORCING()
+            self.collision_MRT()
+            if self.npart:
+                self.beads_collision()
+            self.streaming()
+            if self.npart:
+                self.beads_lubforce()
+                self.beads_move()
+                self.beads_redistribute()
+                self.beads_links()
+                self.beads_filling()
+            self.macrovar()

@@ -1,0 +1,170 @@
+"""CPU oracle: ctypes wrapper of the C++ restatement in lbm_oracle.cpp.
+
+TEST INFRASTRUCTURE ONLY.  The parity tests, ``__graft_entry__.smoke()`` and
+the CPU-baseline leg of ``bench.py`` use it as the checker; the engine never
+calls it.
+
+Parity unpinned: the reference (Fortran + MPI + FFTW 2) cannot be compiled
+or run in this environment and ships no golden vectors, so this restatement
+is validated by invariants, independent restatements and hand-derived cases
+(see tests/), not against the reference's own output.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "liblbm_oracle.so"
+
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    src = HERE / "lbm_oracle.cpp"
+    hdr = HERE.parent / "include" / "lbm.h"
+    if force or not LIB.exists() or LIB.stat().st_mtime < max(src.stat().st_mtime, hdr.stat().st_mtime):
+        subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return LIB
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(LIB))
+        P = C.c_void_p
+        L.orc_create.restype = P
+        L.orc_create.argtypes = [C.c_void_p]
+        L.orc_destroy.argtypes = [P]
+        L.orc_field.restype = P
+        L.orc_field.argtypes = [P, C.c_char_p]
+        for name in ("orc_forcing", "orc_collision_mrt", "orc_beads_collision", "orc_streaming",
+                     "orc_beads_lubforce", "orc_beads_move", "orc_beads_links", "orc_beads_filling",
+                     "orc_macrovar", "orc_rhoupdat", "orc_initpop"):
+            getattr(L, name).argtypes = [P]
+            getattr(L, name).restype = None
+        L.orc_beads_redistribute.argtypes = [P]
+        L.orc_beads_redistribute.restype = C.c_int
+        L.orc_error.argtypes = [P]
+        L.orc_npart.argtypes = [P]
+        L.orc_initpartpos.argtypes = [P, C.c_int]
+        L.orc_release.argtypes = [P, C.c_int]
+        L.orc_release.restype = None
+        L.orc_step.argtypes = [P, C.c_int]
+        L.orc_ran1_sequence.argtypes = [C.c_int32, C.c_int, C.POINTER(C.c_double)]
+        L.orc_ran1_sequence.restype = None
+        _lib = L
+    return _lib
+
+
+def ran1_sequence(seed: int, n: int) -> np.ndarray:
+    out = np.empty(n)
+    lib().orc_ran1_sequence(seed, n, out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out
+
+
+class OracleBox:
+    """The reference's var_inc state on the CPU, with its subroutines.
+
+    Node arrays are (nz, ny, nx) views, populations (19, nz, ny, nx),
+    dense link arrays (18, nz, ny, nx) (ilink(ipop) at index ipop-1),
+    particle vectors (npart_max, 3).  Views alias the C++ state."""
+
+    NODE = ("rho", "ux", "uy", "uz", "fx", "fy", "fz")
+    INODE = ("ibnodes", "isnodes", "ibnodes0", "isnodes0")
+    PART = ("ypglb", "ypglbp", "wp", "wpp", "omgp", "omgpp", "dwdt", "domgdt", "forcep",
+            "forcepp", "torqp", "torqpp", "thetap", "fHIp", "flubp")
+
+    def __init__(self, cfg):
+        self._cfg = cfg
+        self.nx, self.ny, self.nz = cfg.nx, cfg.ny, cfg.nz
+        self._L = lib()
+        self._h = self._L.orc_create(C.addressof(cfg))
+        self.npmax = max(cfg.npart_max, 0)
+
+    def close(self):
+        if self._h:
+            self._L.orc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _view(self, name: str, dtype, shape):
+        p = self._L.orc_field(self._h, name.encode())
+        if not p:
+            raise KeyError(name)
+        n = int(np.prod(shape))
+        ct = C.c_double if dtype == np.float64 else C.c_int32
+        arr = np.ctypeslib.as_array((ct * n).from_address(p))
+        return arr.reshape(shape)
+
+    def __getattr__(self, name):
+        if name.startswith("_"):
+            raise AttributeError(name)
+        sh = (self.nz, self.ny, self.nx)
+        if name == "f":
+            return self._view("f", np.float64, (19,) + sh)
+        if name in self.NODE:
+            return self._view(name, np.float64, sh)
+        if name in self.INODE:
+            return self._view(name, np.int32, sh)
+        if name in ("ilink", "mlink"):
+            return self._view(name, np.int32, (18,) + sh)
+        if name == "alink":
+            return self._view(name, np.float64, (18,) + sh)
+        if name in self.PART:
+            return self._view(name, np.float64, (self.npmax, 3))
+        if name in ("b1r", "b2r", "b3r", "a1r", "a2r", "a3r"):
+            return self._view(name, np.float64, (150,))
+        if name == "ivf":
+            return self._view(name, np.int32, (32,))
+        if name in ("iseedf", "iyf"):
+            return int(self._view(name, np.int32, (1,))[0])
+        raise AttributeError(name)
+
+    @property
+    def error(self) -> int:
+        return self._L.orc_error(self._h)
+
+    # reference subroutines
+    def FORCING(self): self._L.orc_forcing(self._h)
+    def collision_MRT(self): self._L.orc_collision_mrt(self._h)
+    def beads_collision(self): self._L.orc_beads_collision(self._h)
+    def streaming(self): self._L.orc_streaming(self._h)
+    def beads_lubforce(self): self._L.orc_beads_lubforce(self._h)
+    def beads_move(self): self._L.orc_beads_move(self._h)
+    def beads_redistribute(self) -> int: return self._L.orc_beads_redistribute(self._h)
+    def beads_links(self): self._L.orc_beads_links(self._h)
+    def beads_filling(self): self._L.orc_beads_filling(self._h)
+    def macrovar(self): self._L.orc_macrovar(self._h)
+    def rhoupdat(self): self._L.orc_rhoupdat(self._h)
+
+    def initpop(self, ux, uy, uz):
+        self.ux[...] = ux
+        self.uy[...] = uy
+        self.uz[...] = uz
+        self._L.orc_initpop(self._h)
+
+    def initpartpos(self, npart: int) -> int:
+        return self._L.orc_initpartpos(self._h, npart)
+
+    def release_particles(self, ypglb, wp=None, omgp=None):
+        y = np.asarray(ypglb, dtype=np.float64).reshape(-1, 3)
+        n = y.shape[0]
+        self.ypglb[:n] = y
+        self.wp[:n] = 0.0 if wp is None else wp
+        self.omgp[:n] = 0.0 if omgp is None else omgp
+        self._L.orc_release(self._h, n)
+
+    def step(self, nsteps: int = 1) -> int:
+        return self._L.orc_step(self._h, nsteps)

@@ -1,0 +1,196 @@
+"""GPU parity: the CUDA engine (through the C ABI) against the CPU oracle.
+
+Tolerances, as the path's contract states them:
+  * integer work (solid flags, link sets, link fractions as computed
+    geometry) must match bit for bit;
+  * FP64 populations, macroscopic fields and particle state within 1e-12
+    (max-norm relative) over 10 steps;
+  * FP32-shifted populations within 1e-5 of the FP64 oracle over 10 steps.
+"""
+
+import numpy as np
+import pytest
+
+from conftest import gpu_links, oracle_links, relerr
+
+from multiphase_flow_codes_gb300 import _capi as capi
+from multiphase_flow_codes_gb300 import inputs
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL32 = 1e-5
+
+
+def make_pair(oracle_mod, preset=capi.LBM_PRESET_BOX, shape=(32, 32, 32), npart=0, rad=4.5,
+              rhopart=5.0, urms=0.03, k0=4.0, precision=capi.LBM_PREC_F64, wp=None, omgp=None,
+              mrt_type=None):
+    from multiphase_flow_codes_gb300.engine import LBMBox
+    nx, ny, nz = shape
+    cfg = capi.config_init(preset, nx, ny, nz, npart, rad, rhopart)
+    if mrt_type is not None:
+        cfg.mrt_type = mrt_type
+    cfg.precision = precision
+    o = oracle_mod.OracleBox(cfg)
+    if urms > 0:
+        u = inputs.spectral_velocity(nx, k0, urms, ny=ny, nz=nz)
+    else:
+        u = tuple(np.zeros((nz, ny, nx)) for _ in range(3))
+    o.initpop(*u)
+    o.macrovar()
+    box = LBMBox(cfg)
+    box.set_f(o.f.copy())
+    box.macrovar()
+    if npart:
+        chan = preset == capi.LBM_PRESET_CHANNEL
+        y = inputs.initpartpos(nx, ny, nz, npart, rad, channel=chan)
+        o.release_particles(y, wp, omgp)
+        box.release_particles(y, wp, omgp)
+    return o, box
+
+
+def check_links(o, box):
+    po, no, qo, ao = oracle_links(o)
+    pg, ng, qg, ag = gpu_links(box)
+    assert len(po) == len(pg), (len(po), len(pg))
+    assert np.array_equal(po, pg) and np.array_equal(no, ng) and np.array_equal(qo, qg)
+    assert np.array_equal(ao, ag), np.abs(ao - ag).max()
+
+
+def check_flags(o, box):
+    ib, isn = box.get_flags()
+    assert np.array_equal(ib, o.ibnodes)
+    assert np.array_equal(isn, o.isnodes)
+
+
+def test_fused_periodic_no_particles(require_gpu, oracle_mod):
+    o, box = make_pair(oracle_mod)
+    for s in range(10):
+        o.step(1)
+        box.step(1)
+    assert relerr(box.get_f(), o.f) <= TOL64
+    rho, ux, uy, uz = box.get_macro()
+    assert relerr(ux, o.ux) <= TOL64 and relerr(uy, o.uy) <= TOL64 and relerr(uz, o.uz) <= TOL64
+    fx, fy, fz = box.get_force()
+    assert relerr(fx, o.fx) <= TOL64 and relerr(fz, o.fz) <= TOL64
+
+
+def test_forcing_state_matches(require_gpu, oracle_mod):
+    o, box = make_pair(oracle_mod, shape=(16, 16, 16))
+    for _ in range(3):
+        o.FORCING()
+        box.FORCING()
+    iseed, iy, iv, b = box.get_forcing_state()
+    assert iseed == o.iseedf and iy == o.iyf
+    assert np.array_equal(iv, o.ivf)
+    bo = np.concatenate([o.b1r, o.b2r, o.b3r])
+    assert relerr(b, bo) <= 1e-14
+
+
+def test_unfused_subroutines_match(require_gpu, oracle_mod):
+    o, box = make_pair(oracle_mod, shape=(24, 20, 16), npart=2, rad=3.5)
+    for s in range(4):
+        o.step(1)
+        box.step_unfused(1)
+        check_flags(o, box)
+    assert relerr(box.get_f(), o.f) <= TOL64
+
+
+def test_links_bit_exact_at_release(require_gpu, oracle_mod):
+    o, box = make_pair(oracle_mod, shape=(48, 48, 48), npart=12, rad=4.5)
+    check_flags(o, box)
+    check_links(o, box)
+
+
+def test_links_wrapping_particles(require_gpu, oracle_mod):
+    """Spheres straddling the periodic faces and corners."""
+    from multiphase_flow_codes_gb300.engine import LBMBox
+    cfg = capi.config_init(capi.LBM_PRESET_BOX, 32, 32, 32, 3, 4.5, 5.0)
+    o = oracle_mod.OracleBox(cfg)
+    box = LBMBox(cfg)
+    y = np.array([[0.3, 31.9, 15.2], [16.1, 0.05, 31.7], [31.99, 16.5, 0.4]])
+    o.release_particles(y)
+    box.release_particles(y)
+    check_flags(o, box)
+    check_links(o, box)
+
+
+def test_particles_config0_geometry_10_steps(require_gpu, oracle_mod):
+    """The 64^3, 16-sphere (R = 4.5, density ratio 5) workload, 10 steps."""
+    o, box = make_pair(oracle_mod, shape=(64, 64, 64), npart=16, rad=4.5, rhopart=5.0)
+    for s in range(10):
+        o.step(1)
+        box.step(1)
+        check_flags(o, box)
+        p = box.get_particles()
+        assert relerr(p["ypglb"], o.ypglb) <= TOL64
+        assert relerr(p["fHIp"], o.fHIp) <= 1e-10
+    assert relerr(box.get_f(), o.f) <= TOL64
+    check_links(o, box)
+
+
+def test_moving_particles_refill(require_gpu, oracle_mod):
+    """Spheres launched with translation and spin so that nodes are
+    uncovered and refilled every step."""
+    rng = np.random.default_rng(7)
+    wp = rng.uniform(-0.08, 0.08, (6, 3))
+    om = rng.uniform(-0.01, 0.01, (6, 3))
+    o, box = make_pair(oracle_mod, shape=(40, 40, 40), npart=6, rad=4.0, rhopart=2.5, wp=wp, omgp=om)
+    refilled = 0
+    for s in range(10):
+        before = o.ibnodes.copy()
+        o.step(1)
+        box.step(1)
+        refilled += int(((before > 0) & (o.ibnodes < 0)).sum())
+        check_flags(o, box)
+        assert relerr(box.get_f(), o.f) <= TOL64
+    assert refilled > 0
+    p = box.get_particles()
+    assert relerr(p["ypglb"], o.ypglb) <= TOL64
+    assert relerr(p["omgp"], o.omgp) <= 1e-10
+    check_links(o, box)
+
+
+def test_channel_particles(require_gpu, oracle_mod):
+    rng = np.random.default_rng(3)
+    wp = rng.uniform(-0.05, 0.05, (4, 3))
+    o, box = make_pair(oracle_mod, preset=capi.LBM_PRESET_CHANNEL, shape=(30, 36, 28), npart=4,
+                       rad=4.0, rhopart=1.0, wp=wp)
+    check_links(o, box)
+    for s in range(10):
+        o.step(1)
+        box.step(1)
+        check_flags(o, box)
+    assert relerr(box.get_f(), o.f) <= TOL64
+    p = box.get_particles()
+    assert relerr(p["flubp"], o.flubp) <= 1e-10 or np.abs(o.flubp).max() == 0
+
+
+def test_fp32_shifted_close_to_fp64(require_gpu, oracle_mod):
+    o, box = make_pair(oracle_mod, shape=(32, 32, 32), npart=4, rad=4.0, rhopart=2.5,
+                       precision=capi.LBM_PREC_F32)
+    for s in range(10):
+        o.step(1)
+        box.step(1)
+    assert relerr(box.get_f(), o.f) <= TOL32
+    p = box.get_particles()
+    assert relerr(p["fHIp"], o.fHIp) <= 1e-4
+
+
+def test_fortran_layout_roundtrip(require_gpu, oracle_mod):
+    o, box = make_pair(oracle_mod, shape=(12, 10, 8))
+    ff = box.get_f_fortran()
+    assert np.array_equal(np.transpose(ff, (0, 3, 2, 1)), o.f)
+    box.set_f_fortran(ff * 0.5)
+    assert np.array_equal(box.get_f(), o.f * 0.5)
+
+
+def test_mass_momentum(require_gpu, oracle_mod):
+    o, box = make_pair(oracle_mod, shape=(16, 16, 16))
+    box.step(3)
+    f = box.get_f()
+    mm = box.mass_momentum()
+    from conftest import CIX, CIY, CIZ
+    ref = [f.sum(), np.tensordot(CIX, f, axes=(0, 0)).sum(), np.tensordot(CIY, f, axes=(0, 0)).sum(),
+           np.tensordot(CIZ, f, axes=(0, 0)).sum()]
+    assert np.allclose(mm, ref, atol=1e-12)
