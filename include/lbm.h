@@ -178,6 +178,25 @@ int lbm_step(lbm_ctx* ctx, int nsteps);
  * sum c f. */
 int lbm_mass_momentum(lbm_ctx* ctx, double out[4]);
 
+/* Device time per phase of the time step, from CUDA events recorded on the
+ * context's stream around each phase.  enable = 1 clears the totals and
+ * starts recording, 0 stops.  Phases (LBM_PHASE_*): */
+enum {
+  LBM_PHASE_STREAM_COLLIDE = 0, /* fused stream + MRT collide (or the unfused kernels) */
+  LBM_PHASE_BOUNCE = 1,         /* beads_collision: bounce-back + stores              */
+  LBM_PHASE_PARTICLES = 2,      /* beads_lubforce, beads_move, beads_redistribute     */
+  LBM_PHASE_LINKS = 3,          /* beads_links (flag reset + link build)              */
+  LBM_PHASE_FILLING = 4,        /* beads_filling                                      */
+  LBM_PHASE_FORCING = 5,        /* FORCING (state update + force tables)              */
+  LBM_NPHASES = 6
+};
+int lbm_profile(lbm_ctx* ctx, int enable);
+/* total milliseconds and number of timed intervals of one phase since the
+ * last lbm_profile(ctx, 1); synchronises the context's stream */
+int lbm_profile_read(lbm_ctx* ctx, int phase, double* ms_total, int64_t* count);
+/* number of kernels this library has launched in this process */
+int64_t lbm_kernel_launches(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -99,7 +99,12 @@ SIGNATURES = {
     "lbm_rhoupdat": (C.c_int, [_P]),
     "lbm_step": (C.c_int, [_P, C.c_int]),
     "lbm_mass_momentum": (C.c_int, [_P, _D]),
+    "lbm_profile": (C.c_int, [_P, C.c_int]),
+    "lbm_profile_read": (C.c_int, [_P, C.c_int, _D, C.POINTER(C.c_int64)]),
+    "lbm_kernel_launches": (C.c_int64, []),
 }
+
+PHASES = ("stream_collide", "bounce", "particles", "links", "filling", "forcing")
 
 
 def lib() -> C.CDLL:

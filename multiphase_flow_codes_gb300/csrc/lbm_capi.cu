@@ -7,6 +7,8 @@
 // step as: forcing update -> fused collide+stream -> bounce-back ->
 // particle update -> links -> refill, and leaves macrovar's output to be
 // materialised lazily (only when something reads it).
+#include <atomic>
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -18,6 +20,8 @@
 using namespace lbm;
 
 namespace {
+
+std::atomic<long long> g_launches{0};
 
 constexpr int kStagingDoubles = 1 << 25;  // 256 MB chunk for host transfers
 
@@ -37,6 +41,13 @@ struct lbm_ctx {
   size_t esz = 8;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  // next step's FORCING, launched early on a side stream (see do_forcing)
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_main = nullptr, ev_forcing = nullptr, ev_status = nullptr;
+  bool prefetched = false;
+  int prefetch_slot = 0;
+  ForcingDev* d_forcing_backup = nullptr;
+  bool status_pending = false;
   std::string err;
 
   void* f[2] = {nullptr, nullptr};
@@ -53,6 +64,8 @@ struct lbm_ctx {
   double* d_kyr5 = nullptr;
   double* d_kzr5 = nullptr;
   double* ztab = nullptr;
+  double* ytw = nullptr;  // (cos, sin) of 2 pi ky y / ny, [5][ny]
+  double* ztw = nullptr;  // (cos, sin) of 2 pi kz z / nz, [5][nz]
   void* rowtab[3] = {nullptr, nullptr, nullptr};
   void* xtw = nullptr;
   ForceState latest{FM_NONE, 0}, fmacro{FM_NONE, 0};
@@ -66,13 +79,26 @@ struct lbm_ctx {
       *torqpp, *thetap, *fHIp, *flubp;
   int* first_move = nullptr;
   LinkSlab links{};
+  FillList fill{};
 
   DevStatus* status = nullptr;
   DevStatus* status_host = nullptr;
   double* staging = nullptr;
   double* partial = nullptr;
   double* partial_host = nullptr;
+
+  // per-phase timing (lbm_profile)
+  bool prof_on = false;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  struct Interval { int phase; size_t e0, e1; };
+  std::vector<Interval> intervals;
+  size_t open_ev = 0;
 };
+
+namespace lbm {
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+}
 
 namespace {
 
@@ -87,6 +113,26 @@ int fail(lbm_ctx* c, int code, const std::string& m) {
     if (e_ != cudaSuccess)                                                             \
       return fail(ctx, LBM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
+
+cudaEvent_t next_event(lbm_ctx* c, size_t* idx) {
+  if (c->ev_used == c->ev_pool.size()) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    c->ev_pool.push_back(e);
+  }
+  *idx = c->ev_used;
+  return c->ev_pool[c->ev_used++];
+}
+void prof_begin(lbm_ctx* c) {
+  if (!c->prof_on) return;
+  cudaEventRecord(next_event(c, &c->open_ev), c->stream);
+}
+void prof_end(lbm_ctx* c, int phase) {
+  if (!c->prof_on) return;
+  size_t e1;
+  cudaEventRecord(next_event(c, &e1), c->stream);
+  c->intervals.push_back({phase, c->open_ev, e1});
+}
 
 ParticleView pview(lbm_ctx* c) {
   ParticleView v;
@@ -138,6 +184,7 @@ int check_status(lbm_ctx* ctx) {
     const char* what = s.code == LBM_ERR_OVERLAP    ? "particles overlap after a move"
                        : s.code == LBM_ERR_CAPACITY ? "link or geometry capacity exceeded"
                        : s.code == LBM_ERR_STATE    ? "particle image sweep not at a fixed point"
+                       : s.code == LBM_ERR_NONFINITE ? "non-finite particle centre"
                                                     : "device error";
     snprintf(buf, sizeof buf, "%s (particle %d)", what, s.where);
     return fail(ctx, s.code, buf);
@@ -167,19 +214,32 @@ int pick_slot(lbm_ctx* c) {
   return 0;
 }
 
-// FORCING: advance the stochastic state and tabulate the new field
+void launch_forcing_into(lbm_ctx* c, int slot, cudaStream_t st) {
+  launch_forcing_update(c->d_forcing, c->var, c->tf, c->pi2, c->d_kxr6, c->d_kyr5, c->d_kzr5, st);
+  if (c->f32)
+    launch_forcing_tables<float>(c->g, c->d_forcing, c->ytw, c->ztw,
+                                 static_cast<float*>(c->rowtab[slot]), c->ztab, st);
+  else
+    launch_forcing_tables<double>(c->g, c->d_forcing, c->ytw, c->ztw,
+                                  static_cast<double*>(c->rowtab[slot]), c->ztab, st);
+}
+
+// FORCING: advance the stochastic state and tabulate the new field.  If the
+// previous lbm_step already launched this call on the side stream, it is
+// consumed here (the main stream waits for it).
 void do_forcing(lbm_ctx* c) {
   if (c->cfg.forcing == LBM_FORCING_STOCHASTIC) {
+    if (c->prefetched) {
+      cudaStreamWaitEvent(c->stream, c->ev_forcing, 0);
+      c->latest = {FM_TABLE, c->prefetch_slot};
+      c->prefetched = false;
+      return;
+    }
+    prof_begin(c);
     int s = pick_slot(c);
-    launch_forcing_update(c->d_forcing, c->var, c->tf, c->pi2, c->d_kxr6, c->d_kyr5, c->d_kzr5,
-                          c->stream);
-    if (c->f32)
-      launch_forcing_tables<float>(c->g, c->d_forcing, c->d_kyr5, c->d_kzr5,
-                                   static_cast<float*>(c->rowtab[s]), c->ztab, c->stream);
-    else
-      launch_forcing_tables<double>(c->g, c->d_forcing, c->d_kyr5, c->d_kzr5,
-                                    static_cast<double*>(c->rowtab[s]), c->ztab, c->stream);
+    launch_forcing_into(c, s, c->stream);
     c->latest = {FM_TABLE, s};
+    prof_end(c, LBM_PHASE_FORCING);
   } else if (c->cfg.forcing == LBM_FORCING_CONSTANT) {
     c->latest = {FM_CONST, 0};
   } else {
@@ -187,17 +247,59 @@ void do_forcing(lbm_ctx* c) {
   }
 }
 
+// Launch the next step's FORCING on the side stream once the fused kernel
+// just enqueued (the last reader of the table slot it overwrites) is done;
+// it then overlaps the particle kernels of the current step.  The forcing
+// state is backed up first so that cancel_prefetch can undo it.
+void prefetch_forcing(lbm_ctx* c) {
+  if (c->cfg.forcing != LBM_FORCING_STOCHASTIC || c->prefetched) return;
+  int slot = 0;
+  for (int s = 0; s < 3; ++s)
+    if (s != c->latest.slot) { slot = s; break; }
+  cudaEventRecord(c->ev_main, c->stream);
+  cudaStreamWaitEvent(c->side, c->ev_main, 0);
+  cudaMemcpyAsync(c->d_forcing_backup, c->d_forcing, sizeof(ForcingDev), cudaMemcpyDeviceToDevice,
+                  c->side);
+  if (c->prof_on) {
+    size_t e0, e1;
+    cudaEventRecord(next_event(c, &e0), c->side);
+    launch_forcing_into(c, slot, c->side);
+    cudaEventRecord(next_event(c, &e1), c->side);
+    c->intervals.push_back({LBM_PHASE_FORCING, e0, e1});
+  } else {
+    launch_forcing_into(c, slot, c->side);
+  }
+  cudaEventRecord(c->ev_forcing, c->side);
+  c->prefetched = true;
+  c->prefetch_slot = slot;
+}
+
+// Undo a prefetched FORCING (restore the generator and OU state).
+void cancel_prefetch(lbm_ctx* c) {
+  if (!c->prefetched) return;
+  cudaStreamWaitEvent(c->stream, c->ev_forcing, 0);
+  cudaMemcpyAsync(c->d_forcing, c->d_forcing_backup, sizeof(ForcingDev), cudaMemcpyDeviceToDevice,
+                  c->stream);
+  c->prefetched = false;
+}
+
 template <typename T>
 void particle_phase(lbm_ctx* c, T* f_plain) {
   // beads_lubforce, beads_move, beads_redistribute, beads_links, beads_filling
+  prof_begin(c);
   launch_lubforce(c->g, c->npart, c->pp, mstate(c), c->stream);
   launch_move(c->g, c->npart, c->pp, mstate(c), c->stream);
   launch_redistribute(c->g, c->npart, c->pp, mstate(c), c->status, c->stream);
+  prof_end(c, LBM_PHASE_PARTICLES);
   int nf = 1 - c->fcur;
+  prof_begin(c);
   cudaMemsetAsync(c->flags[nf], 0xff, sizeof(int32_t) * c->g.N, c->stream);
-  launch_links(c->g, pview(c), c->flags[nf], c->links, c->status, c->stream);
+  launch_links(c->g, pview(c), c->flags[nf], c->links, c->status, c->f32, c->stream);
+  prof_end(c, LBM_PHASE_LINKS);
+  prof_begin(c);
   launch_filling<T>(c->g, pview(c), c->pp, c->ypglbp, c->wpp, c->omgpp, c->flags[nf],
-                    c->flags[c->fcur], f_plain, c->stream);
+                    c->flags[c->fcur], f_plain, c->fill, c->status, c->stream);
+  prof_end(c, LBM_PHASE_FILLING);
   c->fcur = nf;
 }
 
@@ -206,12 +308,17 @@ void fused_step_t(lbm_ctx* c) {
   do_forcing(c);
   T* fin = fbuf<T>(c, c->cur);
   T* fout = fbuf<T>(c, 1 - c->cur);
+  prof_begin(c);
   launch_fused_step<T>(c->g, c->r, fin, fout, c->flags[c->fcur], fview<T>(c, c->fmacro),
                        fview<T>(c, c->latest), c->stream);
+  prof_end(c, LBM_PHASE_STREAM_COLLIDE);
+  prefetch_forcing(c);
   if (c->particles_on) {
+    prof_begin(c);
     launch_bounce_back<T>(c->g, pview(c), fout, 1, c->flags[c->fcur], c->links, c->fHIp,
                           c->torqp, c->stream);
     launch_bounce_scatter<T>(c->g, pview(c), fout, 1, c->links, c->stream);
+    prof_end(c, LBM_PHASE_BOUNCE);
     particle_phase<T>(c, fout);
   }
   c->cur = 1 - c->cur;
@@ -475,6 +582,13 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
     return LBM_ERR_CUDA;
   }
   ctx->own_stream = true;
+  if (cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_main, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_forcing, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_status, cudaEventDisableTiming) != cudaSuccess) {
+    lbm_destroy(ctx);
+    return LBM_ERR_CUDA;
+  }
   al(&ctx->f[0], 19 * N * ctx->esz);
   al(&ctx->f[1], 19 * N * ctx->esz);
   al(&ctx->macro, 4 * N * ctx->esz);
@@ -490,10 +604,13 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
     rc = fail(ctx, LBM_ERR_NOMEM, "cudaMallocHost");
   if (cfg->forcing == LBM_FORCING_STOCHASTIC) {
     al((void**)&ctx->d_forcing, sizeof(ForcingDev));
+    al((void**)&ctx->d_forcing_backup, sizeof(ForcingDev));
     al((void**)&ctx->d_kxr6, 16 * sizeof(double));
     al((void**)&ctx->d_kyr5, 8 * sizeof(double));
     al((void**)&ctx->d_kzr5, 8 * sizeof(double));
     al((void**)&ctx->ztab, 45LL * g.nz * 2 * sizeof(double));
+    al((void**)&ctx->ytw, 5LL * g.ny * 2 * sizeof(double));
+    al((void**)&ctx->ztw, 5LL * g.nz * 2 * sizeof(double));
     for (int s = 0; s < 3; ++s) al(&ctx->rowtab[s], 9LL * g.ny * g.nz * 2 * ctx->esz);
   }
   ctx->npmax = cfg->npart_max > 0 ? cfg->npart_max : 0;
@@ -506,6 +623,10 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
     al((void**)&ctx->links.alpha, (size_t)ctx->npmax * cap * sizeof(double));
     al((void**)&ctx->links.f9, (size_t)ctx->npmax * cap * sizeof(double));
     al((void**)&ctx->links.count, (size_t)ctx->npmax * sizeof(int32_t));
+    ctx->fill.cap = std::max(4096, 256 * ctx->npmax);
+    al((void**)&ctx->fill.node, (size_t)ctx->fill.cap * sizeof(int32_t));
+    al((void**)&ctx->fill.part, (size_t)ctx->fill.cap * sizeof(int32_t));
+    al((void**)&ctx->fill.count, sizeof(int32_t));
   }
   if (rc) {
     lbm_destroy(ctx);
@@ -549,7 +670,8 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
   if (cfg->forcing == LBM_FORCING_STOCHASTIC) {
     // wavenumbers of the 6x5x5 block, B/para.f90:260-286; state 281-286
     double kx6[16] = {0}, ky5[8] = {0}, kz5[8] = {0};
-    for (int i = 1; i <= 6; ++i) kx6[i - 1] = (double)(i / 2);
+    // kxr(i) = int(i/2) for odd i and kxr(i+1) = kxr(i): 0, 0, 1, 1, 2, 2
+    for (int i = 1; i <= 6; ++i) kx6[i - 1] = (double)((i - 1) / 2);
     for (int j = 1; j <= 5; ++j) {
       int jj = (j > 3) ? j + g.ny - 5 : j;
       ky5[j - 1] = (jj < g.ny / 2 + 2) ? (double)(jj - 1) : (double)(-(g.ny + 1 - jj));
@@ -559,6 +681,20 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
     cudaMemcpy(ctx->d_kxr6, kx6, sizeof kx6, cudaMemcpyHostToDevice);
     cudaMemcpy(ctx->d_kyr5, ky5, sizeof ky5, cudaMemcpyHostToDevice);
     cudaMemcpy(ctx->d_kzr5, kz5, sizeof kz5, cudaMemcpyHostToDevice);
+    auto twid = [&](const double* k5, int n, double* dst) {
+      std::vector<double> t(10 * (size_t)n);
+      for (int j = 0; j < 5; ++j)
+        for (int x = 0; x < n; ++x) {
+          long long m = ((long long)k5[j] * x) % n;
+          if (m < 0) m += n;
+          double ang = ctx->pi2 * (double)m / (double)n;
+          t[2 * ((size_t)j * n + x)] = std::cos(ang);
+          t[2 * ((size_t)j * n + x) + 1] = std::sin(ang);
+        }
+      cudaMemcpy(dst, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice);
+    };
+    twid(ky5, g.ny, ctx->ytw);
+    twid(kz5, g.nz, ctx->ztw);
     ForcingDev st;
     std::memset(&st, 0, sizeof st);
     st.iseedf = -cfg->iseedf;
@@ -582,23 +718,32 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
 int lbm_destroy(lbm_ctx* ctx) {
   if (!ctx) return LBM_OK;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->side) cudaStreamSynchronize(ctx->side);
   void* ptrs[] = {ctx->f[0], ctx->f[1], ctx->macro, ctx->flags[0], ctx->flags[1], ctx->status,
                   ctx->staging, ctx->partial, ctx->xtw, ctx->d_forcing, ctx->d_kxr6,
-                  ctx->d_kyr5, ctx->d_kzr5, ctx->ztab, ctx->rowtab[0], ctx->rowtab[1],
+                  ctx->d_kyr5, ctx->d_kzr5, ctx->ztab, ctx->ytw, ctx->ztw, ctx->d_forcing_backup,
+                  ctx->rowtab[0], ctx->rowtab[1],
                   ctx->rowtab[2], ctx->pbuf, ctx->first_move, ctx->links.code,
-                  ctx->links.alpha, ctx->links.f9, ctx->links.count};
+                  ctx->links.alpha, ctx->links.f9, ctx->links.count, ctx->fill.node,
+                  ctx->fill.part, ctx->fill.count};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
   if (ctx->status_host) cudaFreeHost(ctx->status_host);
   if (ctx->partial_host) cudaFreeHost(ctx->partial_host);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->side) cudaStreamDestroy(ctx->side);
+  for (cudaEvent_t e : {ctx->ev_main, ctx->ev_forcing, ctx->ev_status})
+    if (e) cudaEventDestroy(e);
   delete ctx;
   return LBM_OK;
 }
 
 int lbm_set_stream(lbm_ctx* ctx, void* stream) {
   if (!ctx) return LBM_ERR_ARG;
+  cancel_prefetch(ctx);
   CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaStreamSynchronize(ctx->side));
   if (stream) {
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
     ctx->stream = static_cast<cudaStream_t>(stream);
@@ -610,6 +755,8 @@ int lbm_set_stream(lbm_ctx* ctx, void* stream) {
 int lbm_synchronize(lbm_ctx* ctx) {
   if (!ctx) return LBM_ERR_ARG;
   CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->side));
+  ctx->status_pending = false;
   return check_status(ctx);
 }
 
@@ -715,7 +862,7 @@ int lbm_upload_particles(lbm_ctx* ctx, int npart, const double* ypglb, const dou
   CK(cudaMemsetAsync(ctx->flags[0], 0xff, ctx->g.N * sizeof(int32_t), ctx->stream));
   CK(cudaMemsetAsync(ctx->flags[1], 0xff, ctx->g.N * sizeof(int32_t), ctx->stream));
   ctx->particles_on = npart > 0;
-  if (npart > 0) launch_links(ctx->g, pview(ctx), ctx->flags[ctx->fcur], ctx->links, ctx->status, ctx->stream);
+  if (npart > 0) launch_links(ctx->g, pview(ctx), ctx->flags[ctx->fcur], ctx->links, ctx->status, ctx->f32, ctx->stream);
   CK(cudaGetLastError());
   return check_status(ctx);
 }
@@ -776,7 +923,9 @@ int lbm_download_links(lbm_ctx* ctx, int64_t capacity, int64_t* nlinks, int32_t*
       if (node) node[w] = cd >> 5;
       if (ipop) ipop[w] = cd & 31;
       if (particle) particle[w] = p;
-      if (alpha) alpha[w] = al[(size_t)p * cap + l];
+      if (alpha)
+        alpha[w] = ctx->f32 ? (double)reinterpret_cast<const float*>(&al[(size_t)p * cap])[l]
+                            : al[(size_t)p * cap + l];
     }
   return LBM_OK;
 }
@@ -784,6 +933,7 @@ int lbm_download_links(lbm_ctx* ctx, int64_t capacity, int64_t* nlinks, int32_t*
 int lbm_forcing_state(lbm_ctx* ctx, int dir, int32_t* iseedf, int32_t* iyf, int32_t* ivf,
                       double* b) {
   if (!ctx) return LBM_ERR_ARG;
+  cancel_prefetch(ctx);
   if (ctx->cfg.forcing != LBM_FORCING_STOCHASTIC) return fail(ctx, LBM_ERR_STATE, "no stochastic forcing");
   ForcingDev st;
   CK(cudaMemcpyAsync(&st, ctx->d_forcing, sizeof st, cudaMemcpyDeviceToHost, ctx->stream));
@@ -890,7 +1040,7 @@ int lbm_beads_links(lbm_ctx* ctx) {
   if (!ctx->particles_on) return LBM_OK;
   int nf = 1 - ctx->fcur;
   CK(cudaMemsetAsync(ctx->flags[nf], 0xff, ctx->g.N * sizeof(int32_t), ctx->stream));
-  launch_links(ctx->g, pview(ctx), ctx->flags[nf], ctx->links, ctx->status, ctx->stream);
+  launch_links(ctx->g, pview(ctx), ctx->flags[nf], ctx->links, ctx->status, ctx->f32, ctx->stream);
   ctx->fcur = nf;
   CK(cudaGetLastError());
   return check_status(ctx);
@@ -903,11 +1053,11 @@ int lbm_beads_filling(lbm_ctx* ctx) {
   if (ctx->f32)
     launch_filling<float>(ctx->g, pview(ctx), ctx->pp, ctx->ypglbp, ctx->wpp, ctx->omgpp,
                           ctx->flags[ctx->fcur], ctx->flags[1 - ctx->fcur],
-                          fbuf<float>(ctx, ctx->cur), ctx->stream);
+                          fbuf<float>(ctx, ctx->cur), ctx->fill, ctx->status, ctx->stream);
   else
     launch_filling<double>(ctx->g, pview(ctx), ctx->pp, ctx->ypglbp, ctx->wpp, ctx->omgpp,
                            ctx->flags[ctx->fcur], ctx->flags[1 - ctx->fcur],
-                           fbuf<double>(ctx, ctx->cur), ctx->stream);
+                           fbuf<double>(ctx, ctx->cur), ctx->fill, ctx->status, ctx->stream);
   ctx->macro_derived = false;
   CK(cudaGetLastError());
   return LBM_OK;
@@ -934,8 +1084,19 @@ int lbm_rhoupdat(lbm_ctx* ctx) {
   return LBM_OK;
 }
 
+// Report a device error raised by an earlier lbm_step without blocking:
+// the status word is copied back asynchronously at the end of each call.
+int poll_status(lbm_ctx* ctx) {
+  if (!ctx->status_pending) return 0;
+  if (cudaEventQuery(ctx->ev_status) != cudaSuccess) return 0;
+  ctx->status_pending = false;
+  if (ctx->status_host->code == 0) return 0;
+  return check_status(ctx);
+}
+
 int lbm_step(lbm_ctx* ctx, int nsteps) {
   if (!ctx || nsteps < 0) return LBM_ERR_ARG;
+  if (int rc = poll_status(ctx)) return rc;
   for (int s = 0; s < nsteps; ++s) {
     if (!ctx->macro_derived) {
       if (ctx->f32) unfused_step_t<float>(ctx); else unfused_step_t<double>(ctx);
@@ -944,9 +1105,44 @@ int lbm_step(lbm_ctx* ctx, int nsteps) {
     }
   }
   CK(cudaGetLastError());
-  if (ctx->particles_on) return check_status(ctx);
+  if (ctx->particles_on) {
+    CK(cudaMemcpyAsync(ctx->status_host, ctx->status, sizeof(DevStatus), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaEventRecord(ctx->ev_status, ctx->stream));
+    ctx->status_pending = true;
+  }
   return LBM_OK;
 }
+
+int lbm_profile(lbm_ctx* ctx, int enable) {
+  if (!ctx) return LBM_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->prof_on = enable != 0;
+  if (enable) {
+    ctx->ev_used = 0;
+    ctx->intervals.clear();
+  }
+  return LBM_OK;
+}
+
+int lbm_profile_read(lbm_ctx* ctx, int phase, double* ms_total, int64_t* count) {
+  if (!ctx || phase < 0 || phase >= LBM_NPHASES) return LBM_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  double tot = 0.0;
+  int64_t n = 0;
+  for (const auto& iv : ctx->intervals) {
+    if (iv.phase != phase) continue;
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, ctx->ev_pool[iv.e0], ctx->ev_pool[iv.e1]));
+    tot += ms;
+    ++n;
+  }
+  if (ms_total) *ms_total = tot;
+  if (count) *count = n;
+  return LBM_OK;
+}
+
+int64_t lbm_kernel_launches(void) { return g_launches.load(); }
 
 int lbm_mass_momentum(lbm_ctx* ctx, double out[4]) {
   if (!ctx || !out) return LBM_ERR_ARG;

@@ -1,15 +1,15 @@
 // lbm_forcing.cu - device-side FORCING state update (B/gaussian.f90:182-307).
 //
-// The stochastic forcing draws 150 uniform numbers per call from a
+// The stochastic forcing draws 450 uniform numbers per call from a
 // Park-Miller / Bays-Durham generator (ranff, B/gaussian.f90:374-404), turns
 // them into complex white noise on the 6x5x5 low-mode block, advances the
 // Ornstein-Uhlenbeck coefficients b1r..b3r and projects them onto
-// divergence-free modes a1r..a3r.  It is inherently sequential and tiny, so
-// one thread performs it on the device; keeping it there lets whole time
-// steps run without host round trips (and inside CUDA graphs).  The integer
-// generator is exact; compiled with -fmad=false, the floating-point updates
-// round like the CPU restatement except where the device log/cos/sin differ
-// from the host's by an ulp.
+// divergence-free modes a1r..a3r.  Only the integer generator is sequential;
+// one block runs the whole update on the device, so time steps need no host
+// round trip (and can run inside CUDA graphs).  The generator is exact;
+// compiled with -fmad=false, the floating-point updates round like the CPU
+// restatement except where the device log/cos/sin differ from the host's by
+// an ulp.
 #include "lbm_internal.cuh"
 
 namespace lbm {
@@ -42,32 +42,46 @@ __device__ double ran1_dev(int32_t* idum, int32_t* iy, int32_t* iv) {
 
 __device__ __forceinline__ int m655(int i, int j, int k) { return (i - 1) + 6 * (j - 1) + 30 * (k - 1); }
 
-__global__ void k_forcing_update(ForcingDev* st, double var, double tf, double pi2,
-                                 const double* kxr6, const double* kyr5, const double* kzr5) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double fr[450];
+// One block: thread 0 draws the 450 uniform numbers in the reference's
+// order (mc, k, j, i = 1,3,5; cont1 then rph), then the magnitudes,
+// phases, Ornstein-Uhlenbeck update and projection run one mode per thread.
+__global__ void __launch_bounds__(256) k_forcing_update(ForcingDev* st, double var, double tf,
+                                                        double pi2, const double* kxr6,
+                                                        const double* kyr5, const double* kzr5) {
+  __shared__ double u[450];
+  __shared__ double fr[450];
+  const int tid = threadIdx.x;
   const double smallx = 1.0e-18;
   const double xkf = sqrt(8.0);
   const double dt = 1.0;
-  int32_t idum = st->iseedf, iy = st->iyf;
-  int32_t iv[32];
-  for (int i = 0; i < 32; ++i) iv[i] = st->ivf[i];
-  for (int mc = 1; mc <= 3; ++mc)
-    for (int k = 1; k <= 5; ++k)
-      for (int j = 1; j <= 5; ++j)
-        for (int i = 1; i <= 6; i += 2) {
-          double cont1 = ran1_dev(&idum, &iy, iv);
-          if (cont1 < 1.e-6) cont1 = 1.e-6;
-          double rmag = sqrt(-4.0 * var * dt * log(cont1) / tf);
-          double rph = ran1_dev(&idum, &iy, iv);
-          fr[m655(i, j, k) + 150 * (mc - 1)] = rmag * cos(pi2 * rph);
-          fr[m655(i + 1, j, k) + 150 * (mc - 1)] = rmag * sin(pi2 * rph);
-        }
-  st->iseedf = idum;
-  st->iyf = iy;
-  for (int i = 0; i < 32; ++i) st->ivf[i] = iv[i];
-  for (int mc = 1; mc <= 3; ++mc) {
-    double* q = fr + 150 * (mc - 1);
+  if (tid == 0) {
+    int32_t idum = st->iseedf, iy = st->iyf;
+    int32_t iv[32];
+    for (int i = 0; i < 32; ++i) iv[i] = st->ivf[i];
+    for (int d = 0; d < 450; ++d) u[d] = ran1_dev(&idum, &iy, iv);
+    st->iseedf = idum;
+    st->iyf = iy;
+    for (int i = 0; i < 32; ++i) st->ivf[i] = iv[i];
+  }
+  __syncthreads();
+  // white noise, gaussian.f90:201-215; draw pair d <-> (mc, k, j, i)
+  for (int d = tid; d < 225; d += blockDim.x) {
+    int i = 1 + 2 * (d % 3);
+    int r = d / 3;
+    int j = 1 + r % 5; r /= 5;
+    int k = 1 + r % 5;
+    int mc = 1 + r / 5;
+    double cont1 = u[2 * d];
+    if (cont1 < 1.e-6) cont1 = 1.e-6;
+    double rmag = sqrt(-4.0 * var * dt * log(cont1) / tf);
+    double rph = u[2 * d + 1];
+    fr[m655(i, j, k) + 150 * (mc - 1)] = rmag * cos(pi2 * rph);
+    fr[m655(i + 1, j, k) + 150 * (mc - 1)] = rmag * sin(pi2 * rph);
+  }
+  __syncthreads();
+  // real-valued forcing in the k1 = 0 plane, gaussian.f90:220-236
+  if (tid < 3) {
+    double* q = fr + 150 * tid;
     for (int k = 1; k <= 5; ++k) {
       int kk = (k == 1) ? 1 : 7 - k;
       for (int j = 2; j <= 3; ++j) {
@@ -84,48 +98,52 @@ __global__ void k_forcing_update(ForcingDev* st, double var, double tf, double p
     q[m655(1, 1, 1)] = 0.0;
     q[m655(2, 1, 1)] = 0.0;
   }
+  __syncthreads();
   double* b1 = st->b;
   double* b2 = st->b + 150;
   double* b3 = st->b + 300;
   double* a1 = st->a;
   double* a2 = st->a + 150;
   double* a3 = st->a + 300;
-  for (int k = 1; k <= 5; ++k)
-    for (int j = 1; j <= 5; ++j)
-      for (int i = 1; i <= 6; ++i) {
-        int m = m655(i, j, k);
-        double kx = kxr6[i - 1], ky = kyr5[j - 1], kz = kzr5[k - 1];
-        double radm = sqrt(kx * kx + ky * ky + kz * kz);
-        if (radm < xkf) {
-          b1[m] = b1[m] * (1.0 - dt / tf) + fr[m];
-          b2[m] = b2[m] * (1.0 - dt / tf) + fr[m + 150];
-          b3[m] = b3[m] * (1.0 - dt / tf) + fr[m + 300];
-          double t1 = kx * b1[m], t2 = ky * b2[m], t3 = kz * b3[m];
-          double rs = radm + smallx;
-          double divb = (t1 + t2 + t3) / (rs * rs);
-          if (radm == 0.0) divb = 0.0;
-          a1[m] = b1[m] - kx * divb;
-          a2[m] = b2[m] - ky * divb;
-          a3[m] = b3[m] - kz * divb;
-        } else {
-          a1[m] = 0.0; a2[m] = 0.0; a3[m] = 0.0;
-        }
-      }
-  for (int i = 1; i <= 2; ++i) { a1[m655(i, 1, 1)] = 0.0; a2[m655(i, 1, 1)] = 0.0; a3[m655(i, 1, 1)] = 0.0; }
-  for (int k = 1; k <= 5; ++k) {
-    int kk = (k == 1) ? 1 : 7 - k;
-    for (int j = 2; j <= 3; ++j) {
-      int jj = 7 - j;
-      a1[m655(1, jj, kk)] = a1[m655(1, j, k)]; a1[m655(2, jj, kk)] = -a1[m655(2, j, k)];
-      a2[m655(1, jj, kk)] = a2[m655(1, j, k)]; a2[m655(2, jj, kk)] = -a2[m655(2, j, k)];
-      a3[m655(1, jj, kk)] = a3[m655(1, j, k)]; a3[m655(2, jj, kk)] = -a3[m655(2, j, k)];
+  // OU update and solenoidal projection, gaussian.f90:243-274
+  for (int m = tid; m < 150; m += blockDim.x) {
+    int i = 1 + m % 6, j = 1 + (m / 6) % 5, k = 1 + m / 30;
+    double kx = kxr6[i - 1], ky = kyr5[j - 1], kz = kzr5[k - 1];
+    double radm = sqrt(kx * kx + ky * ky + kz * kz);
+    if (radm < xkf) {
+      b1[m] = b1[m] * (1.0 - dt / tf) + fr[m];
+      b2[m] = b2[m] * (1.0 - dt / tf) + fr[m + 150];
+      b3[m] = b3[m] * (1.0 - dt / tf) + fr[m + 300];
+      double t1 = kx * b1[m], t2 = ky * b2[m], t3 = kz * b3[m];
+      double rs = radm + smallx;
+      double divb = (t1 + t2 + t3) / (rs * rs);
+      if (radm == 0.0) divb = 0.0;
+      a1[m] = b1[m] - kx * divb;
+      a2[m] = b2[m] - ky * divb;
+      a3[m] = b3[m] - kz * divb;
+    } else {
+      a1[m] = 0.0; a2[m] = 0.0; a3[m] = 0.0;
     }
   }
-  for (int k = 2; k <= 3; ++k) {
-    int kk = 7 - k;
-    a1[m655(1, 1, kk)] = a1[m655(1, 1, k)]; a1[m655(2, 1, kk)] = -a1[m655(2, 1, k)];
-    a2[m655(1, 1, kk)] = a2[m655(1, 1, k)]; a2[m655(2, 1, kk)] = -a2[m655(2, 1, k)];
-    a3[m655(1, 1, kk)] = a3[m655(1, 1, k)]; a3[m655(2, 1, kk)] = -a3[m655(2, 1, k)];
+  __syncthreads();
+  // gaussian.f90:277-307
+  if (tid < 3) {
+    double* a = st->a + 150 * tid;
+    a[m655(1, 1, 1)] = 0.0;
+    a[m655(2, 1, 1)] = 0.0;
+    for (int k = 1; k <= 5; ++k) {
+      int kk = (k == 1) ? 1 : 7 - k;
+      for (int j = 2; j <= 3; ++j) {
+        int jj = 7 - j;
+        a[m655(1, jj, kk)] = a[m655(1, j, k)];
+        a[m655(2, jj, kk)] = -a[m655(2, j, k)];
+      }
+    }
+    for (int k = 2; k <= 3; ++k) {
+      int kk = 7 - k;
+      a[m655(1, 1, kk)] = a[m655(1, 1, k)];
+      a[m655(2, 1, kk)] = -a[m655(2, 1, k)];
+    }
   }
 }
 
@@ -134,7 +152,7 @@ __global__ void k_forcing_update(ForcingDev* st, double var, double tf, double p
 void launch_forcing_update(ForcingDev* st, double var, double tf, double pi2,
                            const double* kxr6, const double* kyr5, const double* kzr5,
                            cudaStream_t s) {
-  k_forcing_update<<<1, 32, 0, s>>>(st, var, tf, pi2, kxr6, kyr5, kzr5);
+  { k_forcing_update<<<1, 256, 0, s>>>(st, var, tf, pi2, kxr6, kyr5, kzr5); count_launch(); }
 }
 
 }  // namespace lbm

@@ -105,7 +105,8 @@ __device__ inline void raise_error(DevStatus* st, int code, int where) {
 // the C ABI layer in lbm_capi.cu
 namespace lbm {
 
-struct Ctx;  // defined in lbm_capi.cu
+// process-wide count of kernels this library has launched (lbm_kernel_launches)
+void count_launch();
 
 // fluid
 template <typename T>
@@ -155,8 +156,10 @@ void launch_forcing_update(ForcingDev* st, double var, double tf, double pi2,
                            const double* kxr6, const double* kyr5, const double* kzr5,
                            cudaStream_t s);
 template <typename T>
-void launch_forcing_tables(const Geometry& g, const ForcingDev* st, const double* kyr5,
-                           const double* kzr5, T* rowtab, double* ztab, cudaStream_t s);
+// ytw[jy][y], ztw[kz][z]: (cos, sin) of 2 pi k n / N for the five low
+// wavenumbers of each axis, tabulated once per box
+void launch_forcing_tables(const Geometry& g, const ForcingDev* st, const double* ytw,
+                           const double* ztw, T* rowtab, double* ztab, cudaStream_t s);
 
 // particles
 struct LinkSlab {
@@ -166,8 +169,9 @@ struct LinkSlab {
   int32_t* count;
   int cap;
 };
+// alpha_fp32: link fractions in single precision (the FP32 population path)
 void launch_links(const Geometry& g, const ParticleView& pv, int32_t* isnodes,
-                  LinkSlab ls, DevStatus* st, cudaStream_t s);
+                  LinkSlab ls, DevStatus* st, int alpha_fp32, cudaStream_t s);
 template <typename T>
 void launch_bounce_back(const Geometry& g, const ParticleView& pv, const T* f,
                         int pushed_layout, const int32_t* isnodes, LinkSlab ls,
@@ -192,10 +196,17 @@ void launch_move(const Geometry& g, int npart, const PartParams& pp, MoveState m
                  cudaStream_t s);
 void launch_redistribute(const Geometry& g, int npart, const PartParams& pp, MoveState ms,
                          DevStatus* st, cudaStream_t s);
+// refill events of one step: node index and particle id per event
+struct FillList {
+  int32_t* node;
+  int32_t* part;
+  int32_t* count;
+  int cap;
+};
 template <typename T>
 void launch_filling(const Geometry& g, const ParticleView& pv, const PartParams& pp,
                     const double* ypglbp, const double* wpp, const double* omgpp,
-                    const int32_t* isnodes, const int32_t* isnodes0, T* f,
-                    cudaStream_t s);
+                    const int32_t* isnodes, const int32_t* isnodes0, T* f, FillList fl,
+                    DevStatus* st, cudaStream_t s);
 
 }  // namespace lbm

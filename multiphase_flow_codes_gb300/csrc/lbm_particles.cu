@@ -31,41 +31,71 @@ __device__ __forceinline__ double near_img(double c, double p, int n, int nh) {
   return c;
 }
 __device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+template <typename R>
+__device__ __forceinline__ R near_img_t(R c, R p, int n, int nh) {
+  if ((c - p) > R(nh)) c = c - R(n);
+  if ((c - p) < -R(nh)) c = c + R(n);
+  return c;
+}
 
 // The reference's beads_links keeps shifting the particle centre toward the
 // current point and never resets it inside its loop nest
-// (B/partlib.f90:961-982).  sweep_at returns the value of such a centre
-// coordinate at point jq (1-based, points p_j = j - 0.5) of one sweep over
-// j = 1..n that starts from value c, evaluating the same two conditional
-// shifts at every point.  fl(c - p) is monotone in p, so the shift
-// predicates are monotone and the points where a shift fires are found by
-// bisection instead of visiting every point.
-__device__ double sweep_at(double c, int jq, int n, int nh) {
+// (B/partlib.f90:961-982): at point p_j = j - 0.5 of a sweep j = 1..n it
+// applies "if (c - p > n/2) c -= n; if (c - p < -n/2) c += n" to the value
+// left by the previous point.  fl(c - p) is monotone in p, so both shift
+// predicates are monotone along a sweep and the points where a shift fires
+// are found by bisection instead of visiting every point.
+// The points of one sweep where the shifted coordinate changes, with the
+// value after each change: a sweep starting from c changes at most a few
+// times (a shift down at the first point, a shift up once c - p drops
+// below -n/2), so any point's value is a lookup in this short list.
+constexpr int MAXEV = 6;
+struct SweepEv {
+  int nev;
+  int ok;
+  int j[MAXEV];
+  double v[MAXEV];
+  double v0;
+};
+__device__ SweepEv sweep_events(double c, int n, int nh) {
+  SweepEv s;
+  s.nev = 0;
+  s.ok = 1;
+  s.v0 = c;
   const double dn = (double)n, dnh = (double)nh;
   int j = 1;
   for (int guard = 0; guard < 16; ++guard) {
-    double p = (double)j - 0.5;
+    const double p = (double)j - 0.5;
+    const double before = c;
     if ((c - p) > dnh) c = c - dn;
     if ((c - p) < -dnh) c = c + dn;
-    if (j >= jq) return c;
-    int jn = jq;
-    double p1 = (double)(j + 1) - 0.5;
+    if (__double_as_longlong(c) != __double_as_longlong(before)) {
+      if (s.nev < MAXEV) { s.j[s.nev] = j; s.v[s.nev] = c; ++s.nev; } else s.ok = 0;
+    }
+    if (j >= n) return s;
+    int jn = n + 1;
+    const double p1 = (double)(j + 1) - 0.5;
     if ((c - p1) > dnh) {
       jn = j + 1;
-    } else {
-      double pq = (double)jq - 0.5;
-      if ((c - pq) < -dnh) {
-        int lo = j + 1, hi = jq;
-        while (lo < hi) {
-          int mid = (lo + hi) >> 1;
-          if ((c - ((double)mid - 0.5)) < -dnh) hi = mid; else lo = mid + 1;
-        }
-        jn = lo;
+    } else if ((c - ((double)n - 0.5)) < -dnh) {
+      int lo = j + 1, hi = n;
+      while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if ((c - ((double)mid - 0.5)) < -dnh) hi = mid; else lo = mid + 1;
       }
+      jn = lo;
     }
+    if (jn > n) return s;
     j = jn;
   }
-  return c;
+  s.ok = 0;
+  return s;
+}
+__device__ __forceinline__ double sweep_value(const SweepEv& s, int jq) {
+  double v = s.v0;
+  for (int e = 0; e < s.nev; ++e)
+    if (s.j[e] <= jq) v = s.v[e];
+  return v;
 }
 
 // candidate indices (1-based) along one axis: the union, in ascending order,
@@ -111,35 +141,102 @@ __device__ Cands make_cands(double c, int n, double w, bool periodic) {
 }
 
 constexpr int MAXPLANES = 96;
-constexpr int MAXROWS = 1024;
+constexpr int MAXROWS = 640;   // processed rows per particle: (2 (rad + 2) + 1)^2
+constexpr int MAXC = 128;  // candidate positions per axis
+constexpr int MAXNEAR = 2048;  // fluid nodes within rad + 1.5 of one centre
 
-// beads_links for one particle per block.
+// Sign decisions of the squared-distance tests of beads_links are taken in
+// FP32 when |value| exceeds this margin (the FP32 error is below 1e-4 for
+// the offsets involved) and recomputed with the reference's FP64 expression
+// otherwise, so the outcome is always the FP64 one.
+constexpr float kDecide = 4e-3f;
+
+// beads_links for one particle per block.  Integer outcomes (solid flags,
+// link sets) are exactly those of the reference's FP64 loop nest; the link
+// fraction alpha is FP64 (the reference formula) unless alpha_fp32 is set.
 __global__ void __launch_bounds__(PB) k_links(Geometry g, ParticleView pv, int32_t* isnodes,
-                                              LinkSlab ls, DevStatus* st) {
+                                              LinkSlab ls, DevStatus* st, int alpha_fp32) {
   using Scan = cub::BlockScan<int, PB>;
   __shared__ typename Scan::TempStorage scan_tmp;
   __shared__ int plane_k[MAXPLANES];
   __shared__ double plane_z[MAXPLANES];
+  __shared__ double yval[3][MAXC];
+  __shared__ double xval[3][MAXC];
+  __shared__ float xvalf[3][MAXC];
   __shared__ int nplanes;
   __shared__ int row_k[MAXROWS], row_j[MAXROWS];
   __shared__ double row_z[MAXROWS], row_y[MAXROWS];
+  __shared__ float row_yy[MAXROWS], row_zz[MAXROWS];
   __shared__ int nrows;
   __shared__ int base;
   __shared__ int fixed_ok;
+  __shared__ int near_rc[MAXNEAR];  // fluid nodes within reach: row << 8 | candidate
+  __shared__ int nnear;
 
   const int p = blockIdx.x;
   if (p >= pv.npart) return;
   const double rad = pv.rad;
   const double radp2 = rad * 1.0 + 2.0;
   const double rad2 = (rad * 1.0) * (rad * 1.0);
+  const float rad2f = (float)rad2;
+  // only nodes within rad + sqrt(2) of the centre can be solid or own a link
+  const float reachf = (float)((rad + 1.5) * (rad + 1.5)) + 0.05f;
   const bool channel = g.channel != 0;
   const double x0 = pv.ypglb[3 * p] * 1.0, y0 = pv.ypglb[3 * p + 1] * 1.0,
                z0 = pv.ypglb[3 * p + 2] * 1.0;
   const int tid = threadIdx.x;
 
   if (tid == 0) {
-    nplanes = 0; nrows = 0; base = 0; fixed_ok = 1;
+    nplanes = 0; nrows = 0; base = 0; fixed_ok = 1; nnear = 0;
   }
+  if (!(isfinite(x0) && isfinite(y0) && isfinite(z0))) {
+    if (tid == 0) {
+      ls.count[p] = 0;
+      raise_error(st, LBM_ERR_NONFINITE, p);
+    }
+    return;
+  }
+  // Sweep event lists for the start states of the y sweep (plane 0 starts
+  // at y0, plane 1 at Y1 = end of plane 0's sweep, later planes at Y2) and
+  // of the x sweep (rows likewise: x0, X1, X2), and for the single z sweep.
+  // The end state is a fixed point from the second sweep on (only a centre
+  // within an ulp of n/2 - 1/2 makes the third state differ from the second).
+  __shared__ SweepEv sev[7];  // 0..2: y states, 3..5: x states, 6: z
+  if (tid == 0) {
+    double c = y0;
+    for (int s = 0; s < 3; ++s) {
+      sev[s] = sweep_events(c, g.ny, g.nyh);
+      c = sweep_value(sev[s], g.ny);
+    }
+    SweepEv last = sweep_events(c, g.ny, g.nyh);
+    if (sweep_value(last, g.ny) != c || !(sev[0].ok && sev[1].ok && sev[2].ok)) fixed_ok = 0;
+  } else if (tid == 32 && !channel) {
+    double c = x0;
+    for (int s = 0; s < 3; ++s) {
+      sev[3 + s] = sweep_events(c, g.nx, g.nxh);
+      c = sweep_value(sev[3 + s], g.nx);
+    }
+    SweepEv last = sweep_events(c, g.nx, g.nxh);
+    if (sweep_value(last, g.nx) != c || !(sev[3].ok && sev[4].ok && sev[5].ok)) fixed_ok = 0;
+  } else if (tid == 64) {
+    sev[6] = sweep_events(z0, g.nz, g.nzh);
+    if (!sev[6].ok) fixed_ok = 0;
+  }
+  __syncthreads();
+  Cands cy = make_cands(y0, g.ny, radp2, true);
+  Cands cx = make_cands(x0, g.nx, radp2, !channel);
+  const int ty = min(cy.total(), MAXC);
+  const int tx = min(cx.total(), MAXC);
+  for (int t = tid; t < 3 * MAXC; t += PB) {
+    int s = t / MAXC, c = t % MAXC;
+    if (c < ty) yval[s][c] = sweep_value(sev[s], cy.at(c));
+    if (c < tx) {
+      double v = channel ? x0 : sweep_value(sev[3 + s], cx.at(c));
+      xval[s][c] = v;
+      xvalf[s][c] = (float)v;
+    }
+  }
+  if (tid == 0 && (cy.total() > MAXC || cx.total() > MAXC)) fixed_ok = 0;
   __syncthreads();
 
   // ---- planes: k with |zz0| <= radp2, zc from the k-sweep starting at z0
@@ -152,7 +249,7 @@ __global__ void __launch_bounds__(PB) k_links(Geometry g, ParticleView pv, int32
     bool take = false;
     if (t < tz) {
       k = cz.at(t);
-      zc = sweep_at(z0, k, g.nz, g.nzh);
+      zc = sweep_value(sev[6], k);
       double zpnt = (double)k - 0.5 + 0.0;
       double zz0 = zpnt - zc;
       take = fabs(zz0) <= radp2;
@@ -166,116 +263,154 @@ __global__ void __launch_bounds__(PB) k_links(Geometry g, ParticleView pv, int32
     __syncthreads();
   }
 
-  // ---- rows: per plane, j with the y condition; the y-sweep of plane 0
-  // starts at y0, every later plane at the sweep's fixed point Y1
-  const double Y1 = sweep_at(y0, g.ny, g.ny, g.nyh);
-  if (tid == 0 && sweep_at(Y1, g.ny, g.ny, g.nyh) != Y1) fixed_ok = 0;
-  Cands cy = make_cands(y0, g.ny, radp2, true);
-  int ty = cy.total();
+  // ---- rows: per plane (in k order), j with the exact y condition
   int tpairs = nplanes * ty;
   for (int c0 = 0; c0 < tpairs; c0 += PB) {
     int t = c0 + tid;
     bool take = false;
     int k = 0, j = 0;
-    double zc = 0.0, yc = 0.0;
+    double zc = 0.0, yc = 0.0, zz0 = 0.0, yy0 = 0.0;
     if (t < tpairs) {
       int pi = t / ty;
-      j = cy.at(t - pi * ty);
+      int c = t - pi * ty;
+      j = cy.at(c);
       k = plane_k[pi];
       zc = plane_z[pi];
-      yc = sweep_at(pi == 0 ? y0 : Y1, j, g.ny, g.nyh);
-      double zz0 = ((double)k - 0.5 + 0.0) - zc;
-      double yy0 = ((double)j - 0.5 + 0.0) - yc;
+      yc = yval[min(pi, 2)][c];
+      zz0 = ((double)k - 0.5 + 0.0) - zc;
+      yy0 = ((double)j - 0.5 + 0.0) - yc;
       take = channel ? (sqrt(yy0 * yy0 + zz0 * zz0) <= radp2) : (fabs(yy0) <= radp2);
     }
     int pos, tot;
     Scan(scan_tmp).ExclusiveSum(take ? 1 : 0, pos, tot);
     __syncthreads();
     if (take && nrows + pos < MAXROWS) {
-      row_k[nrows + pos] = k; row_j[nrows + pos] = j;
-      row_z[nrows + pos] = zc; row_y[nrows + pos] = yc;
+      int w = nrows + pos;
+      row_k[w] = k; row_j[w] = j; row_z[w] = zc; row_y[w] = yc;
+      row_yy[w] = (float)yy0; row_zz[w] = (float)zz0;
     }
     __syncthreads();
     if (tid == 0) nrows = min(nrows + tot, MAXROWS);
     __syncthreads();
   }
 
-  // ---- nodes: per row, i candidates; box x-sweep: row 0 starts at x0,
-  // later rows at the fixed point X1.  The channel never shifts x.
-  const double X1 = channel ? x0 : sweep_at(x0, g.nx, g.nx, g.nxh);
-  if (tid == 0 && !channel && sweep_at(X1, g.nx, g.nx, g.nxh) != X1) fixed_ok = 0;
-  Cands cx = make_cands(x0, g.nx, radp2, !channel);
-  int tx = cx.total();
+  // ---- phase 1: nodes of every processed row within reach of the sphere;
+  // solid nodes are flagged, fluid ones kept (in loop order) for phase 2
   int tnodes = nrows * tx;
-  int32_t* code = ls.code + (long long)p * ls.cap;
-  double* alph = ls.alpha + (long long)p * ls.cap;
   for (int c0 = 0; c0 < tnodes; c0 += PB) {
     int t = c0 + tid;
-    int nl = 0;
-    int i = 0, j = 0, k = 0;
-    double xx0 = 0, yy0 = 0, zz0 = 0, rr0 = 0, xc = 0, yc = 0, zc = 0;
-    unsigned linkmask = 0;
+    bool keep = false;
+    int r = 0, ci = 0;
     if (t < tnodes) {
-      int r = t / tx;
-      i = cx.at(t - r * tx);
-      j = row_j[r]; k = row_k[r];
-      zc = row_z[r]; yc = row_y[r];
-      double xpnt = (double)i - 0.5;
-      xc = channel ? x0 : sweep_at(r == 0 ? x0 : X1, i, g.nx, g.nxh);
-      xx0 = xpnt - xc;
-      yy0 = ((double)j - 0.5 + 0.0) - yc;
-      zz0 = ((double)k - 0.5 + 0.0) - zc;
-      bool inside;
-      if (channel) {
-        rr0 = xx0 * xx0 + yy0 * yy0 + zz0 * zz0;
-        inside = sqrt(rr0) <= radp2;
-      } else {
-        inside = fabs(xx0) <= radp2;
-        rr0 = xx0 * xx0 + yy0 * yy0 + zz0 * zz0;
-      }
-      if (inside) {
-        double rr01 = rr0 - rad2;
-        long long node = (long long)(i - 1) + (long long)g.nx * ((j - 1) + (long long)g.ny * (k - 1));
-        if (rr01 <= 0.0) {
+      r = t / tx;
+      ci = t - r * tx;
+      const int i = cx.at(ci);
+      const float xxf = ((float)i - 0.5f) - xvalf[min(r, 2)][ci];
+      const float yyf = row_yy[r], zzf = row_zz[r];
+      const float rr0f = xxf * xxf + yyf * yyf + zzf * zzf;
+      if (rr0f <= reachf) {
+        const int j = row_j[r], k = row_k[r];
+        bool solid;
+        const float d0 = rr0f - rad2f;
+        if (d0 < -kDecide) solid = true;
+        else if (d0 > kDecide) solid = false;
+        else {
+          const double xc = xval[min(r, 2)][ci], yc = row_y[r], zc = row_z[r];
+          double xx0 = ((double)i - 0.5) - xc;
+          double yy0 = ((double)j - 0.5 + 0.0) - yc;
+          double zz0 = ((double)k - 0.5 + 0.0) - zc;
+          double rr0 = xx0 * xx0 + yy0 * yy0 + zz0 * zz0;
+          solid = (rr0 - rad2) <= 0.0;
+        }
+        if (solid) {
+          long long node = (long long)(i - 1) + (long long)g.nx * ((j - 1) + (long long)g.ny * (k - 1));
           atomicMax(&isnodes[node], p);
         } else {
-#pragma unroll
-          for (int ipop = 1; ipop < NPOP; ++ipop) {
-            double xx1 = (double)(i + cix(ipop)) - 0.5 - xc;
-            double yy1 = (double)(j + ciy(ipop)) - 0.5 - yc + 0.0;
-            double zz1 = (double)(k + ciz(ipop)) - 0.5 - zc + 0.0;
-            double rr1 = xx1 * xx1 + yy1 * yy1 + zz1 * zz1;
-            if (rr1 - rad2 <= 0.0) linkmask |= 1u << ipop;
-          }
-          nl = __popc(linkmask);
+          keep = true;
         }
       }
     }
     int pos, tot;
-    Scan(scan_tmp).ExclusiveSum(nl, pos, tot);
+    Scan(scan_tmp).ExclusiveSum(keep ? 1 : 0, pos, tot);
     __syncthreads();
-    if (nl > 0) {
-      long long node = (long long)(i - 1) + (long long)g.nx * ((j - 1) + (long long)g.ny * (k - 1));
-      int w = base + pos;
-      for (int ipop = 1; ipop < NPOP; ++ipop) {
-        if (!(linkmask & (1u << ipop))) continue;
+    if (keep && nnear + pos < MAXNEAR) near_rc[nnear + pos] = (r << 8) | ci;
+    __syncthreads();
+    if (tid == 0) {
+      if (nnear + tot > MAXNEAR) fixed_ok = 0;
+      nnear = min(nnear + tot, MAXNEAR);
+    }
+    __syncthreads();
+  }
+
+  // ---- phase 2: one thread per (fluid near node, direction); links are
+  // written in (node, ipop) order
+  const int npairs = nnear * 18;
+  int32_t* code = ls.code + (long long)p * ls.cap;
+  double* alph = ls.alpha + (long long)p * ls.cap;
+  float* alph32 = reinterpret_cast<float*>(alph);
+  for (int c0 = 0; c0 < npairs; c0 += PB) {
+    const int t = c0 + tid;
+    bool link = false;
+    int r = 0, ci = 0, ipop = 0, i = 0;
+    float xxf = 0.f, yyf = 0.f, zzf = 0.f;
+    if (t < npairs) {
+      const int idx = t / 18;
+      ipop = t - idx * 18 + 1;
+      const int rc = near_rc[idx];
+      r = rc >> 8;
+      ci = rc & 255;
+      i = cx.at(ci);
+      xxf = ((float)i - 0.5f) - xvalf[min(r, 2)][ci];
+      yyf = row_yy[r];
+      zzf = row_zz[r];
+      const float ax = xxf + (float)cix(ipop), ay = yyf + (float)ciy(ipop), az = zzf + (float)ciz(ipop);
+      const float d1 = ax * ax + ay * ay + az * az - rad2f;
+      if (d1 < -kDecide) link = true;
+      else if (d1 > kDecide) link = false;
+      else {
+        const int j = row_j[r], k = row_k[r];
+        const double xc = xval[min(r, 2)][ci], yc = row_y[r], zc = row_z[r];
         double xx1 = (double)(i + cix(ipop)) - 0.5 - xc;
         double yy1 = (double)(j + ciy(ipop)) - 0.5 - yc + 0.0;
         double zz1 = (double)(k + ciz(ipop)) - 0.5 - zc + 0.0;
         double rr1 = xx1 * xx1 + yy1 * yy1 + zz1 * zz1;
-        double rr11 = rr1 - rad2;
-        double aa = rr0 + rr1 - 2.0 * (xx0 * xx1 + yy0 * yy1 + zz0 * zz1);
-        double bb = xx1 * (xx0 - xx1) + yy1 * (yy0 - yy1) + zz1 * (zz0 - zz1);
-        double cc = rr11;
-        double alpha0 = bb / aa;
-        double alpha1 = sqrt(alpha0 * alpha0 - cc / aa);
-        double alpha = -alpha0 + alpha1;
-        alpha = 1.0 - alpha;
-        if (w < ls.cap) {
-          code[w] = (int32_t)(node * 32 + ipop);
-          alph[w] = alpha;
+        link = (rr1 - rad2) <= 0.0;
+      }
+    }
+    int pos, tot;
+    Scan(scan_tmp).ExclusiveSum(link ? 1 : 0, pos, tot);
+    __syncthreads();
+    if (link) {
+      const int w = base + pos;
+      const int j = row_j[r], k = row_k[r];
+      const int ix = cix(ipop), iy = ciy(ipop), iz = ciz(ipop);
+      const bool diag = (ix * ix + iy * iy + iz * iz) == 2;
+      long long node = (long long)(i - 1) + (long long)g.nx * ((j - 1) + (long long)g.ny * (k - 1));
+      if (w < ls.cap) {
+        code[w] = (int32_t)(node * 32 + ipop);
+        // partlib.f90:1016-1023 with aa = |x0 - x1|^2 = |c|^2 (1 or 2) and
+        // bb = x1.(x0 - x1) = -x1.c taken exactly: the same root without the
+        // cancellation in the reference's aa and without divisions
+        if (alpha_fp32) {
+          const float xf = xxf + (float)ix, yf = yyf + (float)iy, zf = zzf + (float)iz;
+          const float cc = xf * xf + yf * yf + zf * zf - rad2f;
+          const float bb = -(xf * (float)ix + yf * (float)iy + zf * (float)iz);
+          const float a0 = diag ? 0.5f * bb : bb;
+          const float ca = diag ? 0.5f * cc : cc;
+          const float a1 = sqrtf(fmaxf(a0 * a0 - ca, 0.0f));
+          alph32[w] = 1.0f - (-a0 + a1);
+        } else {
+          const double xc = xval[min(r, 2)][ci], yc = row_y[r], zc = row_z[r];
+          double xx1 = (double)(i + ix) - 0.5 - xc;
+          double yy1 = (double)(j + iy) - 0.5 - yc + 0.0;
+          double zz1 = (double)(k + iz) - 0.5 - zc + 0.0;
+          double cc = xx1 * xx1 + yy1 * yy1 + zz1 * zz1 - rad2;
+          double bb = -((double)ix * xx1 + (double)iy * yy1 + (double)iz * zz1);
+          double a0 = diag ? 0.5 * bb : bb;
+          double ca = diag ? 0.5 * cc : cc;
+          double a1 = sqrt(fmax(a0 * a0 - ca, 0.0));
+          alph[w] = 1.0 - (-a0 + a1);
         }
-        ++w;
       }
     }
     __syncthreads();
@@ -289,6 +424,25 @@ __global__ void __launch_bounds__(PB) k_links(Geometry g, ParticleView pv, int32
     if (!fixed_ok) raise_error(st, LBM_ERR_STATE, p);
   }
 }
+
+// running sum: plain FP64, or FP32 with Kahan compensation (FP32 path)
+template <typename T>
+struct Acc {
+  double s = 0.0;
+  __device__ void add(double x) { s += x; }
+  __device__ double value() const { return s; }
+};
+template <>
+struct Acc<float> {
+  float s = 0.f, c = 0.f;
+  __device__ void add(float x) {
+    float y = x - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ double value() const { return (double)s - (double)c; }
+};
 
 // post-collision population q at node (i, j, k) (0-based) in either layout.
 // pushed: the fused kernel has already moved it to its streaming target
@@ -317,11 +471,17 @@ __global__ void __launch_bounds__(PB) k_bounce(Geometry g, ParticleView pv, cons
   if (p >= pv.npart) return;
   const int cnt = ls.count[p];
   const int32_t* code = ls.code + (long long)p * ls.cap;
-  const double* alph = ls.alpha + (long long)p * ls.cap;
-  double* f9s = ls.f9 + (long long)p * ls.cap;
-  const double w1 = pv.wp[3 * p], w2 = pv.wp[3 * p + 1], w3 = pv.wp[3 * p + 2];
-  const double omg1 = pv.omgp[3 * p], omg2 = pv.omgp[3 * p + 1], omg3 = pv.omgp[3 * p + 2];
-  double acc[6] = {0, 0, 0, 0, 0, 0};
+  // link fractions and bounced populations are stored in the population
+  // precision (FP32 slabs reuse the first half of the FP64 arrays)
+  const T* alph = reinterpret_cast<const T*>(ls.alpha + (long long)p * ls.cap);
+  T* f9s = reinterpret_cast<T*>(ls.f9 + (long long)p * ls.cap);
+  // per-link arithmetic in the population precision R (FP64 plain path,
+  // FP32 shifted path); each thread's partial force/torque sums are
+  // compensated (FP32) or plain FP64, the block sums are FP64
+  using R = T;
+  Acc<T> acc6[6];
+  const R w1 = R(pv.wp[3 * p]), w2 = R(pv.wp[3 * p + 1]), w3 = R(pv.wp[3 * p + 2]);
+  const R omg1 = R(pv.omgp[3 * p]), omg2 = R(pv.omgp[3 * p + 1]), omg3 = R(pv.omgp[3 * p + 2]);
   const bool channel = g.channel != 0;
   for (int l = threadIdx.x; l < cnt; l += PB) {
     int cd = code[l];
@@ -330,13 +490,13 @@ __global__ void __launch_bounds__(PB) k_bounce(Geometry g, ParticleView pv, cons
     int i = (int)(node % g.nx);
     long long r = node / g.nx;
     int j = (int)(r % g.ny), k = (int)(r / g.ny);
-    double alpha = alph[l];
+    R alpha = alph[l];
     int ipp = ipopp(ipop);
-    double xpnt = (double)(i + 1) - 0.5, ypnt = (double)(j + 1) - 0.5, zpnt = (double)(k + 1) - 0.5;
-    double xc = pv.ypglb[3 * p], yc = pv.ypglb[3 * p + 1], zc = pv.ypglb[3 * p + 2];
-    if (!channel) xc = near_img(xc, xpnt, g.nx, g.nxh);
-    yc = near_img(yc, ypnt, g.ny, g.nyh);
-    zc = near_img(zc, zpnt, g.nz, g.nzh);
+    R xpnt = R(i + 1) - R(0.5), ypnt = R(j + 1) - R(0.5), zpnt = R(k + 1) - R(0.5);
+    R xc = R(pv.ypglb[3 * p]), yc = R(pv.ypglb[3 * p + 1]), zc = R(pv.ypglb[3 * p + 2]);
+    if (!channel) xc = near_img_t<R>(xc, xpnt, g.nx, g.nxh);
+    yc = near_img_t<R>(yc, ypnt, g.ny, g.nyh);
+    zc = near_img_t<R>(zc, zpnt, g.nz, g.nzh);
     int ix = cix(ipop), iy = ciy(ipop), iz = ciz(ipop);
     int im1 = i - ix, im2 = i - 2 * ix;
     int jm1 = wrapi(j - iy, g.ny), km1 = wrapi(k - iz, g.nz);
@@ -349,74 +509,74 @@ __global__ void __launch_bounds__(PB) k_bounce(Geometry g, ParticleView pv, cons
       im1 = wrapi(im1, g.nx);
       im2 = wrapi(im2, g.nx);
     }
-    double xx0 = xpnt + (double)ix * alpha - xc;
-    double yy0 = ypnt + (double)iy * alpha - yc;
-    double zz0 = zpnt + (double)iz * alpha - zc;
-    double ff1 = read_post(g, f, pushed, ipop, i, j, k);
-    double uwx = w1 + omg2 * zz0 - omg3 * yy0;
-    double uwy = w2 + omg3 * xx0 - omg1 * zz0;
-    double uwz = w3 + omg1 * yy0 - omg2 * xx0;
-    double uwpro = uwx * (double)ix + uwy * (double)iy + uwz * (double)iz;
-    const double wwp = ipop <= 6 ? 1.0 / 18.0 : 1.0 / 36.0;
-    double f9;
+    R xx0 = xpnt + R(ix) * alpha - xc;
+    R yy0 = ypnt + R(iy) * alpha - yc;
+    R zz0 = zpnt + R(iz) * alpha - zc;
+    R ff1 = R(read_post(g, f, pushed, ipop, i, j, k));
+    R uwx = w1 + omg2 * zz0 - omg3 * yy0;
+    R uwy = w2 + omg3 * xx0 - omg1 * zz0;
+    R uwz = w3 + omg1 * yy0 - omg2 * xx0;
+    R uwpro = uwx * R(ix) + uwy * R(iy) + uwz * R(iz);
+    const R wwp = ipop <= 6 ? R(1.0 / 18.0) : R(1.0 / 36.0);
+    R f9;
     if (alpha <= 0.5) {
       int ibm1, ibm2;
-      double ff2 = 0.0, ff3 = 0.0;
+      R ff2 = R(0), ff3 = R(0);
       if (out1) ibm1 = 2;
       else {
         long long m1 = (long long)im1 + (long long)g.nx * (jm1 + (long long)g.ny * km1);
         ibm1 = isnodes[m1] >= 0 ? 1 : -1;
-        if (ibm1 < 0) ff2 = read_post(g, f, pushed, ipop, im1, jm1, km1);
+        if (ibm1 < 0) ff2 = R(read_post(g, f, pushed, ipop, im1, jm1, km1));
       }
       if (out2) ibm2 = 2;
       else {
         long long m2 = (long long)im2 + (long long)g.nx * (jm2 + (long long)g.ny * km2);
         ibm2 = isnodes[m2] >= 0 ? 1 : -1;
-        if (ibm1 < 0 && ibm2 < 0) ff3 = read_post(g, f, pushed, ipop, im2, jm2, km2);
+        if (ibm1 < 0 && ibm2 < 0) ff3 = R(read_post(g, f, pushed, ipop, im2, jm2, km2));
       }
       if (ibm1 > 0) {
-        f9 = ff1 - 6.0 * wwp * uwpro;
+        f9 = ff1 - R(6.0) * wwp * uwpro;
       } else if (ibm2 > 0) {
-        f9 = 2.0 * alpha * (ff1 - ff2) + ff2 - 6.0 * wwp * uwpro;
+        f9 = R(2.0) * alpha * (ff1 - ff2) + ff2 - R(6.0) * wwp * uwpro;
       } else {
-        double c1 = alpha * (1.0 + 2.0 * alpha);
-        double c2 = 1.0 - 4.0 * alpha * alpha;
-        double c3 = -alpha * (1.0 - 2.0 * alpha);
-        f9 = c1 * ff1 + c2 * ff2 + c3 * ff3 - 6.0 * wwp * uwpro;
+        R c1 = alpha * (R(1.0) + R(2.0) * alpha);
+        R c2 = R(1.0) - R(4.0) * alpha * alpha;
+        R c3 = -alpha * (R(1.0) - R(2.0) * alpha);
+        f9 = c1 * ff1 + c2 * ff2 + c3 * ff3 - R(6.0) * wwp * uwpro;
       }
     } else {
-      double ff2 = read_post(g, f, pushed, ipp, i, j, k);
+      R ff2 = R(read_post(g, f, pushed, ipp, i, j, k));
       int ibm1;
-      double ff3 = 0.0;
+      R ff3 = R(0);
       if (out1) ibm1 = 2;
       else {
         long long m1 = (long long)im1 + (long long)g.nx * (jm1 + (long long)g.ny * km1);
         ibm1 = isnodes[m1] >= 0 ? 1 : -1;
-        if (ibm1 < 0) ff3 = read_post(g, f, pushed, ipp, im1, jm1, km1);
+        if (ibm1 < 0) ff3 = R(read_post(g, f, pushed, ipp, im1, jm1, km1));
       }
       if (ibm1 > 0) {
-        double c1 = 0.5 / alpha;
-        double c2 = 1.0 - c1;
-        f9 = c1 * ff1 + c2 * ff2 - 6.0 * wwp * c1 * uwpro;
+        R c1 = R(0.5) / alpha;
+        R c2 = R(1.0) - c1;
+        f9 = c1 * ff1 + c2 * ff2 - R(6.0) * wwp * c1 * uwpro;
       } else {
-        double c1 = 1.0 / alpha / (2.0 * alpha + 1.0);
-        double c2 = (2.0 * alpha - 1.0) / alpha;
-        double c3 = 1.0 - c1 - c2;
-        f9 = c1 * ff1 + c2 * ff2 + c3 * ff3 - 6.0 * wwp * c1 * uwpro;
+        R c1 = R(1.0) / alpha / (R(2.0) * alpha + R(1.0));
+        R c2 = (R(2.0) * alpha - R(1.0)) / alpha;
+        R c3 = R(1.0) - c1 - c2;
+        f9 = c1 * ff1 + c2 * ff2 + c3 * ff3 - R(6.0) * wwp * c1 * uwpro;
       }
     }
     f9s[l] = f9;
-    double dff = ff1 + f9;
-    double dxmom = dff * (double)ix, dymom = dff * (double)iy, dzmom = dff * (double)iz;
-    acc[0] += dxmom;
-    acc[1] += dymom;
-    acc[2] += dzmom;
-    acc[3] = acc[3] + dzmom * yy0 - dymom * zz0;
-    acc[4] = acc[4] + dxmom * zz0 - dzmom * xx0;
-    acc[5] = acc[5] + dymom * xx0 - dxmom * yy0;
+    R dff = ff1 + f9;
+    R dxmom = dff * R(ix), dymom = dff * R(iy), dzmom = dff * R(iz);
+    acc6[0].add(dxmom);
+    acc6[1].add(dymom);
+    acc6[2].add(dzmom);
+    acc6[3].add(dzmom * yy0 - dymom * zz0);
+    acc6[4].add(dxmom * zz0 - dzmom * xx0);
+    acc6[5].add(dymom * xx0 - dxmom * yy0);
   }
   for (int c = 0; c < 6; ++c) {
-    double s = Red(red_tmp).Sum(acc[c]);
+    double s = Red(red_tmp).Sum(acc6[c].value());
     __syncthreads();
     if (threadIdx.x == 0) {
       if (c < 3) fHIp[3 * p + c] = s; else torqp[3 * p + c - 3] = s;
@@ -434,7 +594,7 @@ __global__ void __launch_bounds__(PB) k_bounce_store(Geometry g, ParticleView pv
   if (p >= pv.npart) return;
   const int cnt = ls.count[p];
   const int32_t* code = ls.code + (long long)p * ls.cap;
-  const double* f9s = ls.f9 + (long long)p * ls.cap;
+  const T* f9s = reinterpret_cast<const T*>(ls.f9 + (long long)p * ls.cap);
   for (int l = threadIdx.x; l < cnt; l += PB) {
     int cd = code[l];
     int ipop = cd & 31;
@@ -444,7 +604,7 @@ __global__ void __launch_bounds__(PB) k_bounce_store(Geometry g, ParticleView pv
       int i = (int)(node % g.nx);
       int it = i + cix(ipop);
       if (g.channel && (it < 0 || it >= g.nx)) continue;
-      f[ipp * g.N + node] = T(f9s[l]);
+      f[ipp * g.N + node] = f9s[l];
     } else {
       int i = (int)(node % g.nx);
       long long r = node / g.nx;
@@ -453,18 +613,31 @@ __global__ void __launch_bounds__(PB) k_bounce_store(Geometry g, ParticleView pv
       if (g.channel && (it < 0 || it >= g.nx)) continue;
       it = wrapi(it, g.nx);
       int jt = wrapi(j + ciy(ipop), g.ny), kt = wrapi(k + ciz(ipop), g.nz);
-      f[ipp * g.N + (long long)it + (long long)g.nx * (jt + (long long)g.ny * kt)] = T(f9s[l]);
+      f[ipp * g.N + (long long)it + (long long)g.nx * (jt + (long long)g.ny * kt)] = f9s[l];
     }
   }
 }
 
-// beads_lubforce, one thread per particle.  Contributions to particle p are
+// beads_lubforce, one warp per particle.  Contributions to particle p are
 // accumulated in ascending partner id, the order in which the reference's
 // pair loop (id ascending, jj > id) reaches them.  Pairs farther apart than
-// the lubrication range contribute exact zeros in the reference and are
-// skipped after a single-precision range test with a wide margin.
+// the lubrication range contribute exact zeros in the reference; the warp
+// finds the near partners with a single-precision range test (wide margin)
+// and lane 0 adds their FP64 contributions in id order.
+__device__ __forceinline__ bool near_pair(const Geometry& g, const double* y, int p, int q,
+                                          float lim) {
+  float dx = fabsf((float)y[3 * q] - (float)y[3 * p]);
+  float dy = fabsf((float)y[3 * q + 1] - (float)y[3 * p + 1]);
+  float dz = fabsf((float)y[3 * q + 2] - (float)y[3 * p + 2]);
+  if (!g.channel) dx = fminf(dx, (float)g.nx - dx);
+  dy = fminf(dy, (float)g.ny - dy);
+  dz = fminf(dz, (float)g.nz - dz);
+  return dx <= lim && dy <= lim && dz <= lim && dx * dx + dy * dy + dz * dz <= lim * lim;
+}
+
 __global__ void k_lubforce(Geometry g, int npart, PartParams pp, MoveState ms) {
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (p >= npart) return;
   const bool channel = g.channel != 0;
   const double rad = pp.rad, mingap = pp.mingap;
@@ -472,37 +645,38 @@ __global__ void k_lubforce(Geometry g, int npart, PartParams pp, MoveState ms) {
   const float lim = (float)(dist0 + 1.0);
   const double* y = ms.ypglb;
   double acc[3] = {0.0, 0.0, 0.0};
-  const float fpx = (float)y[3 * p], fpy = (float)y[3 * p + 1], fpz = (float)y[3 * p + 2];
-  for (int q = 0; q < npart; ++q) {
-    if (q == p) continue;
-    float dx = fabsf((float)y[3 * q] - fpx), dy = fabsf((float)y[3 * q + 1] - fpy),
-          dz = fabsf((float)y[3 * q + 2] - fpz);
-    if (!channel) dx = fminf(dx, (float)g.nx - dx);
-    dy = fminf(dy, (float)g.ny - dy);
-    dz = fminf(dz, (float)g.nz - dz);
-    if (dx > lim || dy > lim || dz > lim || dx * dx + dy * dy + dz * dz > lim * lim) continue;
-    // the pair as the reference evaluates it: centre "c" is the lower id
-    int id = min(p, q), jj = max(p, q);
-    double xc = y[3 * id], yc = y[3 * id + 1], zc = y[3 * id + 2];
-    double xb = y[3 * jj], yb = y[3 * jj + 1], zb = y[3 * jj + 2];
-    if (!channel) xb = near_img(xb, xc, g.nx, g.nxh);
-    yb = near_img(yb, yc, g.ny, g.nyh);
-    zb = near_img(zb, zc, g.nz, g.nzh);
-    double dxij = xc - xb, dyij = yc - yb, dzij = zc - zb;
-    double dist = sqrt(dxij * dxij + dyij * dyij + dzij * dzij);
-    double hgap = dist - 2.0 * rad;
-    if (!(dist < dist0)) continue;
-    double dist1 = 0.0;
-    if (hgap < 0.0) dist1 = -hgap;
-    double t = (dist0 - dist) / mingap;
-    double fp = (t * t / pp.stf0 + dist1 / mingap / pp.stf1) * pp.fpc;
-    double fpd = fp / dist;
-    if (p == id) {
-      acc[0] = acc[0] + fpd * dxij; acc[1] = acc[1] + fpd * dyij; acc[2] = acc[2] + fpd * dzij;
-    } else {
-      acc[0] = acc[0] - fpd * dxij; acc[1] = acc[1] - fpd * dyij; acc[2] = acc[2] - fpd * dzij;
+  for (int q0 = 0; q0 < npart; q0 += 32) {
+    const int qq = q0 + lane;
+    const bool cand = qq < npart && qq != p && near_pair(g, y, p, qq, lim);
+    unsigned m = __ballot_sync(0xffffffffu, cand);
+    if (lane != 0) continue;
+    while (m) {
+      const int q = q0 + __ffs(m) - 1;
+      m &= m - 1;
+      // the pair as the reference evaluates it: centre "c" is the lower id
+      const int id = min(p, q), jj = max(p, q);
+      double xc = y[3 * id], yc = y[3 * id + 1], zc = y[3 * id + 2];
+      double xb = y[3 * jj], yb = y[3 * jj + 1], zb = y[3 * jj + 2];
+      if (!channel) xb = near_img(xb, xc, g.nx, g.nxh);
+      yb = near_img(yb, yc, g.ny, g.nyh);
+      zb = near_img(zb, zc, g.nz, g.nzh);
+      double dxij = xc - xb, dyij = yc - yb, dzij = zc - zb;
+      double dist = sqrt(dxij * dxij + dyij * dyij + dzij * dzij);
+      double hgap = dist - 2.0 * rad;
+      if (!(dist < dist0)) continue;
+      double dist1 = 0.0;
+      if (hgap < 0.0) dist1 = -hgap;
+      double t = (dist0 - dist) / mingap;
+      double fp = (t * t / pp.stf0 + dist1 / mingap / pp.stf1) * pp.fpc;
+      double fpd = fp / dist;
+      if (p == id) {
+        acc[0] = acc[0] + fpd * dxij; acc[1] = acc[1] + fpd * dyij; acc[2] = acc[2] + fpd * dzij;
+      } else {
+        acc[0] = acc[0] - fpd * dxij; acc[1] = acc[1] - fpd * dyij; acc[2] = acc[2] - fpd * dzij;
+      }
     }
   }
+  if (lane != 0) return;
   if (channel) {
     // particle-wall lubrication, C/partlib.f90:2316-2355
     const double mw = pp.mingap_w;
@@ -594,73 +768,56 @@ __global__ void k_wrap(Geometry g, int npart, MoveState ms) {
 }
 
 // ovlpchk after a move (hgap = dist - 2 rad < 0 aborts the reference,
-// B/partlib.f90:2630-2646); here it raises LBM_ERR_OVERLAP.
+// B/partlib.f90:2630-2646); here it raises LBM_ERR_OVERLAP.  One warp per
+// particle, partners with a larger id.
 __global__ void k_overlap(Geometry g, int npart, PartParams pp, MoveState ms, DevStatus* st) {
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (p >= npart) return;
   const bool channel = g.channel != 0;
   const double* y = ms.ypglb;
   const double xc = y[3 * p], yc = y[3 * p + 1], zc = y[3 * p + 2];
   const float lim = (float)(2.0 * pp.rad + 1.0);
-  for (int q = p + 1; q < npart; ++q) {
-    float dx = fabsf((float)y[3 * q] - (float)xc), dy = fabsf((float)y[3 * q + 1] - (float)yc),
-          dz = fabsf((float)y[3 * q + 2] - (float)zc);
-    if (!channel) dx = fminf(dx, (float)g.nx - dx);
-    dy = fminf(dy, (float)g.ny - dy);
-    dz = fminf(dz, (float)g.nz - dz);
-    if (dx > lim || dy > lim || dz > lim) continue;
+  for (int q = p + 1 + lane; q < npart; q += 32) {
+    if (!near_pair(g, y, p, q, lim)) continue;
     double xb = y[3 * q], yb = y[3 * q + 1], zb = y[3 * q + 2];
     if (!channel) xb = near_img(xb, xc, g.nx, g.nxh);
     yb = near_img(yb, yc, g.ny, g.nyh);
     zb = near_img(zb, zc, g.nz, g.nzh);
     double dist = sqrt((xc - xb) * (xc - xb) + (yc - yb) * (yc - yb) + (zc - zb) * (zc - zb));
     double hgap = dist - 2.0 * pp.rad;
-    if (hgap < 0.0) { raise_error(st, LBM_ERR_OVERLAP, p); return; }
+    if (hgap < 0.0) raise_error(st, LBM_ERR_OVERLAP, p);
   }
 }
 
-// feqpnt, B/partlib.f90:3222-3247
-__device__ void feqpnt(double u9, double v9, double w9, double rho9, double* feq9) {
-  double usqr = u9 * u9 + v9 * v9 + w9 * w9;
-  usqr = 1.5 * usqr;
-  feq9[0] = (1.0 / 3.0) * (rho9 - usqr);
-#pragma unroll
-  for (int ip = 1; ip < NPOP; ++ip) {
-    double G = cix(ip) * u9 + ciy(ip) * v9 + ciz(ip) * w9;
-    double w = ip <= 6 ? 1.0 / 18.0 : 1.0 / 36.0;
-    feq9[ip] = w * (rho9 + 3.0 * G + 4.5 * G * G - usqr);
-  }
-}
-
-// beads_filling, one block per particle: scans the particle's previous
-// bounding box for nodes it covered last step (isnodes0 == p) that are
-// fluid now, and refills them (B/partlib.f90:2846-3094).  Reads only nodes
-// that are fluid in both steps, writes only refilled nodes.
-template <typename T>
-__global__ void __launch_bounds__(PB) k_filling(Geometry g, ParticleView pv, PartParams pp,
-                                                const double* __restrict__ ypglbp,
-                                                const double* __restrict__ wpp,
-                                                const double* __restrict__ omgpp,
-                                                const int32_t* __restrict__ isnodes,
-                                                const int32_t* __restrict__ isnodes0, T* f) {
+// beads_filling (B/partlib.f90:2846-3094), in two kernels.
+// k_fill_detect: one block per particle scans the particle's previous
+// bounding box for nodes it covered last step (isnodes0 == p) that are fluid
+// now and appends them to an event list.
+// k_fill_events: one warp per event refills the node.  A refill reads only
+// nodes that are fluid in both steps and writes only its own node, so the
+// events are independent and their order does not matter.
+__global__ void __launch_bounds__(PB) k_fill_detect(Geometry g, ParticleView pv, PartParams pp,
+                                                    const double* __restrict__ ypglbp,
+                                                    const int32_t* __restrict__ isnodes,
+                                                    const int32_t* __restrict__ isnodes0,
+                                                    FillList fl, DevStatus* st) {
   const int id = blockIdx.x;
   if (id >= pv.npart) return;
   const bool channel = g.channel != 0;
-  const double rad = pp.rad;
   const double cx0 = ypglbp[3 * id], cy0 = ypglbp[3 * id + 1], cz0 = ypglbp[3 * id + 2];
-  // bounding box of the nodes covered at the previous step (0-based node
-  // i has centre i + 0.5)
-  const int r = (int)ceil(rad) + 2;
+  if (!(isfinite(cx0) && isfinite(cy0) && isfinite(cz0))) return;
+  // bounding box of the nodes covered at the previous step (0-based node i
+  // has centre i + 0.5)
+  const int r = (int)ceil(pp.rad) + 2;
   const int bx0 = (int)floor(cx0 - 0.5) - r, by0 = (int)floor(cy0 - 0.5) - r,
             bz0 = (int)floor(cz0 - 0.5) - r;
   const int w = 2 * r + 2;
   const int wx = min(w, g.nx), wy = min(w, g.ny), wz = min(w, g.nz);
-  const long long total = (long long)wx * wy * wz;
-  const double sq2 = sqrt(2.0);
-  for (long long t = threadIdx.x; t < total; t += PB) {
-    int ox = (int)(t % wx);
-    long long rr = t / wx;
-    int oy = (int)(rr % wy), oz = (int)(rr / wy);
+  const int total = wx * wy * wz;
+  for (int t = threadIdx.x; t < total; t += PB) {
+    int ox = t % wx, rr = t / wx;
+    int oy = rr % wy, oz = rr / wy;
     int i = bx0 + ox, j = by0 + oy, k = bz0 + oz;
     if (channel) {
       if (i < 0 || i >= g.nx) continue;
@@ -669,99 +826,166 @@ __global__ void __launch_bounds__(PB) k_filling(Geometry g, ParticleView pv, Par
     }
     j = ((j % g.ny) + g.ny) % g.ny;
     k = ((k % g.nz) + g.nz) % g.nz;
-    long long n = (long long)i + (long long)g.nx * (j + (long long)g.ny * k);
-    if (!(isnodes0[n] == id && isnodes[n] < 0)) continue;
-    double xc = cx0 * 1.0, yc = cy0 * 1.0, zc = cz0 * 1.0;
-    double xpnt = (double)(i + 1) - 0.5, ypnt = (double)(j + 1) - 0.5 + 0.0, zpnt = (double)(k + 1) - 0.5 + 0.0;
+    const int n = i + g.nx * (j + g.ny * k);
+    if (isnodes0[n] != id || isnodes[n] >= 0) continue;
+    const int e = atomicAdd(fl.count, 1);
+    if (e < fl.cap) {
+      fl.node[e] = n;
+      fl.part[e] = id;
+    } else {
+      raise_error(st, LBM_ERR_CAPACITY, id);
+    }
+  }
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ int warp_sum(int v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// equilibrium of one population, feqpnt (B/partlib.f90:3222-3247)
+template <typename R>
+__device__ __forceinline__ R feq_q(int q, R u9, R v9, R w9, R rho9) {
+  R usqr = R(1.5) * (u9 * u9 + v9 * v9 + w9 * w9);
+  if (q == 0) return R(1.0 / 3.0) * (rho9 - usqr);
+  R G = R(cix(q)) * u9 + R(ciy(q)) * v9 + R(ciz(q)) * w9;
+  R wq = q <= 6 ? R(1.0 / 18.0) : R(1.0 / 36.0);
+  return wq * (rho9 + R(3.0) * G + R(4.5) * G * G - usqr);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_fill_events(Geometry g, ParticleView pv, PartParams pp,
+                                                     const double* __restrict__ ypglbp,
+                                                     const double* __restrict__ wpp,
+                                                     const double* __restrict__ omgpp,
+                                                     const int32_t* __restrict__ isnodes,
+                                                     const int32_t* __restrict__ isnodes0, T* f,
+                                                     FillList fl) {
+  using R = T;  // refill arithmetic in the population precision
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int nev = min(*fl.count, fl.cap);
+  const bool channel = g.channel != 0;
+  const double rad = pp.rad;
+  for (int e = warp; e < nev; e += nwarps) {
+    const int n = fl.node[e];
+    const int id = fl.part[e];
+    const int i = n % g.nx, jk = n / g.nx;
+    const int j = jk % g.ny, k = jk / g.ny;
+    // back-trace of the surface point and the lattice direction closest to
+    // the surface normal (partlib.f90:2861-2925); centre offsets in FP64
+    double xc = ypglbp[3 * id], yc = ypglbp[3 * id + 1], zc = ypglbp[3 * id + 2];
+    const double xpnt = (double)(i + 1) - 0.5, ypnt = (double)(j + 1) - 0.5 + 0.0,
+                 zpnt = (double)(k + 1) - 0.5 + 0.0;
     if (!channel) xc = near_img(xc, xpnt, g.nx, g.nxh);
     yc = near_img(yc, ypnt, g.ny, g.nyh);
     zc = near_img(zc, zpnt, g.nz, g.nzh);
-    double w1 = -0.5 * (pv.wp[3 * id] * 1.0 + wpp[3 * id] * 1.0);
-    double w2 = -0.5 * (pv.wp[3 * id + 1] * 1.0 + wpp[3 * id + 1] * 1.0);
-    double w3 = -0.5 * (pv.wp[3 * id + 2] * 1.0 + wpp[3 * id + 2] * 1.0);
-    double omg1 = -0.5 * (pv.omgp[3 * id] * 1.0 + omgpp[3 * id] * 1.0);
-    double omg2 = -0.5 * (pv.omgp[3 * id + 1] * 1.0 + omgpp[3 * id + 1] * 1.0);
-    double omg3 = -0.5 * (pv.omgp[3 * id + 2] * 1.0 + omgpp[3 * id + 2] * 1.0);
-    double aa = w1 * w1 + w2 * w2 + w3 * w3;
-    double bb = (xpnt - xc) * w1 + (ypnt - yc) * w2 + (zpnt - zc) * w3;
-    double cc = (xpnt - xc) * (xpnt - xc) + (ypnt - yc) * (ypnt - yc) +
-                (zpnt - zc) * (zpnt - zc) - (rad * 1.0) * (rad * 1.0);
-    double ddt0 = bb / aa;
-    double ddt1 = sqrt(ddt0 * ddt0 - cc / aa);
-    double ddt = -ddt0 + ddt1;
-    if (ddt < 0.0) ddt = 0.0;
-    if (ddt > 1.0) ddt = 1.0;
-    double xp1 = xpnt + w1 * ddt, yp1 = ypnt + w2 * ddt, zp1 = zpnt + w3 * ddt;
-    double xp2 = xp1 + (omg2 * (zp1 - zc) - omg3 * (yp1 - yc)) * ddt;
-    double yp2 = yp1 + (omg3 * (xp1 - xc) - omg1 * (zp1 - zc)) * ddt;
-    double zp2 = zp1 + (omg1 * (yp1 - yc) - omg2 * (xp1 - xc)) * ddt;
-    double xx0 = xp2 - xc, yy0 = yp2 - yc, zz0 = zp2 - zc;
-    double prod0 = -100.0;
+    const R dx = R(xpnt - xc), dy = R(ypnt - yc), dz = R(zpnt - zc);
+    const R w1 = R(-0.5 * (pv.wp[3 * id] + wpp[3 * id]));
+    const R w2 = R(-0.5 * (pv.wp[3 * id + 1] + wpp[3 * id + 1]));
+    const R w3 = R(-0.5 * (pv.wp[3 * id + 2] + wpp[3 * id + 2]));
+    const R omg1 = R(-0.5 * (pv.omgp[3 * id] + omgpp[3 * id]));
+    const R omg2 = R(-0.5 * (pv.omgp[3 * id + 1] + omgpp[3 * id + 1]));
+    const R omg3 = R(-0.5 * (pv.omgp[3 * id + 2] + omgpp[3 * id + 2]));
+    const R aa = w1 * w1 + w2 * w2 + w3 * w3;
+    const R bb = dx * w1 + dy * w2 + dz * w3;
+    const R cc = dx * dx + dy * dy + dz * dz - R(rad) * R(rad);
+    const R ddt0 = bb / aa;
+    const R ddt1 = sqrt(ddt0 * ddt0 - cc / aa);
+    R ddt = -ddt0 + ddt1;
+    if (ddt < R(0)) ddt = R(0);
+    if (ddt > R(1)) ddt = R(1);
+    const R xp1 = dx + w1 * ddt, yp1 = dy + w2 * ddt, zp1 = dz + w3 * ddt;  // relative to centre
+    const R xx0 = xp1 + (omg2 * zp1 - omg3 * yp1) * ddt;
+    const R yy0 = yp1 + (omg3 * xp1 - omg1 * zp1) * ddt;
+    const R zz0 = zp1 + (omg1 * yp1 - omg2 * xp1) * ddt;
+    const R sq2 = sqrt(R(2.0));
+    R prod0 = R(-100.0);
     int ipmx = 0;
+#pragma unroll
     for (int ipop = 1; ipop < NPOP; ++ipop) {
-      double prod = (double)cix(ipop) * xx0 + (double)ciy(ipop) * yy0 + (double)ciz(ipop) * zz0;
+      R prod = R(cix(ipop)) * xx0 + R(ciy(ipop)) * yy0 + R(ciz(ipop)) * zz0;
       if (ipop <= 6) prod = prod * sq2;
       if (prod > prod0) { ipmx = ipop; prod0 = prod; }
     }
-    double fnew[NPOP], f9[NPOP], feq9[NPOP];
-    bool have = false;
-    if (ipmx > 0) {
-      int i2 = i + cix(ipmx);
+    // non-equilibrium part copied from the neighbour along ipmx if it is
+    // fluid in both steps (partlib.f90:2963-2995); lane q holds population q
+    const int q = lane < NPOP ? lane : 0;
+    R fnew = R(0);
+    {
+      bool have = false;
+      int m = 0;
+      if (ipmx > 0) {
+        int i2 = i + cix(ipmx);
+        bool ok = true;
+        if (channel) ok = i2 >= 0 && i2 < g.nx;
+        else i2 = wrapi(i2, g.nx);
+        if (ok) {
+          const int j2 = wrapi(j + ciy(ipmx), g.ny), k2 = wrapi(k + ciz(ipmx), g.nz);
+          m = i2 + g.nx * (j2 + g.ny * k2);
+          have = isnodes[m] < 0 && isnodes0[m] < 0;
+        }
+      }
+      if (have) {
+        const R fq = lane < NPOP ? R(f[(size_t)q * g.N + m]) : R(0);
+        const R rho9 = warp_sum(fq);
+        const R u9 = warp_sum(R(cix(q)) * fq);
+        const R v9 = warp_sum(R(ciy(q)) * fq);
+        const R ww9 = warp_sum(R(ciz(q)) * fq);
+        fnew = fq - feq_q<R>(q, u9, v9, ww9, rho9);
+      }
+    }
+    // local mean density of the neighbours fluid in both steps
+    // (partlib.f90:3008-3065); lane d-1 handles neighbour d
+    int cnt = 0;
+    R rs = R(0);
+    if (lane < 18) {
+      const int d = lane + 1;
+      int i2 = i + cix(d);
       bool ok = true;
       if (channel) ok = i2 >= 0 && i2 < g.nx;
       else i2 = wrapi(i2, g.nx);
       if (ok) {
-        int j2 = wrapi(j + ciy(ipmx), g.ny), k2 = wrapi(k + ciz(ipmx), g.nz);
-        long long m = (long long)i2 + (long long)g.nx * (j2 + (long long)g.ny * k2);
+        const int j2 = wrapi(j + ciy(d), g.ny), k2 = wrapi(k + ciz(d), g.nz);
+        const int m = i2 + g.nx * (j2 + g.ny * k2);
         if (isnodes[m] < 0 && isnodes0[m] < 0) {
-          have = true;
-          double rho9 = 0.0, u9 = 0.0, v9 = 0.0, ww9 = 0.0;
-          for (int ip = 0; ip < NPOP; ++ip) f9[ip] = (double)f[ip * g.N + m];
-          for (int ip = 0; ip < NPOP; ++ip) {
-            rho9 = rho9 + f9[ip];
-            u9 = u9 + (double)cix(ip) * f9[ip];
-            v9 = v9 + (double)ciy(ip) * f9[ip];
-            ww9 = ww9 + (double)ciz(ip) * f9[ip];
-          }
-          feqpnt(u9, v9, ww9, rho9, feq9);
-          for (int ip = 0; ip < NPOP; ++ip) fnew[ip] = f9[ip] - feq9[ip];
+          cnt = 1;
+#pragma unroll
+          for (int ii = 0; ii < NPOP; ++ii) rs += R(f[(size_t)ii * g.N + m]);
         }
       }
     }
-    if (!have)
-      for (int ip = 0; ip < NPOP; ++ip) fnew[ip] = 0.0;
-    int nghb = 0;
-    double rho9 = 0.0;
-    for (int ipop = 1; ipop < NPOP; ++ipop) {
-      int i2 = i + cix(ipop);
-      if (channel) { if (i2 < 0 || i2 >= g.nx) continue; }
-      else i2 = wrapi(i2, g.nx);
-      int j2 = wrapi(j + ciy(ipop), g.ny), k2 = wrapi(k + ciz(ipop), g.nz);
-      long long m = (long long)i2 + (long long)g.nx * (j2 + (long long)g.ny * k2);
-      if (isnodes[m] < 0 && isnodes0[m] < 0) {
-        nghb = nghb + 1;
-        for (int ii = 0; ii < NPOP; ++ii) rho9 = rho9 + (double)f[ii * g.N + m];
-      }
-    }
-    if (nghb > 0) rho9 = rho9 / (double)nghb;
-    else rho9 = channel ? 0.0 : pp.rho0;
-    xx0 = xpnt - xc; yy0 = ypnt - yc; zz0 = zpnt - zc;
-    w1 = pv.wp[3 * id]; w2 = pv.wp[3 * id + 1]; w3 = pv.wp[3 * id + 2];
-    omg1 = pv.omgp[3 * id]; omg2 = pv.omgp[3 * id + 1]; omg3 = pv.omgp[3 * id + 2];
-    double u9 = w1 + omg2 * zz0 - omg3 * yy0;
-    double v9 = w2 + omg3 * xx0 - omg1 * zz0;
-    double ww9 = w3 + omg1 * yy0 - omg2 * xx0;
-    feqpnt(u9, v9, ww9, rho9, feq9);
-    for (int ip = 0; ip < NPOP; ++ip) f[ip * g.N + n] = T(fnew[ip] + feq9[ip]);
+    const int nghb = warp_sum(cnt);
+    const R rsum = warp_sum(rs);
+    const R rho9 = nghb > 0 ? rsum / R(nghb) : (channel ? R(0) : R(pp.rho0));
+    // equilibrium with the rigid-body velocity at the node
+    const R wx = R(pv.wp[3 * id]), wy = R(pv.wp[3 * id + 1]), wz = R(pv.wp[3 * id + 2]);
+    const R ox = R(pv.omgp[3 * id]), oy = R(pv.omgp[3 * id + 1]), oz = R(pv.omgp[3 * id + 2]);
+    const R u9 = wx + oy * dz - oz * dy;
+    const R v9 = wy + oz * dx - ox * dz;
+    const R w9 = wz + ox * dy - oy * dx;
+    if (lane < NPOP) f[(size_t)q * g.N + n] = T(fnew + feq_q<R>(q, u9, v9, w9, rho9));
   }
 }
 
 }  // namespace
 
 void launch_links(const Geometry& g, const ParticleView& pv, int32_t* isnodes, LinkSlab ls,
-                  DevStatus* st, cudaStream_t s) {
+                  DevStatus* st, int alpha_fp32, cudaStream_t s) {
   if (pv.npart <= 0) return;
-  k_links<<<pv.npart, PB, 0, s>>>(g, pv, isnodes, ls, st);
+  { k_links<<<pv.npart, PB, 0, s>>>(g, pv, isnodes, ls, st, alpha_fp32); count_launch(); }
 }
 
 template <typename T>
@@ -769,42 +993,45 @@ void launch_bounce_back(const Geometry& g, const ParticleView& pv, const T* f, i
                         const int32_t* isnodes, LinkSlab ls, double* fHIp, double* torqp,
                         cudaStream_t s) {
   if (pv.npart <= 0) return;
-  k_bounce<T><<<pv.npart, PB, 0, s>>>(g, pv, f, pushed, isnodes, ls, fHIp, torqp);
+  { k_bounce<T><<<pv.npart, PB, 0, s>>>(g, pv, f, pushed, isnodes, ls, fHIp, torqp); count_launch(); }
 }
 
 template <typename T>
 void launch_bounce_scatter(const Geometry& g, const ParticleView& pv, T* f, int pushed,
                            LinkSlab ls, cudaStream_t s) {
   if (pv.npart <= 0) return;
-  k_bounce_store<T><<<pv.npart, PB, 0, s>>>(g, pv, f, pushed, ls);
+  { k_bounce_store<T><<<pv.npart, PB, 0, s>>>(g, pv, f, pushed, ls); count_launch(); }
 }
 
 void launch_lubforce(const Geometry& g, int npart, const PartParams& pp, MoveState ms,
                      cudaStream_t s) {
   if (npart <= 0) return;
-  k_lubforce<<<(npart + 127) / 128, 128, 0, s>>>(g, npart, pp, ms);
+  { k_lubforce<<<(npart * 32 + 127) / 128, 128, 0, s>>>(g, npart, pp, ms); count_launch(); }
 }
 
 void launch_move(const Geometry& g, int npart, const PartParams& pp, MoveState ms,
                  cudaStream_t s) {
   if (npart <= 0) return;
-  k_move<<<(npart + 127) / 128, 128, 0, s>>>(npart, pp, ms);
-  k_clear_first<<<1, 1, 0, s>>>(ms.first_move);
+  { k_move<<<(npart + 127) / 128, 128, 0, s>>>(npart, pp, ms); count_launch(); }
+  { k_clear_first<<<1, 1, 0, s>>>(ms.first_move); count_launch(); }
 }
 
 void launch_redistribute(const Geometry& g, int npart, const PartParams& pp, MoveState ms,
                          DevStatus* st, cudaStream_t s) {
   if (npart <= 0) return;
-  k_wrap<<<(npart + 127) / 128, 128, 0, s>>>(g, npart, ms);
-  k_overlap<<<(npart + 127) / 128, 128, 0, s>>>(g, npart, pp, ms, st);
+  { k_wrap<<<(npart + 127) / 128, 128, 0, s>>>(g, npart, ms); count_launch(); }
+  { k_overlap<<<(npart * 32 + 127) / 128, 128, 0, s>>>(g, npart, pp, ms, st); count_launch(); }
 }
 
 template <typename T>
 void launch_filling(const Geometry& g, const ParticleView& pv, const PartParams& pp,
                     const double* ypglbp, const double* wpp, const double* omgpp,
-                    const int32_t* isnodes, const int32_t* isnodes0, T* f, cudaStream_t s) {
+                    const int32_t* isnodes, const int32_t* isnodes0, T* f, FillList fl,
+                    DevStatus* st, cudaStream_t s) {
   if (pv.npart <= 0) return;
-  k_filling<T><<<pv.npart, PB, 0, s>>>(g, pv, pp, ypglbp, wpp, omgpp, isnodes, isnodes0, f);
+  cudaMemsetAsync(fl.count, 0, sizeof(int), s);
+  { k_fill_detect<<<pv.npart, PB, 0, s>>>(g, pv, pp, ypglbp, isnodes, isnodes0, fl, st); count_launch(); }
+  { k_fill_events<T><<<4 * 152, 128, 0, s>>>(g, pv, pp, ypglbp, wpp, omgpp, isnodes, isnodes0, f, fl); count_launch(); }
 }
 
 template void launch_bounce_back<double>(const Geometry&, const ParticleView&, const double*,
@@ -819,9 +1046,11 @@ template void launch_bounce_scatter<float>(const Geometry&, const ParticleView&,
                                            LinkSlab, cudaStream_t);
 template void launch_filling<double>(const Geometry&, const ParticleView&, const PartParams&,
                                      const double*, const double*, const double*,
-                                     const int32_t*, const int32_t*, double*, cudaStream_t);
+                                     const int32_t*, const int32_t*, double*, FillList,
+                                     DevStatus*, cudaStream_t);
 template void launch_filling<float>(const Geometry&, const ParticleView&, const PartParams&,
                                     const double*, const double*, const double*,
-                                    const int32_t*, const int32_t*, float*, cudaStream_t);
+                                    const int32_t*, const int32_t*, float*, FillList,
+                                    DevStatus*, cudaStream_t);
 
 }  // namespace lbm

@@ -73,6 +73,28 @@ class LBMBox:
     def synchronize(self):
         self._ck(self._L.lbm_synchronize(self._h), "lbm_synchronize")
 
+    def set_stream(self, stream_ptr: int):
+        """Run all work of this box on the given cudaStream_t (an integer)."""
+        self._ck(self._L.lbm_set_stream(self._h, C.c_void_p(stream_ptr)), "set_stream")
+
+    def profile(self, enable: bool = True):
+        """Start (and clear) or stop per-phase CUDA-event timing of step()."""
+        self._ck(self._L.lbm_profile(self._h, 1 if enable else 0), "profile")
+
+    def profile_read(self) -> dict:
+        """{phase: (total ms, timed intervals)} since profile(True)."""
+        out = {}
+        for i, name in enumerate(capi.PHASES):
+            ms = C.c_double(0.0)
+            n = C.c_int64(0)
+            self._ck(self._L.lbm_profile_read(self._h, i, C.byref(ms), C.byref(n)), "profile_read")
+            out[name] = (ms.value, int(n.value))
+        return out
+
+    @staticmethod
+    def kernel_launches() -> int:
+        return int(capi.lib().lbm_kernel_launches())
+
     # ---- populations -----------------------------------------------------
     def set_f(self, f: np.ndarray):
         f = np.ascontiguousarray(f, dtype=np.float64).reshape(19, self.nz, self.ny, self.nx)

@@ -180,7 +180,8 @@ struct Oracle {
     aip = 0.4 * amp * (cfg.rad * cfg.rad);
     tscale = pi2 * cfg.vscale / (double)ny;            // para.f90:60
     // forcing wavenumbers for the 6x5x5 low-mode block, para.f90:260-286
-    for (int i = 1; i <= 6; ++i) kxr6[i - 1] = (double)(i / 2);
+    // kxr(i) = int(i/2) for odd i and kxr(i+1) = kxr(i): 0, 0, 1, 1, 2, 2
+    for (int i = 1; i <= 6; ++i) kxr6[i - 1] = (double)((i - 1) / 2);
     for (int j = 1; j <= 5; ++j) {
       int jj = (j > 3) ? j + ny - 5 : j;
       kyr5[j - 1] = (jj < ny / 2 + 2) ? (double)(jj - 1) : (double)(-(ny + 1 - jj));
