@@ -197,6 +197,31 @@ int lbm_profile_read(lbm_ctx* ctx, int phase, double* ms_total, int64_t* count);
 /* number of kernels this library has launched in this process */
 int64_t lbm_kernel_launches(void);
 
+/* ---- allocation-free diagnostics ----------------------------------------- */
+/* No counterpart in the reference.  Mass and momentum totals (out[0] = sum
+ * f, out[1..3] = sum c f) of a population field the caller already holds on
+ * the device, for callers that cannot allocate: a host solver that has
+ * reserved the GPU's memory for its own state and forbids further
+ * allocation, or an embedding runtime that owns all device memory through
+ * its own pool.  Nothing is allocated (no cudaMalloc, cudaFree or allocating
+ * library call; no context needed).
+ *   f       device pointer, 19*nx*ny*nz doubles laid out f[q][z][y][x]
+ *   out     device pointer to 4 doubles
+ *   stream  cudaStream_t to run on (NULL: the legacy default stream); the
+ *           call returns after enqueueing, out is ready when the stream is
+ * Scratch is one file-scope 256-byte-aligned device array of
+ * LBM_NOALLOC_MAX_PLANES x 4 doubles (128 KiB) that every GPU loading this
+ * library holds until the process exits; nz > LBM_NOALLOC_MAX_PLANES is
+ * rejected with LBM_ERR_ARG.  All calls share that array and it keeps the
+ * last call's partial sums: calls that overlap on one GPU (for example on
+ * two streams) race on it, so the caller must order them.  No entry needs
+ * clearing between calls (each call writes every entry it reads).  The first
+ * call on each device looks up
+ * the array's device address with that device current; make that first call
+ * before any stream capture. */
+#define LBM_NOALLOC_MAX_PLANES 4096
+int lbm_mass_momentum_noalloc(const double* f, int nx, int ny, int nz, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

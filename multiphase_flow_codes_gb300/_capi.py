@@ -102,6 +102,7 @@ SIGNATURES = {
     "lbm_profile": (C.c_int, [_P, C.c_int]),
     "lbm_profile_read": (C.c_int, [_P, C.c_int, _D, C.POINTER(C.c_int64)]),
     "lbm_kernel_launches": (C.c_int64, []),
+    "lbm_mass_momentum_noalloc": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, _P]),
 }
 
 PHASES = ("stream_collide", "bounce", "particles", "links", "filling", "forcing")

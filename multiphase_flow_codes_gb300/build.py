@@ -31,6 +31,7 @@ UNITS = [
     ("lbm_forcing.cu", ["-fmad=false"]),
     ("lbm_particles.cu", ["-fmad=false"]),
     ("lbm_capi.cu", []),
+    ("lbm_noalloc.cu", []),
 ]
 
 
