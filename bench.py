@@ -162,6 +162,8 @@ def run_device(wl, u, y, steps, warmup, device, want_f=False):
     box.macrovar()
     if wl.npart:
         box.release_particles(y)
+    box.autotune(reps=3)          # pick the stream+collide variant on this state
+    variant = box.variant()
     for _ in range(warmup):
         box.step(1)
     box.synchronize()
@@ -183,14 +185,26 @@ def run_device(wl, u, y, steps, warmup, device, want_f=False):
     f = box.get_f() if want_f else None
     parts = box.get_particles() if (want_f and wl.npart) else None
     box.close()
-    return ms, launches, phases, f, parts
+    return ms, launches, phases, f, parts, variant
 
 
-def run_e2e(wl, f0_fortran, y, steps, device):
+def kernel_name(variant):
+    v, st, groups, per_sm = variant
+    if v == 3:
+        return (f"k_fused_staged_x2 (stream + MRT collide + forcing, FP32 pairs on f32x2; "
+                f"{st} stages, {groups} consumer groups, {per_sm} CTAs/SM)")
+    if v == 2:
+        return f"k_fused_staged (stream + MRT collide + forcing; {st} stages, {per_sm} CTAs/SM)"
+    return "k_fused (stream + MRT collide + forcing; direct)"
+
+
+def run_e2e(wl, f0_fortran, y, steps, device, variant=None):
     """End to end through the C ABI with host buffers (see module doc)."""
     import torch
     from multiphase_flow_codes_gb300.engine import LBMBox
     box = LBMBox(wl.cfg)
+    if variant is not None:
+        box.set_variant(*variant)
     npart = y.shape[0]
     pin = torch.empty(f0_fortran.size, dtype=torch.float64, pin_memory=True).numpy()
     hf = np.ndarray(f0_fortran.shape, dtype=np.float64, buffer=pin, order="F")
@@ -337,7 +351,7 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     sampler.start()
-    ms, launches, phases, f64, p64 = run_device(wl, u, y, args.steps, args.warmup, local,
+    ms, launches, phases, f64, p64, variant = run_device(wl, u, y, args.steps, args.warmup, local,
                                                want_f=not args.no_fp32)
     clocks = sampler.stop()
     t_ms = ms
@@ -361,15 +375,20 @@ def main():
         traffic = figs[key]["dram_bytes_per_node"] * N
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
-            "kernel": "k_fused (stream + MRT collide + forcing)",
+            "kernel": kernel_name(variant),
             "alg_bytes_per_launch": alg_bytes, "peak_source": peak_src}
     fp64 = {}
-    fp64_peak = figs.get("fp64_fma_tflops")
     if dtype == "f64" and key in figs and figs[key].get("fp64_flop_per_node") and sc_n:
+        import ctypes as C
+        peak = C.c_double(0.0)
+        rc = capi.lib().lbm_fma_throughput(capi.LBM_PREC_F64, C.byref(peak))
+        fp64_peak = peak.value if rc == 0 and peak.value > 0 else None
         tf = figs[key]["fp64_flop_per_node"] * N / (sc_ms / sc_n / 1e3) / 1e12
         fp64 = {"achieved_tflops": tf, "peak_tflops": fp64_peak,
-                "frac": tf / fp64_peak if fp64_peak else None,
-                "note": "FP64 FMA peak measured on this GPU; the FP64 kernel is FP64-issue bound"}
+                "frac": tf / fp64_peak if fp64_peak else None, "unit": "TFLOP/s",
+                "flop_per_node": figs[key]["fp64_flop_per_node"],
+                "note": "FP64 FMA peak measured live on this GPU (lbm_fma_throughput); FP64 flops "
+                        "per node from the ncu instruction counters; the FP64 kernel is FP64-issue bound"}
 
     line = {"metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms / args.steps,
@@ -385,7 +404,7 @@ def main():
         wl32 = config.config2() if args.workload in ("config1", "box256_p1000_f64") else workload(args.workload)
         if wl32.cfg.precision != capi.LBM_PREC_F32:
             wl32.cfg.precision = capi.LBM_PREC_F32
-        ms32, l32, ph32, f32, p32 = run_device(wl32, u, y, args.steps, args.warmup, local, want_f=True)
+        ms32, l32, ph32, f32, p32, variant32 = run_device(wl32, u, y, args.steps, args.warmup, local, want_f=True)
         sc32, n32 = ph32["stream_collide"]
         ach32 = 2 * 19 * 4 * N / (sc32 / n32 / 1e3) / 1e9 if n32 else None
         err = float(np.abs(f32 - f64).max() / np.abs(f64).max())
@@ -396,7 +415,7 @@ def main():
             "value": N * args.steps * world / (ms32 / 1e3) / 1e6, "unit": "MLUPS",
             "ms_per_step": ms32 / args.steps, "vs_fp64": (N * args.steps / (ms32 / 1e3)) / (N * args.steps / (ms / 1e3)),
             "roofline": {"bound": "hbm", "achieved": ach32, "peak": hbm, "unit": "GB/s",
-                         "frac": (ach32 / hbm) if ach32 else None,
+                         "frac": (ach32 / hbm) if ach32 else None, "kernel": kernel_name(variant32),
                          "traffic": (figs.get(f"fused_f32_{c.nx}", {}).get("dram_bytes_per_node") or 0) * N or None},
             "rel_err_f_vs_fp64": err, "rel_rms_particle_force_vs_fp64": ferr,
             "error_after_steps": args.warmup + args.steps,
@@ -407,7 +426,7 @@ def main():
         f0 = initial_f(u)
         f0_fortran = np.asfortranarray(np.transpose(f0, (0, 3, 2, 1)))
         del f0
-        e_ms, h2d, d2h = run_e2e(wl, f0_fortran, y, args.steps, local)
+        e_ms, h2d, d2h = run_e2e(wl, f0_fortran, y, args.steps, local, variant)
         e_t = e_ms
         if dist:
             t = torch.tensor([e_ms], device=f"cuda:{local}")

@@ -173,6 +173,30 @@ int lbm_rhoupdat(lbm_ctx* ctx);           /* collision.f90:213 rhoupdat       */
  * entries above in that order. */
 int lbm_step(lbm_ctx* ctx, int nsteps);
 
+/* ---- kernel selection (no counterpart in the reference) ------------------ */
+/* Variants of the fused stream + collide kernel of lbm_step.  Both compute
+ * the same per-node arithmetic; they differ in how the populations move. */
+enum {
+  LBM_VARIANT_DIRECT = 1, /* one thread per node: loads and pushed stores straight to HBM */
+  LBM_VARIANT_STAGED = 2, /* persistent CTAs: a producer warp streams whole x-rows into
+                             shared memory with bulk copies, consumer warps collide and
+                             push them (nx a multiple of 4)                               */
+  LBM_VARIANT_STAGED_X2 = 3 /* the same in FP32 with two nodes per thread on packed f32x2
+                             arithmetic (FP32 precision, nx a multiple of 4, at most 512) */
+};
+/* Select a variant and its schedule.  For the staged variants: stages
+ * (2..8: rows in flight + 1; 0: default), groups (STAGED_X2 only: groups of
+ * consumer warps, each colliding its own row; 0: one) and ctas_per_sm (0: as
+ * many as fit).  LBM_ERR_ARG when the variant or schedule does not apply to
+ * this box.  A new context uses, where it applies, STAGED_X2 in FP32, else
+ * STAGED in FP32, else DIRECT. */
+int lbm_set_variant(lbm_ctx* ctx, int variant, int stages, int groups, int ctas_per_sm);
+int lbm_get_variant(lbm_ctx* ctx, int* variant, int* stages, int* groups, int* ctas_per_sm);
+/* Time every applicable variant and schedule (reps launches each) on the
+ * context's current populations without advancing them, keep the fastest and
+ * report its mean milliseconds per launch.  Synchronises the stream. */
+int lbm_autotune(lbm_ctx* ctx, int reps, double* best_ms);
+
 /* ---- diagnostics --------------------------------------------------------- */
 /* FP64 totals over all nodes: out[0] = sum f (mass), out[1..3] = momentum
  * sum c f. */
@@ -196,6 +220,10 @@ int lbm_profile(lbm_ctx* ctx, int enable);
 int lbm_profile_read(lbm_ctx* ctx, int phase, double* ms_total, int64_t* count);
 /* number of kernels this library has launched in this process */
 int64_t lbm_kernel_launches(void);
+/* Measured FMA throughput (TFLOP/s, an FMA counted as 2 flops) of the
+ * current device in FP64 (precision = LBM_PREC_F64) or FP32: the compute
+ * roofline of the fused kernel.  No counterpart in the reference. */
+int lbm_fma_throughput(int precision, double* tflops);
 
 /* ---- allocation-free diagnostics ----------------------------------------- */
 /* No counterpart in the reference.  Mass and momentum totals (out[0] = sum

@@ -28,10 +28,12 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relax
 # (source, extra flags)
 UNITS = [
     ("lbm_fluid.cu", []),
+    ("lbm_staged.cu", []),
     ("lbm_forcing.cu", ["-fmad=false"]),
     ("lbm_particles.cu", ["-fmad=false"]),
     ("lbm_capi.cu", []),
     ("lbm_noalloc.cu", []),
+    ("lbm_probe.cu", []),
 ]
 
 

@@ -57,6 +57,9 @@ struct lbm_ctx {
   bool macro_derived = true;   // macro arrays equal macrovar(f) (or pending)
   int32_t* flags[2] = {nullptr, nullptr};
   int fcur = 0;
+  // stream + collide kernel (lbm_set_variant / lbm_autotune)
+  int variant = LBM_VARIANT_DIRECT;
+  StagedPlan staged;
 
   // forcing
   ForcingDev* d_forcing = nullptr;
@@ -185,8 +188,10 @@ int check_status(lbm_ctx* ctx) {
                        : s.code == LBM_ERR_CAPACITY ? "link or geometry capacity exceeded"
                        : s.code == LBM_ERR_STATE    ? "particle image sweep not at a fixed point"
                        : s.code == LBM_ERR_NONFINITE ? "non-finite particle centre"
+                       : s.code == LBM_ERR_TIMEOUT  ? "a bounded device-side wait ran out"
                                                     : "device error";
-    snprintf(buf, sizeof buf, "%s (particle %d)", what, s.where);
+    snprintf(buf, sizeof buf, "%s (%s %d)", what, s.code == LBM_ERR_TIMEOUT ? "block" : "particle",
+             s.where);
     return fail(ctx, s.code, buf);
   }
   return 0;
@@ -303,14 +308,44 @@ void particle_phase(lbm_ctx* c, T* f_plain) {
   c->fcur = nf;
 }
 
+// the fused stream + collide of the selected variant, fin -> fout
+template <typename T>
+void launch_stream_collide(lbm_ctx* c, const T* fin, T* fout) {
+  if (c->variant == LBM_VARIANT_STAGED || c->variant == LBM_VARIANT_STAGED_X2)
+    launch_fused_staged<T>(c->g, c->r, fin, fout, c->flags[c->fcur], fview<T>(c, c->fmacro),
+                           fview<T>(c, c->latest), c->staged, c->status, c->stream);
+  else
+    launch_fused_step<T>(c->g, c->r, fin, fout, c->flags[c->fcur], fview<T>(c, c->fmacro),
+                         fview<T>(c, c->latest), c->stream);
+}
+
+// plan a staged variant with `stages` stages (0: the default, four where two
+// CTAs of that size fit on an SM, else fewer) and ctas_per_sm resident CTAs
+// (0: as many as fit)
+bool plan_staged(lbm_ctx* c, int variant, int stages, int ctas_per_sm, StagedPlan* p,
+                 int groups = 1) {
+  const bool packed = variant == LBM_VARIANT_STAGED_X2;
+  if (variant != LBM_VARIANT_STAGED && !packed) return false;
+  if (stages == 0) {
+    for (int S = 4; S >= 2 && stages == 0; --S) {
+      StagedPlan t;
+      const bool ok = c->f32 ? plan_fused_staged<float>(c->g, S, 0, packed, groups, &t)
+                             : plan_fused_staged<double>(c->g, S, 0, packed, groups, &t);
+      if (ok && (t.ctas_per_sm >= 2 || S == 2)) stages = S;
+    }
+    if (stages == 0) return false;
+  }
+  return c->f32 ? plan_fused_staged<float>(c->g, stages, ctas_per_sm, packed, groups, p)
+                : plan_fused_staged<double>(c->g, stages, ctas_per_sm, packed, groups, p);
+}
+
 template <typename T>
 void fused_step_t(lbm_ctx* c) {
   do_forcing(c);
   T* fin = fbuf<T>(c, c->cur);
   T* fout = fbuf<T>(c, 1 - c->cur);
   prof_begin(c);
-  launch_fused_step<T>(c->g, c->r, fin, fout, c->flags[c->fcur], fview<T>(c, c->fmacro),
-                       fview<T>(c, c->latest), c->stream);
+  launch_stream_collide<T>(c, fin, fout);
   prof_end(c, LBM_PHASE_STREAM_COLLIDE);
   prefetch_forcing(c);
   if (c->particles_on) {
@@ -611,7 +646,7 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
     al((void**)&ctx->ztab, 45LL * g.nz * 2 * sizeof(double));
     al((void**)&ctx->ytw, 5LL * g.ny * 2 * sizeof(double));
     al((void**)&ctx->ztw, 5LL * g.nz * 2 * sizeof(double));
-    for (int s = 0; s < 3; ++s) al(&ctx->rowtab[s], 9LL * g.ny * g.nz * 2 * ctx->esz);
+    for (int s = 0; s < 3; ++s) al(&ctx->rowtab[s], (long long)kRowCoef * g.ny * g.nz * ctx->esz);
   }
   ctx->npmax = cfg->npart_max > 0 ? cfg->npart_max : 0;
   if (ctx->npmax > 0) {
@@ -710,6 +745,19 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
   if (e != cudaSuccess) {
     lbm_destroy(ctx);
     return LBM_ERR_CUDA;
+  }
+  {
+    StagedPlan p;
+    if (ctx->f32) {
+      if (plan_staged(ctx, LBM_VARIANT_STAGED_X2, 0, 0, &p)) {
+        ctx->variant = LBM_VARIANT_STAGED_X2;
+        ctx->staged = p;
+      } else if (plan_staged(ctx, LBM_VARIANT_STAGED, 0, 0, &p)) {
+        ctx->variant = LBM_VARIANT_STAGED;
+        ctx->staged = p;
+      }
+    }
+    cudaGetLastError();
   }
   *out = ctx;
   return LBM_OK;
@@ -1105,12 +1153,98 @@ int lbm_step(lbm_ctx* ctx, int nsteps) {
     }
   }
   CK(cudaGetLastError());
-  if (ctx->particles_on) {
+  if (ctx->particles_on || ctx->variant != LBM_VARIANT_DIRECT) {
     CK(cudaMemcpyAsync(ctx->status_host, ctx->status, sizeof(DevStatus), cudaMemcpyDeviceToHost,
                        ctx->stream));
     CK(cudaEventRecord(ctx->ev_status, ctx->stream));
     ctx->status_pending = true;
   }
+  return LBM_OK;
+}
+
+int lbm_set_variant(lbm_ctx* ctx, int variant, int stages, int groups, int ctas_per_sm) {
+  if (!ctx) return LBM_ERR_ARG;
+  if (variant == LBM_VARIANT_DIRECT) {
+    ctx->variant = variant;
+    return LBM_OK;
+  }
+  if ((variant != LBM_VARIANT_STAGED && variant != LBM_VARIANT_STAGED_X2) || stages < 0 ||
+      stages > 8 || groups < 0 || groups > 8 || ctas_per_sm < 0)
+    return fail(ctx, LBM_ERR_ARG, "unknown stream+collide variant or schedule");
+  StagedPlan p;
+  if (!plan_staged(ctx, variant, stages, ctas_per_sm, &p, groups == 0 ? 1 : groups)) {
+    cudaGetLastError();
+    return fail(ctx, LBM_ERR_ARG, "this stream+collide variant does not apply to this box");
+  }
+  ctx->variant = variant;
+  ctx->staged = p;
+  return LBM_OK;
+}
+
+int lbm_get_variant(lbm_ctx* ctx, int* variant, int* stages, int* groups, int* ctas_per_sm) {
+  if (!ctx) return LBM_ERR_ARG;
+  if (variant) *variant = ctx->variant;
+  const bool st = ctx->variant != LBM_VARIANT_DIRECT;
+  if (stages) *stages = st ? ctx->staged.S : 0;
+  if (groups) *groups = st ? ctx->staged.groups : 0;
+  if (ctas_per_sm) *ctas_per_sm = st ? ctx->staged.ctas_per_sm : 0;
+  return LBM_OK;
+}
+
+int lbm_autotune(lbm_ctx* ctx, int reps, double* best_ms) {
+  if (!ctx || reps < 1) return LBM_ERR_ARG;
+  if (int rc = poll_status(ctx)) return rc;
+  struct Cand { int variant; StagedPlan p; };
+  std::vector<Cand> cands;
+  cands.push_back({LBM_VARIANT_DIRECT, StagedPlan{}});
+  for (int variant : {LBM_VARIANT_STAGED, LBM_VARIANT_STAGED_X2})
+    for (int groups = 1; groups <= 8; ++groups)
+      for (int S = 2; S <= 8; ++S)
+        for (int per_sm : {1, 2, 3, 4}) {
+          StagedPlan p;
+          if (!plan_staged(ctx, variant, S, per_sm, &p, groups)) continue;
+          bool dup = false;
+          for (const Cand& c : cands)
+            dup |= c.variant == variant && c.p.S == p.S && c.p.ctas_per_sm == p.ctas_per_sm &&
+                   c.p.groups == p.groups;
+          if (!dup) cands.push_back({variant, p});
+        }
+  cudaGetLastError();
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  const int keep_variant = ctx->variant;
+  const StagedPlan keep_plan = ctx->staged;
+  double best = 1e30;
+  size_t best_i = 0;
+  const bool prof = ctx->prof_on;
+  ctx->prof_on = false;
+  for (size_t i = 0; i < cands.size(); ++i) {
+    ctx->variant = cands[i].variant;
+    ctx->staged = cands[i].p;
+    auto run = [&]() {
+      if (ctx->f32) launch_stream_collide<float>(ctx, fbuf<float>(ctx, ctx->cur), fbuf<float>(ctx, 1 - ctx->cur));
+      else launch_stream_collide<double>(ctx, fbuf<double>(ctx, ctx->cur), fbuf<double>(ctx, 1 - ctx->cur));
+    };
+    run();
+    cudaEventRecord(e0, ctx->stream);
+    for (int k = 0; k < reps; ++k) run();
+    cudaEventRecord(e1, ctx->stream);
+    if (cudaEventSynchronize(e1) != cudaSuccess) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms / reps < best) { best = ms / reps; best_i = i; }
+  }
+  ctx->prof_on = prof;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ctx->variant = keep_variant;
+  ctx->staged = keep_plan;
+  CK(cudaGetLastError());
+  if (int rc = check_status(ctx)) return rc;
+  ctx->variant = cands[best_i].variant;
+  ctx->staged = cands[best_i].p;
+  if (best_ms) *best_ms = best;
   return LBM_OK;
 }
 

@@ -16,13 +16,12 @@
 // plus a 4-byte flag.  In FP64 the MRT arithmetic, not HBM, bounds it on
 // GB300, whose FP64 rate is a small fraction of its FP32 rate.
 #include "lbm_internal.cuh"
+#include "lbm_collide.cuh"
 
 namespace lbm {
 
 namespace {
 
-template <typename T>
-struct Vec2 { T x, y; };
 
 // MRT collision of one fluid node, B/collision.f90:36-203.  f holds the
 // node's 19 populations on entry and the post-collision populations on
@@ -189,237 +188,19 @@ __device__ __forceinline__ void body_force(const ForceView<T>& fv, const Geometr
                                            int y, int z, T& fx, T& fy, T& fz) {
   if (fv.mode == FM_CONST) { fx = fv.cfx; fy = fv.cfy; fz = fv.cfz; return; }
   if (fv.mode != FM_TABLE) { fx = T(0); fy = T(0); fz = T(0); return; }
-  const Vec2<T>* tab = reinterpret_cast<const Vec2<T>*>(fv.rowtab);
   const T c1 = fv.xtw[4 * x], s1 = fv.xtw[4 * x + 1], c2 = fv.xtw[4 * x + 2], s2 = fv.xtw[4 * x + 3];
   T out[3];
-  const long long plane = (long long)g.nz * g.ny;
-  const long long row = (long long)z * g.ny + y;
+  const T* k = fv.rowtab + ((long long)z * g.ny + y) * kRowCoef;
 #pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    Vec2<T> B0 = tab[(c * 3 + 0) * plane + row];
-    Vec2<T> B1 = tab[(c * 3 + 1) * plane + row];
-    Vec2<T> B2 = tab[(c * 3 + 2) * plane + row];
-    out[c] = B0.x + T(2.0) * (B1.x * c1 - B1.y * s1) + T(2.0) * (B2.x * c2 - B2.y * s2);
-  }
+  for (int c = 0; c < 3; ++c)
+    out[c] = k[5 * c] + k[5 * c + 1] * c1 + k[5 * c + 2] * s1 + k[5 * c + 3] * c2 + k[5 * c + 4] * s2;
   fx = out[0]; fy = out[1]; fz = out[2];
 }
 
 __device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
-// Relaxation rates of the 15 non-conserved moments, in the kernel's own
-// precision: s[k] (moment k = 1..15 in the order of collision.f90:101-118)
-// and h[k] = 1 - s[k]/2, the weight of the forcing term's moments.
-template <typename T>
-struct RatesT {
-  T s[16], h[16];
-  T omegepsl, omegepslj, omegxx;
-};
 
-template <typename T>
-RatesT<T> rates_t(const Rates& r) {
-  RatesT<T> o;
-  const double sk[16] = {0.0, r.s1, r.s2, r.s4, r.s4, r.s4, r.s9, r.s10, r.s9, r.s10,
-                         r.s13, r.s13, r.s13, r.s16, r.s16, r.s16};
-  for (int k = 0; k < 16; ++k) {
-    o.s[k] = T(sk[k]);
-    o.h[k] = T(1.0 - 0.5 * sk[k]);
-  }
-  o.omegepsl = T(r.omegepsl);
-  o.omegepslj = T(r.omegepslj);
-  o.omegxx = T(r.omegxx);
-  return o;
-}
 
-// MRT collision with Guo forcing in moment space.  Algebraically the
-// collision_MRT of collision.f90:36-203: there f9 = f + Fbar/2 is relaxed in
-// moment space, transformed back with rho and u from macrovar, and Fbar/2 is
-// added again.  The moments of Fbar have the closed form
-//   m1 = 38 u.F, m2 = -11 u.F, m3..5 = -2/3 F, m6 = 2(2 Fx ux - Fy uy - Fz uz),
-//   m7 = -m6/2, m8 = 2(Fy uy - Fz uz), m9 = -m8/2, m10 = Fx uy + Fy ux,
-//   m11 = Fy uz + Fz uy, m12 = Fx uz + Fz ux, m13..15 = 0,
-// with mass 0 and momentum F, so the whole step is one forward transform,
-// m'_k = m_k - s_k (m_k - meq_k) + (1 - s_k/2) mF_k, and one inverse
-// transform with momentum u + F/2.  This removes the per-direction forcing
-// arithmetic, which matters most in FP64 where the GPU's FP64 issue rate
-// bounds the kernel.  Results agree with the literal form to rounding.
-//   f       in: post-streaming populations; out: post-collision populations
-//   fp*     body force of the previous step (macrovar's u = j + Fp/2)
-//   f*      body force of this step
-template <typename T>
-__device__ __forceinline__ void collide_fast(T (&f)[NPOP], T fpx, T fpy, T fpz, T fx, T fy,
-                                             T fz, const RatesT<T>& r) {
-  const T a1 = f[1] + f[2], d1 = f[1] - f[2];
-  const T a3 = f[3] + f[4], d3 = f[3] - f[4];
-  const T a5 = f[5] + f[6], d5 = f[5] - f[6];
-  const T s78 = f[7] + f[8], d78 = f[7] - f[8], s910 = f[9] + f[10], d910 = f[9] - f[10];
-  const T s1112 = f[11] + f[12], d1112 = f[11] - f[12];
-  const T s1314 = f[13] + f[14], d1314 = f[13] - f[14];
-  const T s1516 = f[15] + f[16], d1516 = f[15] - f[16];
-  const T s1718 = f[17] + f[18], d1718 = f[17] - f[18];
-  const T sum1 = a1 + a3 + a5;
-  const T Sxy = s78 + s910, Sxz = s1112 + s1314, Syz = s1516 + s1718;
-  const T sum2 = Sxy + Sxz + Syz;
-  const T D1 = d78 + d910, D2 = d1112 + d1314;
-  const T sum3 = D1 + D2;
-  const T A = s78 - s910, Bv = d1516 + d1718;
-  const T sum4 = A + Bv;
-  const T C = s1112 - s1314, Dd = s1516 - s1718;
-  const T sum5 = C + Dd;
-  const T rho = f[0] + sum1 + sum2;
-  // macrovar: u = sum c f + F_prev / 2
-  const T ux = d1 + sum3 + T(0.5) * fpx;
-  const T uy = d3 + sum4 + T(0.5) * fpy;
-  const T uz = d5 + sum5 + T(0.5) * fpz;
-
-  // moments of f (collision.f90:101-118)
-  const T sum7 = a3 + a5, sum8 = Sxy + Sxz, sum10 = a3 - a5, sum11 = Sxy - Sxz;
-  const T ev1 = T(-30.0) * f[0] + T(-11.0) * sum1 + T(8.0) * sum2;
-  const T ev2 = T(12.0) * f[0] + T(-4.0) * sum1 + sum2;
-  const T ev3 = T(-4.0) * d1 + sum3;
-  const T ev4 = T(-4.0) * d3 + sum4;
-  const T ev5 = T(-4.0) * d5 + sum5;
-  const T ev6 = T(2.0) * (a1 - Syz) - sum7 + sum8;
-  const T ev7 = T(-4.0) * a1 + T(2.0) * (sum7 - Syz) + sum8;
-  const T ev8 = sum10 + sum11;
-  const T ev9 = T(-2.0) * sum10 + sum11;
-  const T ev10 = d78 - d910;
-  const T ev11 = d1516 - d1718;
-  const T ev12 = d1112 - d1314;
-  const T ev13 = D1 - D2;
-  const T ev14 = Bv - A;
-  const T ev15 = C - Dd;
-
-  // equilibrium moments (collision.f90:66-81)
-  const T uxs = ux * ux, uys = uy * uy, uzs = uz * uz;
-  const T t1 = uxs + uys + uzs;
-  const T eq1 = T(-11.0) * rho + T(19.0) * t1;
-  const T eq2 = r.omegepsl * rho + r.omegepslj * t1;
-  const T eq6 = T(2.0) * uxs - uys - uzs;
-  const T eq8 = uys - uzs;
-
-  // forcing moments
-  const T fa = fx * ux, fb = fy * uy, fc = fz * uz;
-  const T G3 = fa + fb + fc;
-  const T e6 = T(2.0) * fa - fb - fc;
-  const T e8 = fb - fc;
-
-  // post-collision moments
-  const T m1 = ev1 - r.s[1] * (ev1 - eq1) + r.h[1] * (T(38.0) * G3);
-  const T m2 = ev2 - r.s[2] * (ev2 - eq2) + r.h[2] * (T(-11.0) * G3);
-  const T m3 = ev3 - r.s[3] * (ev3 - T(-2.0 / 3.0) * ux) + r.h[3] * (T(-2.0 / 3.0) * fx);
-  const T m4 = ev4 - r.s[4] * (ev4 - T(-2.0 / 3.0) * uy) + r.h[4] * (T(-2.0 / 3.0) * fy);
-  const T m5 = ev5 - r.s[5] * (ev5 - T(-2.0 / 3.0) * uz) + r.h[5] * (T(-2.0 / 3.0) * fz);
-  const T m6 = ev6 - r.s[6] * (ev6 - eq6) + r.h[6] * (T(2.0) * e6);
-  const T m7 = ev7 - r.s[7] * (ev7 - r.omegxx * eq6) - r.h[7] * e6;
-  const T m8 = ev8 - r.s[8] * (ev8 - eq8) + r.h[8] * (T(2.0) * e8);
-  const T m9 = ev9 - r.s[9] * (ev9 - r.omegxx * eq8) - r.h[9] * e8;
-  const T m10 = ev10 - r.s[10] * (ev10 - ux * uy) + r.h[10] * (fx * uy + fy * ux);
-  const T m11 = ev11 - r.s[11] * (ev11 - uy * uz) + r.h[11] * (fy * uz + fz * uy);
-  const T m12 = ev12 - r.s[12] * (ev12 - ux * uz) + r.h[12] * (fx * uz + fz * ux);
-  const T m13 = ev13 - r.s[13] * ev13;
-  const T m14 = ev14 - r.s[14] * ev14;
-  const T m15 = ev15 - r.s[15] * ev15;
-
-  // inverse transform (collision.f90:137-200) with momentum u + F/2
-  const T tl1 = T(1.0 / 19.0) * rho;
-  const T tl2 = T(-11.0 / 2394.0) * m1;
-  const T tl3 = T(8.0 / 2394.0) * m1;
-  const T tl4 = T(-4.0 / 252.0) * m2;
-  const T tl5 = T(1.0 / 252.0) * m2;
-  const T tl6 = T(0.1) * (ux + T(0.5) * fx);
-  const T tl7 = T(1.0 / 40.0) * m3;
-  const T tl8 = T(0.1) * (uy + T(0.5) * fy);
-  const T tl9 = T(1.0 / 40.0) * m4;
-  const T tl10 = T(0.1) * (uz + T(0.5) * fz);
-  const T tl11 = T(1.0 / 40.0) * m5;
-  const T tl12 = T(1.0 / 36.0) * m6;
-  const T tl13 = T(1.0 / 72.0) * m7;
-  const T tl14 = T(1.0 / 12.0) * m8;
-  const T tl15 = T(1.0 / 24.0) * m9;
-  const T tl16 = T(0.25) * m10;
-  const T tl17 = T(0.25) * m11;
-  const T tl18 = T(0.25) * m12;
-  const T tl19 = T(0.125) * m13;
-  const T tl20 = T(0.125) * m14;
-  const T tl21 = T(0.125) * m15;
-
-  f[0] = tl1 + T(-30.0 / 2394.0) * m1 + T(12.0 / 252.0) * m2;
-  const T suma = tl1 + tl2 + tl4;
-  const T sumb = tl1 + tl3 + tl5;
-  const T sumc = tl6 - T(4.0) * tl7;
-  const T sumd = T(2.0) * tl12 - T(4.0) * tl13;
-  const T sume = tl8 - T(4.0) * tl9;
-  const T sumf = -tl12 + T(2.0) * tl13 + tl14 - T(2.0) * tl15;
-  const T sumg = tl10 - T(4.0) * tl11;
-  const T sumh = -tl12 + T(2.0) * tl13 - tl14 + T(2.0) * tl15;
-  const T sumi = tl12 + tl13 + tl14 + tl15;
-  const T sumk = tl12 + tl13 - tl14 - tl15;
-  const T sump = T(-2.0) * (tl12 + tl13);
-  const T sum67 = tl6 + tl7, sum89 = tl8 + tl9, sum1011 = tl10 + tl11;
-
-  const T ad = suma + sumd, af = suma + sumf, ah = suma + sumh;
-  f[1] = ad + sumc;
-  f[2] = ad - sumc;
-  f[3] = af + sume;
-  f[4] = af - sume;
-  f[5] = ah + sumg;
-  f[6] = ah - sumg;
-  {  // x-y diagonals 7..10
-    const T base = sumb + sumi, p = sum67 + sum89, m = sum67 - sum89;
-    const T r1 = tl19 - tl20, r2 = tl19 + tl20;
-    f[7] = base + p + tl16 + r1;
-    f[8] = base - m - tl16 - r2;
-    f[9] = base + m - tl16 + r2;
-    f[10] = base - p + tl16 - r1;
-  }
-  {  // x-z diagonals 11..14
-    const T base = sumb + sumk, p = sum67 + sum1011, m = sum67 - sum1011;
-    const T r1 = tl21 - tl19, r2 = tl19 + tl21;
-    f[11] = base + p + tl18 + r1;
-    f[12] = base - m - tl18 + r2;
-    f[13] = base + m - tl18 - r2;
-    f[14] = base - p + tl18 - r1;
-  }
-  {  // y-z diagonals 15..18
-    const T base = sumb + sump, p = sum89 + sum1011, m = sum89 - sum1011;
-    const T r1 = tl20 - tl21, r2 = tl20 + tl21;
-    f[15] = base + p + tl17 + r1;
-    f[16] = base - m - tl17 - r2;
-    f[17] = base + m - tl17 + r2;
-    f[18] = base - p + tl17 - r1;
-  }
-}
-
-// Body force of two fields (previous and current step) at one node, sharing
-// the per-x twiddles; see ForceView.
-template <typename T>
-__device__ __forceinline__ void body_force2(const ForceView<T>& fa, const ForceView<T>& fb,
-                                            int x, int row, int plane, T (&oa)[3], T (&ob)[3]) {
-  T c1 = T(0), s1 = T(0), c2 = T(0), s2 = T(0);
-  if (fa.mode == FM_TABLE || fb.mode == FM_TABLE) {
-    c1 = fa.xtw[4 * x]; s1 = fa.xtw[4 * x + 1]; c2 = fa.xtw[4 * x + 2]; s2 = fa.xtw[4 * x + 3];
-  }
-  const ForceView<T>* fv[2] = {&fa, &fb};
-  T* out[2] = {oa, ob};
-#pragma unroll
-  for (int w = 0; w < 2; ++w) {
-    const ForceView<T>& v = *fv[w];
-    if (v.mode == FM_TABLE) {
-      const Vec2<T>* tab = reinterpret_cast<const Vec2<T>*>(v.rowtab);
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        Vec2<T> B0 = tab[(c * 3 + 0) * plane + row];
-        Vec2<T> B1 = tab[(c * 3 + 1) * plane + row];
-        Vec2<T> B2 = tab[(c * 3 + 2) * plane + row];
-        out[w][c] = B0.x + T(2.0) * (B1.x * c1 - B1.y * s1) + T(2.0) * (B2.x * c2 - B2.y * s2);
-      }
-    } else if (v.mode == FM_CONST) {
-      out[w][0] = v.cfx; out[w][1] = v.cfy; out[w][2] = v.cfz;
-    } else {
-      out[w][0] = T(0); out[w][1] = T(0); out[w][2] = T(0);
-    }
-  }
-}
 
 // --------------------------------------------------------------------------
 // fused stream + collide (push).  One thread per node, a block covers part
@@ -440,7 +221,7 @@ __global__ void __launch_bounds__(128) k_fused(Geometry g, RatesT<T> r, const T*
   for (int q = 0; q < NPOP; ++q) f[q] = fin[(size_t)q * N + n];
   if (isnodes[n] < 0) {
     T fp[3], fc[3];
-    body_force2(fprev, fnew, x, z * g.ny + y, g.nz * g.ny, fp, fc);
+    body_force2(fprev, fnew, x, z * g.ny + y, fp, fc);
     collide_fast(f, fp[0], fp[1], fp[2], fc[0], fc[1], fc[2], r);
   }
   // push: neighbour offsets with periodic wrap
@@ -675,6 +456,9 @@ __global__ void k_force_ztab(Geometry g, const ForcingDev* st, const double* __r
   ztab[2 * t + 1] = si;
 }
 
+// Row coefficients of the force series (kRowCoef layout) from the (kx, z)
+// table: one thread per (row, component, kx).  The kx = 1, 2 terms of the
+// real inverse transform enter twice (kx and -kx), hence the factor 2.
 template <typename T>
 __global__ void k_force_rowtab(Geometry g, const double* __restrict__ ztab,
                                const double* __restrict__ ytw, T* __restrict__ rowtab) {
@@ -694,8 +478,15 @@ __global__ void k_force_rowtab(Geometry g, const double* __restrict__ ztab,
     sr += ar * cs - aim * sn;
     si += ar * sn + aim * cs;
   }
-  rowtab[2 * t] = sr;
-  rowtab[2 * t + 1] = si;
+  const int c = ckx / 3, kx = ckx % 3;
+  T* k = rowtab + ((long long)z * g.ny + y) * kRowCoef + 5 * c;
+  if (kx == 0) {
+    k[0] = sr;
+    if (c == 0) rowtab[((long long)z * g.ny + y) * kRowCoef + 15] = T(0);
+  } else {
+    k[2 * kx - 1] = T(2.0) * sr;
+    k[2 * kx] = T(-2.0) * si;
+  }
 }
 
 inline dim3 row_grid(const Geometry& g, int bx) { return dim3((g.nx + bx - 1) / bx, g.ny, g.nz); }

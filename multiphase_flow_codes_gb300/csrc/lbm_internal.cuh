@@ -63,10 +63,17 @@ enum ForceMode { FM_NONE = 0, FM_TABLE = 1, FM_CONST = 2 };
 //   F_c = Re B0 + 2 (Re B1 cos(2 pi x/nx) - Im B1 sin(..))
 //             + 2 (Re B2 cos(4 pi x/nx) - Im B2 sin(..)),
 // B_kx = rowtab[((c*3 + kx)*nz + z)*ny + y] (complex).
+// The stochastic body force along one x-row (y, z) is a short Fourier series
+// in x (kx = 0, 1, 2 are the only x wavenumbers of the forcing):
+//   F_c(x) = k0 + k1 cos(2 pi x/nx) + k2 sin(2 pi x/nx) + k3 cos(4 pi x/nx) + k4 sin(4 pi x/nx)
+// The table holds, per row, (k0..k4) of c = x, y, z at [5c .. 5c+4] and a
+// zero in slot 15: 16 values, a multiple of 16 bytes in either precision.
+constexpr int kRowCoef = 16;
+
 template <typename T>
 struct ForceView {
   int mode;                 // ForceMode
-  const T* rowtab;          // interleaved (re, im), 3*3*nz*ny complex
+  const T* rowtab;          // [z*ny + y][kRowCoef] x-series coefficients, see below
   const T* xtw;             // per x: cos1, sin1, cos2, sin2
   T cfx, cfy, cfz;          // constant force (FM_CONST)
 };
@@ -113,6 +120,28 @@ template <typename T>
 void launch_fused_step(const Geometry& g, const Rates& r, const T* fin, T* fout,
                        const int32_t* isnodes, const ForceView<T>& fprev,
                        const ForceView<T>& fnew, cudaStream_t s);
+// the same step with its rows staged through shared memory by bulk copies
+// (lbm_staged.cu); periodic boxes with nx a multiple of 4
+struct StagedPlan {
+  int S = 0;            // input stages (rows in flight + 1)
+  bool packed = false;  // FP32 pair kernel on f32x2 arithmetic
+  int groups = 1;       // packed: consumer warp groups (rows in the collision at once)
+  int ctas_per_sm = 0;
+  int grid = 0, threads = 0;
+  size_t smem = 0;
+};
+template <typename T>
+bool staged_eligible(const Geometry& g, int S, bool packed);
+template <typename T>
+int staged_max_stages(const Geometry& g);
+template <typename T>
+bool plan_fused_staged(const Geometry& g, int S, int ctas_per_sm, bool packed, int groups,
+                       StagedPlan* plan);
+template <typename T>
+void launch_fused_staged(const Geometry& g, const Rates& r, const T* fin, T* fout,
+                         const int32_t* isnodes, const ForceView<T>& fprev,
+                         const ForceView<T>& fnew, const StagedPlan& p, DevStatus* st,
+                         cudaStream_t s);
 template <typename T>
 void launch_macrovar(const Geometry& g, const T* f, const int32_t* isnodes,
                      const ForceView<T>& fv, const ParticleView& pv, T* rho, T* ux,

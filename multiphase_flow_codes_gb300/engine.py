@@ -234,6 +234,26 @@ class LBMBox:
         """The time step of main.f90:172-188, ``nsteps`` times (fused path)."""
         self._ck(self._L.lbm_step(self._h, int(nsteps)), "step")
 
+    # ---- kernel selection -------------------------------------------------
+    def set_variant(self, variant: int, stages: int = 0, groups: int = 0, ctas_per_sm: int = 0):
+        """Pick the stream+collide kernel (capi.LBM_VARIANT_*) and its schedule."""
+        self._ck(self._L.lbm_set_variant(self._h, int(variant), int(stages), int(groups),
+                                         int(ctas_per_sm)), "set_variant")
+
+    def variant(self) -> tuple:
+        """(variant, stages, groups, ctas_per_sm) of the stream+collide kernel in use."""
+        v, s, g, c = C.c_int(0), C.c_int(0), C.c_int(0), C.c_int(0)
+        self._ck(self._L.lbm_get_variant(self._h, C.byref(v), C.byref(s), C.byref(g), C.byref(c)),
+                 "get_variant")
+        return v.value, s.value, g.value, c.value
+
+    def autotune(self, reps: int = 5) -> float:
+        """Time every applicable stream+collide variant on the current state
+        (without advancing it), keep the fastest; returns its ms per launch."""
+        ms = C.c_double(0.0)
+        self._ck(self._L.lbm_autotune(self._h, int(reps), C.byref(ms)), "autotune")
+        return ms.value
+
     def step_unfused(self, nsteps: int = 1):
         """The same sequence, one reference subroutine per call."""
         for _ in range(nsteps):

@@ -65,3 +65,14 @@ def test_footprint_and_bad_arguments(engine_lib):
     assert engine_lib.lbm_create(C.byref(bad), C.byref(h)) == capi.LBM_ERR_ARG
     with pytest.raises(capi.LBMError):
         capi.config_init(capi.LBM_PRESET_BOX, 2, 2, 2, 0, 1.0, 1.0)
+
+
+@pytest.mark.gpu
+def test_fma_throughput_probe(engine_lib, require_gpu):
+    """The FP64 and FP32 FMA rates the roofline of the fused kernel is quoted against."""
+    f64, f32 = C.c_double(0.0), C.c_double(0.0)
+    assert engine_lib.lbm_fma_throughput(capi.LBM_PREC_F64, C.byref(f64)) == capi.LBM_OK
+    assert engine_lib.lbm_fma_throughput(capi.LBM_PREC_F32, C.byref(f32)) == capi.LBM_OK
+    assert 0.1 < f64.value < 200.0
+    assert f32.value > f64.value
+    assert engine_lib.lbm_fma_throughput(capi.LBM_PREC_F64, None) == capi.LBM_ERR_ARG
