@@ -151,7 +151,7 @@ def initial_f(u):
     return f
 
 
-def run_device(wl, u, y, steps, warmup, device, want_f=False):
+def run_device(wl, u, y, steps, warmup, device, want_f=False, variant=None):
     """Device-resident timing of `steps` C-ABI step calls."""
     import torch
     from multiphase_flow_codes_gb300.engine import LBMBox
@@ -162,7 +162,10 @@ def run_device(wl, u, y, steps, warmup, device, want_f=False):
     box.macrovar()
     if wl.npart:
         box.release_particles(y)
-    box.autotune(reps=3)          # pick the stream+collide variant on this state
+    if variant is None:
+        box.autotune(reps=3)      # pick the stream+collide variant on this state
+    else:
+        box.set_variant(*variant)
     variant = box.variant()
     for _ in range(warmup):
         box.step(1)
@@ -258,7 +261,7 @@ def cpu_oracle(wl, u, y, steps, threads=None):
 
 
 def workload(name: str):
-    """config0/1/2, or box{n}_p{npart}_{f64|f32} (radius 4, density ratio 2.5)."""
+    """config0/1/2, or box{n}[x{ny}x{nz}]_p{npart}_{f64|f32} (radius 4, density ratio 2.5)."""
     from multiphase_flow_codes_gb300 import _capi as capi
     from multiphase_flow_codes_gb300 import config
     table = {"config0": config.config0, "config1": config.config1, "config2": config.config2,
@@ -267,12 +270,15 @@ def workload(name: str):
     if name in table:
         return table[name]()
     import re
-    m = re.fullmatch(r"box(\d+)_p(\d+)_(f64|f32)", name)
+    m = re.fullmatch(r"box(\d+)(?:x(\d+)x(\d+))?_p(\d+)_(f64|f32)", name)
     if not m:
         raise SystemExit(f"unknown workload {name}")
-    n, npart = int(m.group(1)), int(m.group(2))
-    prec = capi.LBM_PREC_F64 if m.group(3) == "f64" else capi.LBM_PREC_F32
-    return config.box(n, npart, 4.0, 2.5, 8.0 if n >= 256 else 4.0, 0.04, 2000, precision=prec, name=name)
+    n, npart = int(m.group(1)), int(m.group(4))
+    ny = int(m.group(2)) if m.group(2) else n
+    nz = int(m.group(3)) if m.group(3) else n
+    prec = capi.LBM_PREC_F64 if m.group(5) == "f64" else capi.LBM_PREC_F32
+    return config.box(n, npart, 4.0, 2.5, 8.0 if n >= 256 else 4.0, 0.04, 2000, precision=prec,
+                      name=name, ny=ny, nz=nz)
 
 
 def dist_setup(args):
@@ -299,6 +305,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--variant", default=None,
+                    help="stream+collide kernel as 'variant,stages,groups,ctas_per_sm' "
+                         "(default: autotuned on the workload)")
     ap.add_argument("--ref-max-steps", type=int, default=6,
                     help="--impl reference: at most this many full CPU steps are timed")
     args = ap.parse_args()
@@ -351,8 +360,9 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     sampler.start()
+    fixed = tuple(int(v) for v in args.variant.split(",")) if args.variant else None
     ms, launches, phases, f64, p64, variant = run_device(wl, u, y, args.steps, args.warmup, local,
-                                               want_f=not args.no_fp32)
+                                                         want_f=not args.no_fp32, variant=fixed)
     clocks = sampler.stop()
     t_ms = ms
     if dist:

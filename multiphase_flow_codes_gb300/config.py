@@ -30,8 +30,9 @@ class Workload:
 
 
 def box(n: int, npart: int, rad: float, rhopart: float, k0: float, urms: float, steps: int,
-        precision: int = capi.LBM_PREC_F64, name: str = "") -> Workload:
-    cfg = capi.config_init(capi.LBM_PRESET_BOX, n, n, n, npart, rad, rhopart)
+        precision: int = capi.LBM_PREC_F64, name: str = "", ny: int | None = None,
+        nz: int | None = None) -> Workload:
+    cfg = capi.config_init(capi.LBM_PRESET_BOX, n, ny or n, nz or n, npart, rad, rhopart)
     cfg.visc = 0.0036  # tau = 3 visc + 0.5 = 0.5108
     cfg.precision = precision
     return Workload(name or f"box{n}", cfg, npart, k0, urms, steps)

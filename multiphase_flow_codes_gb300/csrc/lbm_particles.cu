@@ -295,45 +295,53 @@ __global__ void __launch_bounds__(PB) k_links(Geometry g, ParticleView pv, int32
   }
 
   // ---- phase 1: nodes of every processed row within reach of the sphere;
-  // solid nodes are flagged, fluid ones kept (in loop order) for phase 2
-  int tnodes = nrows * tx;
-  for (int c0 = 0; c0 < tnodes; c0 += PB) {
-    int t = c0 + tid;
-    bool keep = false;
-    int r = 0, ci = 0;
-    if (t < tnodes) {
-      r = t / tx;
-      ci = t - r * tx;
-      const int i = cx.at(ci);
-      const float xxf = ((float)i - 0.5f) - xvalf[min(r, 2)][ci];
-      const float yyf = row_yy[r], zzf = row_zz[r];
-      const float rr0f = xxf * xxf + yyf * yyf + zzf * zzf;
-      if (rr0f <= reachf) {
-        const int j = row_j[r], k = row_k[r];
-        bool solid;
-        const float d0 = rr0f - rad2f;
-        if (d0 < -kDecide) solid = true;
-        else if (d0 > kDecide) solid = false;
-        else {
-          const double xc = xval[min(r, 2)][ci], yc = row_y[r], zc = row_z[r];
-          double xx0 = ((double)i - 0.5) - xc;
-          double yy0 = ((double)j - 0.5 + 0.0) - yc;
-          double zz0 = ((double)k - 0.5 + 0.0) - zc;
-          double rr0 = xx0 * xx0 + yy0 * yy0 + zz0 * zz0;
-          solid = (rr0 - rad2) <= 0.0;
-        }
-        if (solid) {
+  // solid nodes are flagged, fluid ones kept (in row, then x order) for
+  // phase 2.  One thread per row; a block scan of the per-row counts places
+  // each row's nodes.
+  // class of node (row r, x candidate ci): 0 out of reach, 1 solid, 2 fluid
+  auto node_class = [&](int r, int ci) -> int {
+    const int i = cx.at(ci);
+    const float xxf = ((float)i - 0.5f) - xvalf[min(r, 2)][ci];
+    const float yyf = row_yy[r], zzf = row_zz[r];
+    const float rr0f = xxf * xxf + yyf * yyf + zzf * zzf;
+    if (!(rr0f <= reachf)) return 0;
+    const float d0 = rr0f - rad2f;
+    if (d0 < -kDecide) return 1;
+    if (d0 > kDecide) return 2;
+    const double xc = xval[min(r, 2)][ci], yc = row_y[r], zc = row_z[r];
+    const int j = row_j[r], k = row_k[r];
+    double xx0 = ((double)i - 0.5) - xc;
+    double yy0 = ((double)j - 0.5 + 0.0) - yc;
+    double zz0 = ((double)k - 0.5 + 0.0) - zc;
+    double rr0 = xx0 * xx0 + yy0 * yy0 + zz0 * zz0;
+    return (rr0 - rad2) <= 0.0 ? 1 : 2;
+  };
+  for (int r0 = 0; r0 < nrows; r0 += PB) {
+    const int r = r0 + tid;
+    int cnt = 0;
+    if (r < nrows) {
+      const int j = row_j[r], k = row_k[r];
+      for (int ci = 0; ci < tx; ++ci) {
+        const int cl = node_class(r, ci);
+        if (cl == 1) {
+          const int i = cx.at(ci);
           long long node = (long long)(i - 1) + (long long)g.nx * ((j - 1) + (long long)g.ny * (k - 1));
           atomicMax(&isnodes[node], p);
-        } else {
-          keep = true;
+        } else if (cl == 2) {
+          ++cnt;
         }
       }
     }
     int pos, tot;
-    Scan(scan_tmp).ExclusiveSum(keep ? 1 : 0, pos, tot);
-    __syncthreads();
-    if (keep && nnear + pos < MAXNEAR) near_rc[nnear + pos] = (r << 8) | ci;
+    Scan(scan_tmp).ExclusiveSum(cnt, pos, tot);
+    if (cnt) {
+      int w = nnear + pos;
+      for (int ci = 0; ci < tx; ++ci)
+        if (node_class(r, ci) == 2) {
+          if (w < MAXNEAR) near_rc[w] = (r << 8) | ci;
+          ++w;
+        }
+    }
     __syncthreads();
     if (tid == 0) {
       if (nnear + tot > MAXNEAR) fixed_ok = 0;
@@ -342,20 +350,28 @@ __global__ void __launch_bounds__(PB) k_links(Geometry g, ParticleView pv, int32
     __syncthreads();
   }
 
-  // ---- phase 2: one thread per (fluid near node, direction); links are
-  // written in (node, ipop) order
-  const int npairs = nnear * 18;
+  // ---- phase 2: one thread per fluid near node tests its 18 directions.
+  // Within each chunk of PB near nodes the links are written direction by
+  // direction (ipop, then node order), so that the bounce-back kernels that
+  // walk the list read and write neighbouring x nodes of one population
+  // array together.  Offsets come from warp ballots per direction and one
+  // warp-wide scan of the (direction, warp) counts.
+  constexpr int NW = PB / 32;
+  constexpr int NCNT = 18 * NW;
+  constexpr int PER_LANE = (NCNT + 31) / 32;
+  __shared__ int woff[NCNT];
+  __shared__ int chunk_links;
+  const int warp = tid >> 5, lane = tid & 31;
+  const unsigned lane_lt = (1u << lane) - 1u;
   int32_t* code = ls.code + (long long)p * ls.cap;
   double* alph = ls.alpha + (long long)p * ls.cap;
   float* alph32 = reinterpret_cast<float*>(alph);
-  for (int c0 = 0; c0 < npairs; c0 += PB) {
-    const int t = c0 + tid;
-    bool link = false;
-    int r = 0, ci = 0, ipop = 0, i = 0;
+  for (int n0 = 0; n0 < nnear; n0 += PB) {
+    const int idx = n0 + tid;
+    unsigned mask = 0;
+    int r = 0, ci = 0, i = 0;
     float xxf = 0.f, yyf = 0.f, zzf = 0.f;
-    if (t < npairs) {
-      const int idx = t / 18;
-      ipop = t - idx * 18 + 1;
+    if (idx < nnear) {
       const int rc = near_rc[idx];
       r = rc >> 8;
       ci = rc & 255;
@@ -363,58 +379,96 @@ __global__ void __launch_bounds__(PB) k_links(Geometry g, ParticleView pv, int32
       xxf = ((float)i - 0.5f) - xvalf[min(r, 2)][ci];
       yyf = row_yy[r];
       zzf = row_zz[r];
-      const float ax = xxf + (float)cix(ipop), ay = yyf + (float)ciy(ipop), az = zzf + (float)ciz(ipop);
-      const float d1 = ax * ax + ay * ay + az * az - rad2f;
-      if (d1 < -kDecide) link = true;
-      else if (d1 > kDecide) link = false;
-      else {
-        const int j = row_j[r], k = row_k[r];
-        const double xc = xval[min(r, 2)][ci], yc = row_y[r], zc = row_z[r];
-        double xx1 = (double)(i + cix(ipop)) - 0.5 - xc;
-        double yy1 = (double)(j + ciy(ipop)) - 0.5 - yc + 0.0;
-        double zz1 = (double)(k + ciz(ipop)) - 0.5 - zc + 0.0;
-        double rr1 = xx1 * xx1 + yy1 * yy1 + zz1 * zz1;
-        link = (rr1 - rad2) <= 0.0;
+#pragma unroll
+      for (int ipop = 1; ipop < NPOP; ++ipop) {
+        const float ax = xxf + (float)cix(ipop), ay = yyf + (float)ciy(ipop), az = zzf + (float)ciz(ipop);
+        const float d1 = ax * ax + ay * ay + az * az - rad2f;
+        bool link;
+        if (d1 < -kDecide) link = true;
+        else if (d1 > kDecide) link = false;
+        else {
+          const int j = row_j[r], k = row_k[r];
+          const double xc = xval[min(r, 2)][ci], yc = row_y[r], zc = row_z[r];
+          double xx1 = (double)(i + cix(ipop)) - 0.5 - xc;
+          double yy1 = (double)(j + ciy(ipop)) - 0.5 - yc + 0.0;
+          double zz1 = (double)(k + ciz(ipop)) - 0.5 - zc + 0.0;
+          double rr1 = xx1 * xx1 + yy1 * yy1 + zz1 * zz1;
+          link = (rr1 - rad2) <= 0.0;
+        }
+        if (link) mask |= 1u << ipop;
       }
     }
-    int pos, tot;
-    Scan(scan_tmp).ExclusiveSum(link ? 1 : 0, pos, tot);
+#pragma unroll
+    for (int q = 0; q < 18; ++q) {
+      const unsigned bal = __ballot_sync(0xffffffffu, (mask >> (q + 1)) & 1u);
+      if (lane == 0) woff[q * NW + warp] = __popc(bal);
+    }
     __syncthreads();
-    if (link) {
-      const int w = base + pos;
-      const int j = row_j[r], k = row_k[r];
+    if (warp == 0) {
+      // exclusive scan of the NCNT counts, PER_LANE consecutive entries a lane
+      int v[PER_LANE], sum = 0;
+#pragma unroll
+      for (int e = 0; e < PER_LANE; ++e) {
+        const int t = lane * PER_LANE + e;
+        v[e] = t < NCNT ? woff[t] : 0;
+        sum += v[e];
+      }
+      int incl = sum;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int o = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += o;
+      }
+      int run = incl - sum;
+#pragma unroll
+      for (int e = 0; e < PER_LANE; ++e) {
+        const int t = lane * PER_LANE + e;
+        if (t < NCNT) woff[t] = run;
+        run += v[e];
+      }
+      if (lane == 31) chunk_links = incl;
+    }
+    __syncthreads();
+    const int j = row_j[r], k = row_k[r];
+    const long long node =
+        (long long)(i - 1) + (long long)g.nx * ((j - 1) + (long long)g.ny * (k - 1));
+#pragma unroll 1
+    for (int q = 0; q < 18; ++q) {
+      const int ipop = q + 1;
+      const bool has = (mask >> ipop) & 1u;
+      const unsigned bal = __ballot_sync(0xffffffffu, has);
+      if (!has) continue;
+      const int w = base + woff[q * NW + warp] + __popc(bal & lane_lt);
+      if (w >= ls.cap) continue;
       const int ix = cix(ipop), iy = ciy(ipop), iz = ciz(ipop);
       const bool diag = (ix * ix + iy * iy + iz * iz) == 2;
-      long long node = (long long)(i - 1) + (long long)g.nx * ((j - 1) + (long long)g.ny * (k - 1));
-      if (w < ls.cap) {
-        code[w] = (int32_t)(node * 32 + ipop);
-        // partlib.f90:1016-1023 with aa = |x0 - x1|^2 = |c|^2 (1 or 2) and
-        // bb = x1.(x0 - x1) = -x1.c taken exactly: the same root without the
-        // cancellation in the reference's aa and without divisions
-        if (alpha_fp32) {
-          const float xf = xxf + (float)ix, yf = yyf + (float)iy, zf = zzf + (float)iz;
-          const float cc = xf * xf + yf * yf + zf * zf - rad2f;
-          const float bb = -(xf * (float)ix + yf * (float)iy + zf * (float)iz);
-          const float a0 = diag ? 0.5f * bb : bb;
-          const float ca = diag ? 0.5f * cc : cc;
-          const float a1 = sqrtf(fmaxf(a0 * a0 - ca, 0.0f));
-          alph32[w] = 1.0f - (-a0 + a1);
-        } else {
-          const double xc = xval[min(r, 2)][ci], yc = row_y[r], zc = row_z[r];
-          double xx1 = (double)(i + ix) - 0.5 - xc;
-          double yy1 = (double)(j + iy) - 0.5 - yc + 0.0;
-          double zz1 = (double)(k + iz) - 0.5 - zc + 0.0;
-          double cc = xx1 * xx1 + yy1 * yy1 + zz1 * zz1 - rad2;
-          double bb = -((double)ix * xx1 + (double)iy * yy1 + (double)iz * zz1);
-          double a0 = diag ? 0.5 * bb : bb;
-          double ca = diag ? 0.5 * cc : cc;
-          double a1 = sqrt(fmax(a0 * a0 - ca, 0.0));
-          alph[w] = 1.0 - (-a0 + a1);
-        }
+      code[w] = (int32_t)(node * 32 + ipop);
+      // partlib.f90:1016-1023 with aa = |x0 - x1|^2 = |c|^2 (1 or 2) and
+      // bb = x1.(x0 - x1) = -x1.c taken exactly: the same root without the
+      // cancellation in the reference's aa and without divisions
+      if (alpha_fp32) {
+        const float xf = xxf + (float)ix, yf = yyf + (float)iy, zf = zzf + (float)iz;
+        const float cc = xf * xf + yf * yf + zf * zf - rad2f;
+        const float bb = -(xf * (float)ix + yf * (float)iy + zf * (float)iz);
+        const float a0 = diag ? 0.5f * bb : bb;
+        const float ca = diag ? 0.5f * cc : cc;
+        const float a1 = sqrtf(fmaxf(a0 * a0 - ca, 0.0f));
+        alph32[w] = 1.0f - (-a0 + a1);
+      } else {
+        const double xc = xval[min(r, 2)][ci], yc = row_y[r], zc = row_z[r];
+        double xx1 = (double)(i + ix) - 0.5 - xc;
+        double yy1 = (double)(j + iy) - 0.5 - yc + 0.0;
+        double zz1 = (double)(k + iz) - 0.5 - zc + 0.0;
+        double cc = xx1 * xx1 + yy1 * yy1 + zz1 * zz1 - rad2;
+        double bb = -((double)ix * xx1 + (double)iy * yy1 + (double)iz * zz1);
+        double a0 = diag ? 0.5 * bb : bb;
+        double ca = diag ? 0.5 * cc : cc;
+        double a1 = sqrt(fmax(a0 * a0 - ca, 0.0));
+        alph[w] = 1.0 - (-a0 + a1);
       }
     }
     __syncthreads();
-    if (tid == 0) base += tot;
+    if (tid == 0) base += chunk_links;
     __syncthreads();
   }
   if (tid == 0) {
@@ -484,12 +538,13 @@ __global__ void __launch_bounds__(PB) k_bounce(Geometry g, ParticleView pv, cons
   const R omg1 = R(pv.omgp[3 * p]), omg2 = R(pv.omgp[3 * p + 1]), omg3 = R(pv.omgp[3 * p + 2]);
   const bool channel = g.channel != 0;
   for (int l = threadIdx.x; l < cnt; l += PB) {
-    int cd = code[l];
-    int ipop = cd & 31;
-    long long node = cd >> 5;
-    int i = (int)(node % g.nx);
-    long long r = node / g.nx;
-    int j = (int)(r % g.ny), k = (int)(r / g.ny);
+    // 32-bit decode: node < 2^26
+    const int cd = code[l];
+    const int ipop = cd & 31;
+    const int node = cd >> 5;
+    const int r = node / g.nx;
+    const int i = node - r * g.nx;
+    const int k = r / g.ny, j = r - k * g.ny;
     R alpha = alph[l];
     int ipp = ipopp(ipop);
     R xpnt = R(i + 1) - R(0.5), ypnt = R(j + 1) - R(0.5), zpnt = R(k + 1) - R(0.5);
@@ -596,19 +651,18 @@ __global__ void __launch_bounds__(PB) k_bounce_store(Geometry g, ParticleView pv
   const int32_t* code = ls.code + (long long)p * ls.cap;
   const T* f9s = reinterpret_cast<const T*>(ls.f9 + (long long)p * ls.cap);
   for (int l = threadIdx.x; l < cnt; l += PB) {
-    int cd = code[l];
-    int ipop = cd & 31;
-    long long node = cd >> 5;
-    int ipp = ipopp(ipop);
+    const int cd = code[l];
+    const int ipop = cd & 31;
+    const int node = cd >> 5;
+    const int ipp = ipopp(ipop);
+    const int r = node / g.nx;
+    const int i = node - r * g.nx;
     if (pushed) {
-      int i = (int)(node % g.nx);
       int it = i + cix(ipop);
       if (g.channel && (it < 0 || it >= g.nx)) continue;
       f[ipp * g.N + node] = f9s[l];
     } else {
-      int i = (int)(node % g.nx);
-      long long r = node / g.nx;
-      int j = (int)(r % g.ny), k = (int)(r / g.ny);
+      const int k = r / g.ny, j = r - k * g.ny;
       int it = i + cix(ipop);
       if (g.channel && (it < 0 || it >= g.nx)) continue;
       it = wrapi(it, g.nx);
