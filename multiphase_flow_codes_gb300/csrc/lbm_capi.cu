@@ -176,6 +176,18 @@ T* fbuf(lbm_ctx* c, int i) { return static_cast<T*>(c->f[i]); }
 template <typename T>
 T* mbuf(lbm_ctx* c, int comp) { return static_cast<T*>(c->macro) + comp * c->g.N; }
 
+// a flag buffer: N particle ids, then the solid mask (Geometry::sw words a row)
+size_t flag_bytes(const Geometry& g) {
+  return (size_t)g.N * sizeof(int32_t) + (size_t)g.ny * g.nz * g.sw * sizeof(uint32_t);
+}
+// all nodes fluid: ids -1, mask clear
+cudaError_t reset_flags(lbm_ctx* c, int i) {
+  cudaError_t e = cudaMemsetAsync(c->flags[i], 0xff, (size_t)c->g.N * sizeof(int32_t), c->stream);
+  if (e != cudaSuccess) return e;
+  return cudaMemsetAsync(c->flags[i] + c->g.N, 0,
+                         (size_t)c->g.ny * c->g.nz * c->g.sw * sizeof(uint32_t), c->stream);
+}
+
 int check_status(lbm_ctx* ctx) {
   CK(cudaMemcpyAsync(ctx->status_host, ctx->status, sizeof(DevStatus), cudaMemcpyDeviceToHost,
                      ctx->stream));
@@ -298,7 +310,7 @@ void particle_phase(lbm_ctx* c, T* f_plain) {
   prof_end(c, LBM_PHASE_PARTICLES);
   int nf = 1 - c->fcur;
   prof_begin(c);
-  cudaMemsetAsync(c->flags[nf], 0xff, sizeof(int32_t) * c->g.N, c->stream);
+  reset_flags(c, nf);
   launch_links(c->g, pview(c), c->flags[nf], c->links, c->status, c->f32, c->stream);
   prof_end(c, LBM_PHASE_LINKS);
   prof_begin(c);
@@ -398,14 +410,17 @@ uint64_t footprint(const lbm_config& c, int64_t* cap_out) {
   uint64_t b = 0;
   b += 2 * 19 * N * es;   // populations
   b += 4 * N * es;        // macro
-  b += 2 * N * 4;         // flags
+  b += 2 * (N * 4 + (uint64_t)c.ny * c.nz * 16 * ((c.nx + 127) / 128));  // flags + masks
   uint64_t np = c.npart_max > 0 ? c.npart_max : 0;
   int64_t cap = c.link_capacity > 0 ? c.link_capacity : default_link_capacity(c.rad);
   if (cap_out) *cap_out = cap;
   b += np * 15 * 3 * 8;
   b += np * (uint64_t)cap * (4 + 8 + 8) + np * 4;
+  b += np * (kSweepBytes + 3 * 4);                       // nearest-image sweeps
+  if (np > 0) b += 2ull * std::max<uint64_t>(4096, 256 * np) * 4 + 4;  // refill list
   if (c.forcing == LBM_FORCING_STOCHASTIC) {
-    b += 3 * 9ull * c.ny * c.nz * 2 * es + 45ull * c.nz * 2 * 8;
+    b += 3ull * kRowCoef * c.ny * c.nz * es + 45ull * c.nz * 2 * 8;  // row tables, z table
+    b += 10ull * (c.ny + c.nz) * 8 + 2 * sizeof(ForcingDev) + 32 * 8;
   }
   b += 4ull * c.nx * es;
   uint64_t stage = std::min<uint64_t>(19 * N, kStagingDoubles) * 8;
@@ -576,6 +591,7 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
   g.nxh = g.nx / 2; g.nyh = g.ny / 2; g.nzh = g.nz / 2;
   g.N = (long long)g.nx * g.ny * g.nz;
   g.channel = cfg->boundary == LBM_BC_XWALLS;
+  g.sw = 4 * ((g.nx + 127) / 128);
   ctx->f32 = cfg->precision == LBM_PREC_F32;
   ctx->esz = ctx->f32 ? 4 : 8;
   // MRT rates, B/para.f90:91-135
@@ -627,8 +643,8 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
   al(&ctx->f[0], 19 * N * ctx->esz);
   al(&ctx->f[1], 19 * N * ctx->esz);
   al(&ctx->macro, 4 * N * ctx->esz);
-  al((void**)&ctx->flags[0], N * sizeof(int32_t));
-  al((void**)&ctx->flags[1], N * sizeof(int32_t));
+  al((void**)&ctx->flags[0], flag_bytes(g));
+  al((void**)&ctx->flags[1], flag_bytes(g));
   al((void**)&ctx->status, sizeof(DevStatus));
   al((void**)&ctx->staging, std::min<long long>(19 * N, kStagingDoubles) * sizeof(double));
   al((void**)&ctx->partial, 4 * 1024 * sizeof(double));
@@ -658,6 +674,8 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
     al((void**)&ctx->links.alpha, (size_t)ctx->npmax * cap * sizeof(double));
     al((void**)&ctx->links.f9, (size_t)ctx->npmax * cap * sizeof(double));
     al((void**)&ctx->links.count, (size_t)ctx->npmax * sizeof(int32_t));
+    al(&ctx->links.sweeps, (size_t)ctx->npmax * kSweepBytes);
+    al((void**)&ctx->links.sweep_ok, (size_t)ctx->npmax * 3 * sizeof(int32_t));
     ctx->fill.cap = std::max(4096, 256 * ctx->npmax);
     al((void**)&ctx->fill.node, (size_t)ctx->fill.cap * sizeof(int32_t));
     al((void**)&ctx->fill.part, (size_t)ctx->fill.cap * sizeof(int32_t));
@@ -681,8 +699,8 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
   cudaMemsetAsync(ctx->f[0], 0, 19 * N * ctx->esz, ctx->stream);
   cudaMemsetAsync(ctx->f[1], 0, 19 * N * ctx->esz, ctx->stream);
   cudaMemsetAsync(ctx->macro, 0, 4 * N * ctx->esz, ctx->stream);
-  cudaMemsetAsync(ctx->flags[0], 0xff, N * sizeof(int32_t), ctx->stream);
-  cudaMemsetAsync(ctx->flags[1], 0xff, N * sizeof(int32_t), ctx->stream);
+  reset_flags(ctx, 0);
+  reset_flags(ctx, 1);
   cudaMemsetAsync(ctx->status, 0, sizeof(DevStatus), ctx->stream);
   // x twiddles for the forcing: cos/sin of 2 pi kx x / nx, kx = 1, 2
   {
@@ -772,7 +790,8 @@ int lbm_destroy(lbm_ctx* ctx) {
                   ctx->d_kyr5, ctx->d_kzr5, ctx->ztab, ctx->ytw, ctx->ztw, ctx->d_forcing_backup,
                   ctx->rowtab[0], ctx->rowtab[1],
                   ctx->rowtab[2], ctx->pbuf, ctx->first_move, ctx->links.code,
-                  ctx->links.alpha, ctx->links.f9, ctx->links.count, ctx->fill.node,
+                  ctx->links.alpha, ctx->links.f9, ctx->links.count, ctx->links.sweeps,
+                  ctx->links.sweep_ok, ctx->fill.node,
                   ctx->fill.part, ctx->fill.count};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -907,8 +926,8 @@ int lbm_upload_particles(lbm_ctx* ctx, int npart, const double* ypglb, const dou
     int one = 1;
     CK(cudaMemcpyAsync(ctx->first_move, &one, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
   }
-  CK(cudaMemsetAsync(ctx->flags[0], 0xff, ctx->g.N * sizeof(int32_t), ctx->stream));
-  CK(cudaMemsetAsync(ctx->flags[1], 0xff, ctx->g.N * sizeof(int32_t), ctx->stream));
+  CK(reset_flags(ctx, 0));
+  CK(reset_flags(ctx, 1));
   ctx->particles_on = npart > 0;
   if (npart > 0) launch_links(ctx->g, pview(ctx), ctx->flags[ctx->fcur], ctx->links, ctx->status, ctx->f32, ctx->stream);
   CK(cudaGetLastError());
@@ -1087,7 +1106,7 @@ int lbm_beads_links(lbm_ctx* ctx) {
   if (!ctx) return LBM_ERR_ARG;
   if (!ctx->particles_on) return LBM_OK;
   int nf = 1 - ctx->fcur;
-  CK(cudaMemsetAsync(ctx->flags[nf], 0xff, ctx->g.N * sizeof(int32_t), ctx->stream));
+  CK(reset_flags(ctx, nf));
   launch_links(ctx->g, pview(ctx), ctx->flags[nf], ctx->links, ctx->status, ctx->f32, ctx->stream);
   ctx->fcur = nf;
   CK(cudaGetLastError());

@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(128) k_fused(Geometry g, RatesT<T> r, const T*
   T f[NPOP];
 #pragma unroll
   for (int q = 0; q < NPOP; ++q) f[q] = fin[(size_t)q * N + n];
-  if (isnodes[n] < 0) {
+  if (!is_solid(solid_mask(isnodes, g), g, z * g.ny + y, x)) {
     T fp[3], fc[3];
     body_force2(fprev, fnew, x, z * g.ny + y, fp, fc);
     collide_fast(f, fp[0], fp[1], fp[2], fc[0], fc[1], fc[2], r);

@@ -5,8 +5,11 @@
 //                 double (plain path) or float (shifted FP32 path), two
 //                 buffers (current / next) of 19*N elements each;
 //   node flags    isnodes[z][y][x] int32: particle id (0-based) for solid
-//                 nodes, -1 for fluid; a second buffer keeps the flags of the
-//                 previous step (isnodes0 of the reference);
+//                 nodes, -1 for fluid, followed in the same allocation by
+//                 the solid mask: one bit per node, rows (y, z) of sw 32-bit
+//                 words (sw a multiple of 4, so a row is a 16-byte multiple);
+//                 a second buffer keeps the flags of the previous step
+//                 (isnodes0 of the reference);
 //   forcing       for the low-wavenumber forcing, per-row coefficient tables
 //                 rowtab[comp][kx][z][y] (complex) from which the body force
 //                 at any node follows with five FMAs per component, plus a
@@ -83,7 +86,17 @@ struct Geometry {
   int nxh, nyh, nzh;
   long long N;
   int channel;
+  int sw;                   // 32-bit words per row of the solid mask
 };
+
+// the solid mask that follows the N particle ids of a flag buffer
+__host__ __device__ __forceinline__ const uint32_t* solid_mask(const int32_t* isnodes,
+                                                               const Geometry& g) {
+  return reinterpret_cast<const uint32_t*>(isnodes + g.N);
+}
+__device__ __forceinline__ bool is_solid(const uint32_t* mask, const Geometry& g, int row, int x) {
+  return (mask[(size_t)row * g.sw + (x >> 5)] >> (x & 31)) & 1u;
+}
 
 // Particle state on the device, (3, npart_max) FP64 vectors, 0-based ids.
 struct ParticleView {
@@ -197,7 +210,10 @@ struct LinkSlab {
   double* f9;
   int32_t* count;
   int cap;
+  void* sweeps;      // per particle: nearest-image sweep events of the 3 axes (kSweepBytes)
+  int32_t* sweep_ok; // per particle and axis: 1 if the sweep reached its fixed point
 };
+constexpr int kSweepBytes = 7 * 96;
 // alpha_fp32: link fractions in single precision (the FP32 population path)
 void launch_links(const Geometry& g, const ParticleView& pv, int32_t* isnodes,
                   LinkSlab ls, DevStatus* st, int alpha_fp32, cudaStream_t s);

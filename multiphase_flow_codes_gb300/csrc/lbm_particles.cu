@@ -57,6 +57,7 @@ struct SweepEv {
   double v[MAXEV];
   double v0;
 };
+static_assert(7 * sizeof(SweepEv) <= kSweepBytes, "sweep slab too small");
 __device__ SweepEv sweep_events(double c, int n, int nh) {
   SweepEv s;
   s.nev = 0;
@@ -154,6 +155,45 @@ constexpr float kDecide = 4e-3f;
 // beads_links for one particle per block.  Integer outcomes (solid flags,
 // link sets) are exactly those of the reference's FP64 loop nest; the link
 // fraction alpha is FP64 (the reference formula) unless alpha_fp32 is set.
+// The nearest-image history of the in-place sweeps of beads_links
+// (partlib.f90:959-985) for every particle: one thread per (particle, axis).
+// The y and x sweeps are taken from three start states (the centre, the end
+// state of one sweep, the end state of two); the end state is a fixed point
+// from the second sweep on unless the centre lies within an ulp of
+// n/2 - 1/2, which sweep_ok reports.  FP64 and serial by nature; run for all
+// particles at once rather than inside each link block.
+__global__ void k_link_sweeps(Geometry g, ParticleView pv, LinkSlab ls) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 3 * pv.npart) return;
+  const int p = t / 3, axis = t - 3 * p;
+  SweepEv* out = reinterpret_cast<SweepEv*>(static_cast<char*>(ls.sweeps) + (size_t)p * kSweepBytes);
+  const double c0 = pv.ypglb[3 * p + (axis == 0 ? 1 : axis == 1 ? 0 : 2)];
+  int ok = 1;
+  if (!isfinite(c0)) {
+    ok = 0;
+  } else if (axis == 2) {
+    out[6] = sweep_events(c0, g.nz, g.nzh);
+    ok = out[6].ok;
+  } else if (axis == 1 && g.channel) {
+    // no x sweep in the channel (walls in x)
+    SweepEv e;
+    e.nev = 0; e.ok = 1; e.v0 = c0;
+    out[3] = e; out[4] = e; out[5] = e;
+  } else {
+    const int n = axis == 0 ? g.ny : g.nx, nh = axis == 0 ? g.nyh : g.nxh;
+    SweepEv* o = out + (axis == 0 ? 0 : 3);
+    double c = c0;
+    for (int s = 0; s < 3; ++s) {
+      o[s] = sweep_events(c, n, nh);
+      ok &= o[s].ok;
+      c = sweep_value(o[s], n);
+    }
+    SweepEv last = sweep_events(c, n, nh);
+    if (sweep_value(last, n) != c) ok = 0;
+  }
+  ls.sweep_ok[3 * p + axis] = ok;
+}
+
 __global__ void __launch_bounds__(PB) k_links(Geometry g, ParticleView pv, int32_t* isnodes,
                                               LinkSlab ls, DevStatus* st, int alpha_fp32) {
   using Scan = cub::BlockScan<int, PB>;
@@ -196,35 +236,25 @@ __global__ void __launch_bounds__(PB) k_links(Geometry g, ParticleView pv, int32
     }
     return;
   }
-  // Sweep event lists for the start states of the y sweep (plane 0 starts
-  // at y0, plane 1 at Y1 = end of plane 0's sweep, later planes at Y2) and
-  // of the x sweep (rows likewise: x0, X1, X2), and for the single z sweep.
-  // The end state is a fixed point from the second sweep on (only a centre
-  // within an ulp of n/2 - 1/2 makes the third state differ from the second).
+  // Sweep event lists (k_link_sweeps) for the start states of the y sweep
+  // (plane 0 starts at y0, plane 1 at Y1 = end of plane 0's sweep, later
+  // planes at Y2) and of the x sweep (rows likewise: x0, X1, X2), and for the
+  // single z sweep.
   __shared__ SweepEv sev[7];  // 0..2: y states, 3..5: x states, 6: z
+  if (tid < 7) sev[tid] = reinterpret_cast<const SweepEv*>(
+      static_cast<const char*>(ls.sweeps) + (size_t)p * kSweepBytes)[tid];
   if (tid == 0) {
-    double c = y0;
-    for (int s = 0; s < 3; ++s) {
-      sev[s] = sweep_events(c, g.ny, g.nyh);
-      c = sweep_value(sev[s], g.ny);
-    }
-    SweepEv last = sweep_events(c, g.ny, g.nyh);
-    if (sweep_value(last, g.ny) != c || !(sev[0].ok && sev[1].ok && sev[2].ok)) fixed_ok = 0;
-  } else if (tid == 32 && !channel) {
-    double c = x0;
-    for (int s = 0; s < 3; ++s) {
-      sev[3 + s] = sweep_events(c, g.nx, g.nxh);
-      c = sweep_value(sev[3 + s], g.nx);
-    }
-    SweepEv last = sweep_events(c, g.nx, g.nxh);
-    if (sweep_value(last, g.nx) != c || !(sev[3].ok && sev[4].ok && sev[5].ok)) fixed_ok = 0;
-  } else if (tid == 64) {
-    sev[6] = sweep_events(z0, g.nz, g.nzh);
-    if (!sev[6].ok) fixed_ok = 0;
+    const int32_t* ok = ls.sweep_ok + 3 * p;
+    if (!(ok[0] && ok[1] && ok[2])) fixed_ok = 0;
   }
+  // candidate windows of the three axes, computed once for the block
+  __shared__ Cands cands[3];
+  if (tid == 0) cands[0] = make_cands(y0, g.ny, radp2, true);
+  else if (tid == 32) cands[1] = make_cands(x0, g.nx, radp2, !channel);
+  else if (tid == 64) cands[2] = make_cands(z0, g.nz, radp2, true);
   __syncthreads();
-  Cands cy = make_cands(y0, g.ny, radp2, true);
-  Cands cx = make_cands(x0, g.nx, radp2, !channel);
+  const Cands& cy = cands[0];
+  const Cands& cx = cands[1];
   const int ty = min(cy.total(), MAXC);
   const int tx = min(cx.total(), MAXC);
   for (int t = tid; t < 3 * MAXC; t += PB) {
@@ -240,7 +270,7 @@ __global__ void __launch_bounds__(PB) k_links(Geometry g, ParticleView pv, int32
   __syncthreads();
 
   // ---- planes: k with |zz0| <= radp2, zc from the k-sweep starting at z0
-  Cands cz = make_cands(z0, g.nz, radp2, true);
+  const Cands& cz = cands[2];
   int tz = cz.total();
   for (int c0 = 0; c0 < tz; c0 += PB) {
     int t = c0 + tid;
@@ -327,6 +357,9 @@ __global__ void __launch_bounds__(PB) k_links(Geometry g, ParticleView pv, int32
           const int i = cx.at(ci);
           long long node = (long long)(i - 1) + (long long)g.nx * ((j - 1) + (long long)g.ny * (k - 1));
           atomicMax(&isnodes[node], p);
+          uint32_t* mask = const_cast<uint32_t*>(solid_mask(isnodes, g));
+          atomicOr(&mask[((size_t)(k - 1) * g.ny + (j - 1)) * g.sw + ((i - 1) >> 5)],
+                   1u << ((i - 1) & 31));
         } else if (cl == 2) {
           ++cnt;
         }
@@ -361,6 +394,7 @@ __global__ void __launch_bounds__(PB) k_links(Geometry g, ParticleView pv, int32
   constexpr int PER_LANE = (NCNT + 31) / 32;
   __shared__ int woff[NCNT];
   __shared__ int chunk_links;
+  __shared__ int16_t link_src[PB * 18];  // per link of the chunk: near node (local) << 5 | ipop
   const int warp = tid >> 5, lane = tid & 31;
   const unsigned lane_lt = (1u << lane) - 1u;
   int32_t* code = ls.code + (long long)p * ls.cap;
@@ -429,25 +463,39 @@ __global__ void __launch_bounds__(PB) k_links(Geometry g, ParticleView pv, int32
       if (lane == 31) chunk_links = incl;
     }
     __syncthreads();
-    const int j = row_j[r], k = row_k[r];
-    const long long node =
-        (long long)(i - 1) + (long long)g.nx * ((j - 1) + (long long)g.ny * (k - 1));
+    {
+      const int j = row_j[r], k = row_k[r];
+      const long long node =
+          (long long)(i - 1) + (long long)g.nx * ((j - 1) + (long long)g.ny * (k - 1));
 #pragma unroll 1
-    for (int q = 0; q < 18; ++q) {
-      const int ipop = q + 1;
-      const bool has = (mask >> ipop) & 1u;
-      const unsigned bal = __ballot_sync(0xffffffffu, has);
-      if (!has) continue;
-      const int w = base + woff[q * NW + warp] + __popc(bal & lane_lt);
-      if (w >= ls.cap) continue;
+      for (int q = 0; q < 18; ++q) {
+        const int ipop = q + 1;
+        const bool has = (mask >> ipop) & 1u;
+        const unsigned bal = __ballot_sync(0xffffffffu, has);
+        if (!has) continue;
+        const int l = woff[q * NW + warp] + __popc(bal & lane_lt);
+        link_src[l] = (int16_t)((tid << 5) | ipop);
+        if (base + l < ls.cap) code[base + l] = (int32_t)(node * 32 + ipop);
+      }
+    }
+    __syncthreads();
+    // link fractions, one thread per link of the chunk (all lanes busy)
+    for (int l = tid; l < chunk_links; l += PB) {
+      const int w = base + l;
+      if (w >= ls.cap) break;
+      const int src = link_src[l];
+      const int ipop = src & 31;
+      const int rc = near_rc[n0 + (src >> 5)];
+      const int lr = rc >> 8, lci = rc & 255;
+      const int li = cx.at(lci);
       const int ix = cix(ipop), iy = ciy(ipop), iz = ciz(ipop);
       const bool diag = (ix * ix + iy * iy + iz * iz) == 2;
-      code[w] = (int32_t)(node * 32 + ipop);
       // partlib.f90:1016-1023 with aa = |x0 - x1|^2 = |c|^2 (1 or 2) and
       // bb = x1.(x0 - x1) = -x1.c taken exactly: the same root without the
       // cancellation in the reference's aa and without divisions
       if (alpha_fp32) {
-        const float xf = xxf + (float)ix, yf = yyf + (float)iy, zf = zzf + (float)iz;
+        const float xf = ((float)li - 0.5f) - xvalf[min(lr, 2)][lci] + (float)ix;
+        const float yf = row_yy[lr] + (float)iy, zf = row_zz[lr] + (float)iz;
         const float cc = xf * xf + yf * yf + zf * zf - rad2f;
         const float bb = -(xf * (float)ix + yf * (float)iy + zf * (float)iz);
         const float a0 = diag ? 0.5f * bb : bb;
@@ -455,10 +503,11 @@ __global__ void __launch_bounds__(PB) k_links(Geometry g, ParticleView pv, int32
         const float a1 = sqrtf(fmaxf(a0 * a0 - ca, 0.0f));
         alph32[w] = 1.0f - (-a0 + a1);
       } else {
-        const double xc = xval[min(r, 2)][ci], yc = row_y[r], zc = row_z[r];
-        double xx1 = (double)(i + ix) - 0.5 - xc;
-        double yy1 = (double)(j + iy) - 0.5 - yc + 0.0;
-        double zz1 = (double)(k + iz) - 0.5 - zc + 0.0;
+        const int lj = row_j[lr], lk = row_k[lr];
+        const double xc = xval[min(lr, 2)][lci], yc = row_y[lr], zc = row_z[lr];
+        double xx1 = (double)(li + ix) - 0.5 - xc;
+        double yy1 = (double)(lj + iy) - 0.5 - yc + 0.0;
+        double zz1 = (double)(lk + iz) - 0.5 - zc + 0.0;
         double cc = xx1 * xx1 + yy1 * yy1 + zz1 * zz1 - rad2;
         double bb = -((double)ix * xx1 + (double)iy * yy1 + (double)iz * zz1);
         double a0 = diag ? 0.5 * bb : bb;
@@ -502,15 +551,17 @@ struct Acc<float> {
 // pushed: the fused kernel has already moved it to its streaming target
 // (or bounced it back in place at a channel wall).
 template <typename T>
-__device__ __forceinline__ double read_post(const Geometry& g, const T* f, int pushed, int q, int i,
-                                            int j, int k) {
-  long long n = (long long)i + (long long)g.nx * (j + (long long)g.ny * k);
-  if (!pushed) return (double)f[q * g.N + n];
+__device__ __forceinline__ T read_post(const Geometry& g, const T* f, int pushed, int q, int i,
+                                       int j, int k) {
+  // 32-bit element indices: 19 N < 2^31 (N < 2^26 is enforced)
+  const int N = (int)g.N;
+  const int n = i + g.nx * (j + g.ny * k);
+  if (!pushed) return f[q * N + n];
   int it = i + cix(q);
-  if (g.channel && (it < 0 || it >= g.nx)) return (double)f[ipopp(q) * g.N + n];
+  if (g.channel && (it < 0 || it >= g.nx)) return f[ipopp(q) * N + n];
   it = wrapi(it, g.nx);
-  int jt = wrapi(j + ciy(q), g.ny), kt = wrapi(k + ciz(q), g.nz);
-  return (double)f[q * g.N + (long long)it + (long long)g.nx * (jt + (long long)g.ny * kt)];
+  const int jt = wrapi(j + ciy(q), g.ny), kt = wrapi(k + ciz(q), g.nz);
+  return f[q * N + it + g.nx * (jt + g.ny * kt)];
 }
 
 // beads_collision for one particle per block: every link computes the
@@ -536,7 +587,9 @@ __global__ void __launch_bounds__(PB) k_bounce(Geometry g, ParticleView pv, cons
   Acc<T> acc6[6];
   const R w1 = R(pv.wp[3 * p]), w2 = R(pv.wp[3 * p + 1]), w3 = R(pv.wp[3 * p + 2]);
   const R omg1 = R(pv.omgp[3 * p]), omg2 = R(pv.omgp[3 * p + 1]), omg3 = R(pv.omgp[3 * p + 2]);
+  const R xc0 = R(pv.ypglb[3 * p]), yc0 = R(pv.ypglb[3 * p + 1]), zc0 = R(pv.ypglb[3 * p + 2]);
   const bool channel = g.channel != 0;
+  const uint32_t* mask = solid_mask(isnodes, g);
   for (int l = threadIdx.x; l < cnt; l += PB) {
     // 32-bit decode: node < 2^26
     const int cd = code[l];
@@ -548,7 +601,7 @@ __global__ void __launch_bounds__(PB) k_bounce(Geometry g, ParticleView pv, cons
     R alpha = alph[l];
     int ipp = ipopp(ipop);
     R xpnt = R(i + 1) - R(0.5), ypnt = R(j + 1) - R(0.5), zpnt = R(k + 1) - R(0.5);
-    R xc = R(pv.ypglb[3 * p]), yc = R(pv.ypglb[3 * p + 1]), zc = R(pv.ypglb[3 * p + 2]);
+    R xc = xc0, yc = yc0, zc = zc0;
     if (!channel) xc = near_img_t<R>(xc, xpnt, g.nx, g.nxh);
     yc = near_img_t<R>(yc, ypnt, g.ny, g.nyh);
     zc = near_img_t<R>(zc, zpnt, g.nz, g.nzh);
@@ -579,14 +632,12 @@ __global__ void __launch_bounds__(PB) k_bounce(Geometry g, ParticleView pv, cons
       R ff2 = R(0), ff3 = R(0);
       if (out1) ibm1 = 2;
       else {
-        long long m1 = (long long)im1 + (long long)g.nx * (jm1 + (long long)g.ny * km1);
-        ibm1 = isnodes[m1] >= 0 ? 1 : -1;
+        ibm1 = is_solid(mask, g, km1 * g.ny + jm1, im1) ? 1 : -1;
         if (ibm1 < 0) ff2 = R(read_post(g, f, pushed, ipop, im1, jm1, km1));
       }
       if (out2) ibm2 = 2;
       else {
-        long long m2 = (long long)im2 + (long long)g.nx * (jm2 + (long long)g.ny * km2);
-        ibm2 = isnodes[m2] >= 0 ? 1 : -1;
+        ibm2 = is_solid(mask, g, km2 * g.ny + jm2, im2) ? 1 : -1;
         if (ibm1 < 0 && ibm2 < 0) ff3 = R(read_post(g, f, pushed, ipop, im2, jm2, km2));
       }
       if (ibm1 > 0) {
@@ -605,8 +656,7 @@ __global__ void __launch_bounds__(PB) k_bounce(Geometry g, ParticleView pv, cons
       R ff3 = R(0);
       if (out1) ibm1 = 2;
       else {
-        long long m1 = (long long)im1 + (long long)g.nx * (jm1 + (long long)g.ny * km1);
-        ibm1 = isnodes[m1] >= 0 ? 1 : -1;
+        ibm1 = is_solid(mask, g, km1 * g.ny + jm1, im1) ? 1 : -1;
         if (ibm1 < 0) ff3 = R(read_post(g, f, pushed, ipp, im1, jm1, km1));
       }
       if (ibm1 > 0) {
@@ -630,11 +680,40 @@ __global__ void __launch_bounds__(PB) k_bounce(Geometry g, ParticleView pv, cons
     acc6[4].add(dxmom * zz0 - dzmom * xx0);
     acc6[5].add(dymom * xx0 - dxmom * yy0);
   }
-  for (int c = 0; c < 6; ++c) {
-    double s = Red(red_tmp).Sum(acc6[c].value());
+  if constexpr (sizeof(T) == 4) {
+    // per warp: exact two-sum tree of the compensated FP32 partial sums;
+    // across warps: FP64 in a fixed order (deterministic)
+    __shared__ double wsum[6][PB / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      float hi = acc6[c].s, lo = -acc6[c].c;
+#pragma unroll
+      for (int d = 16; d > 0; d >>= 1) {
+        const float oh = __shfl_down_sync(0xffffffffu, hi, d);
+        const float ol = __shfl_down_sync(0xffffffffu, lo, d);
+        const float sh = hi + oh;            // two-sum of the high parts
+        const float bp = sh - hi;
+        const float err = (hi - (sh - bp)) + (oh - bp);
+        hi = sh;
+        lo = lo + ol + err;
+      }
+      if (lane == 0) wsum[c][warp] = (double)hi + (double)lo;
+    }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < 6) {
+      const int c = threadIdx.x;
+      double s = 0.0;
+      for (int w = 0; w < PB / 32; ++w) s += wsum[c][w];
       if (c < 3) fHIp[3 * p + c] = s; else torqp[3 * p + c - 3] = s;
+    }
+  } else {
+    for (int c = 0; c < 6; ++c) {
+      double s = Red(red_tmp).Sum(acc6[c].value());
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        if (c < 3) fHIp[3 * p + c] = s; else torqp[3 * p + c - 3] = s;
+      }
     }
   }
 }
@@ -1039,6 +1118,7 @@ __global__ void __launch_bounds__(128) k_fill_events(Geometry g, ParticleView pv
 void launch_links(const Geometry& g, const ParticleView& pv, int32_t* isnodes, LinkSlab ls,
                   DevStatus* st, int alpha_fp32, cudaStream_t s) {
   if (pv.npart <= 0) return;
+  { k_link_sweeps<<<(3 * pv.npart + 127) / 128, 128, 0, s>>>(g, pv, ls); count_launch(); }
   { k_links<<<pv.npart, PB, 0, s>>>(g, pv, isnodes, ls, st, alpha_fp32); count_launch(); }
 }
 

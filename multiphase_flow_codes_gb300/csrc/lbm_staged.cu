@@ -92,25 +92,27 @@ __device__ __forceinline__ void fence_mbar_init() {
 }
 
 // Shared memory of one CTA: S input stages, each holding the 19 population
-// rows, the flag row and the force-series coefficients of the row for the
+// rows, the solid-mask row and the force-series coefficients of the row for the
 // two force fields (kRowCoef values each); then the full and empty mbarriers
 // of every stage and an abort flag.
 template <typename T>
 struct StagedLayout {
-  int nx, S;
-  __host__ __device__ size_t coef_offset() const { return (size_t)nx * (NPOP * sizeof(T) + 4); }
+  int nx, S, sw;
+  __host__ __device__ size_t coef_offset() const {
+    return (size_t)nx * NPOP * sizeof(T) + (size_t)sw * 4;
+  }
   __host__ __device__ size_t stage_bytes() const { return coef_offset() + 2 * kRowCoef * sizeof(T); }
   __host__ __device__ size_t bar_offset() const { return S * stage_bytes(); }
   __host__ __device__ size_t total() const { return bar_offset() + 16 * (size_t)S + 16; }
 };
 
 // Producer warp: keeps the CTA's rows flowing into the S stages.  Lane q < 19
-// copies population row q, lane 19 the flag row, lanes 20 and 21 the force
+// copies population row q, lane 19 the solid-mask row, lanes 20 and 21 the force
 // coefficients of the row (tabulated forcing only).
 template <typename T>
 __device__ void stage_producer(const StagedLayout<T>& L, unsigned char* smem, uint64_t* full,
                                uint64_t* empty, volatile int* abort_flag, int row0, int nloc,
-                               const T* __restrict__ fin, const int32_t* __restrict__ isnodes,
+                               const T* __restrict__ fin, const uint32_t* __restrict__ mask,
                                const ForceView<T>& fa, const ForceView<T>& fb, int N,
                                DevStatus* st) {
   const int lane = threadIdx.x & 31, S = L.S, nx = L.nx;
@@ -139,7 +141,7 @@ __device__ void stage_producer(const StagedLayout<T>& L, unsigned char* smem, ui
     if (lane < NPOP)
       bulk_g2s(dst + (size_t)lane * nx, fin + (size_t)lane * N + base, row_bytes, full + s);
     else if (lane == NPOP)
-      bulk_g2s(dst + (size_t)NPOP * nx, isnodes + base, (unsigned)(nx * 4), full + s);
+      bulk_g2s(dst + (size_t)NPOP * nx, mask + (size_t)row * L.sw, (unsigned)(L.sw * 4), full + s);
     else if (lane == NPOP + 1 && ta)
       bulk_g2s(stage + L.coef_offset(), fa.rowtab + (size_t)row * kRowCoef, coef_bytes, full + s);
     else if (lane == NPOP + 2 && tb)
@@ -179,7 +181,7 @@ __global__ void __launch_bounds__(288) k_fused_staged(Geometry g, RatesT<T> r,
                                                       ForceView<T> fprev, ForceView<T> fnew,
                                                       int S, DevStatus* st) {
   extern __shared__ __align__(128) unsigned char smem[];
-  const StagedLayout<T> L{g.nx, S};
+  const StagedLayout<T> L{g.nx, S, g.sw};
   const int nx = g.nx, ny = g.ny, nz = g.nz;
   const int nrows = ny * nz;
   const int N = (int)g.N;
@@ -206,8 +208,8 @@ __global__ void __launch_bounds__(288) k_fused_staged(Geometry g, RatesT<T> r,
   __syncthreads();
 
   if (warp == 0) {
-    stage_producer<T>(L, smem, full, empty, abort_flag, row0, nloc, fin, isnodes, fprev, fnew, N,
-                      st);
+    stage_producer<T>(L, smem, full, empty, abort_flag, row0, nloc, fin, solid_mask(isnodes, g),
+                      fprev, fnew, N, st);
     return;
   }
 
@@ -227,7 +229,7 @@ __global__ void __launch_bounds__(288) k_fused_staged(Geometry g, RatesT<T> r,
     }
     const unsigned char* stage = smem + (size_t)s * L.stage_bytes();
     const T* in = reinterpret_cast<const T*>(stage);
-    const int32_t* fl = reinterpret_cast<const int32_t*>(in + (size_t)NPOP * nx);
+    const uint32_t* mrow = reinterpret_cast<const uint32_t*>(in + (size_t)NPOP * nx);
     const T* ka = reinterpret_cast<const T*>(stage + L.coef_offset());
     const T* kb = ka + kRowCoef;
     const int n0 = nxy * z + nx * y;
@@ -237,7 +239,7 @@ __global__ void __launch_bounds__(288) k_fused_staged(Geometry g, RatesT<T> r,
       T f[NPOP];
 #pragma unroll
       for (int q = 0; q < NPOP; ++q) f[q] = in[q * nx + x];
-      if (fl[x] < 0) {
+      if (!((mrow[x >> 5] >> (x & 31)) & 1u)) {
         const T c1 = fnew.xtw[4 * x], s1 = fnew.xtw[4 * x + 1];
         const T c2 = fnew.xtw[4 * x + 2], s2 = fnew.xtw[4 * x + 3];
         T fp[3], fc[3];
@@ -279,7 +281,7 @@ __global__ void __launch_bounds__(288) k_fused_staged_x2(Geometry g, RatesT<F2> 
                                                          ForceView<float> fnew, int S,
                                                          DevStatus* st) {
   extern __shared__ __align__(128) unsigned char smem[];
-  const StagedLayout<float> L{g.nx, S};
+  const StagedLayout<float> L{g.nx, S, g.sw};
   const int nx = g.nx, ny = g.ny, nz = g.nz;
   const int nrows = ny * nz;
   const int N = (int)g.N;
@@ -314,8 +316,8 @@ __global__ void __launch_bounds__(288) k_fused_staged_x2(Geometry g, RatesT<F2> 
   __syncthreads();
 
   if (warp == 0) {
-    stage_producer<float>(L, smem, full, empty, abort_flag, row0, nloc, fin, isnodes, fprev,
-                          fnew, N, st);
+    stage_producer<float>(L, smem, full, empty, abort_flag, row0, nloc, fin,
+                          solid_mask(isnodes, g), fprev, fnew, N, st);
     return;
   }
   const int cw = warp - 1;
@@ -358,13 +360,12 @@ __global__ void __launch_bounds__(288) k_fused_staged_x2(Geometry g, RatesT<F2> 
     const unsigned char* stage = smem + (size_t)s * L.stage_bytes();
     const float* in = reinterpret_cast<const float*>(stage);
     if (active) {
-      const int2 fl = *reinterpret_cast<const int2*>(
-          reinterpret_cast<const int32_t*>(in + (size_t)NPOP * nx) + x0);
+      const uint32_t mw = reinterpret_cast<const uint32_t*>(in + (size_t)NPOP * nx)[x0 >> 5];
       F2 f[NPOP];
 #pragma unroll
       for (int q = 0; q < NPOP; ++q)
         f[q] = F2(*reinterpret_cast<const unsigned long long*>(in + q * nx + x0), 0);
-      const bool fl0 = fl.x < 0, fl1 = fl.y < 0;
+      const bool fl0 = !((mw >> (x0 & 31)) & 1u), fl1 = !((mw >> ((x0 + 1) & 31)) & 1u);
       if (fl0 || fl1) {
         const float* ka = reinterpret_cast<const float*>(stage + L.coef_offset());
         F2 fp[3], fc[3];
@@ -424,7 +425,7 @@ template <typename T>
 bool staged_eligible(const Geometry& g, int S, bool packed) {
   if (g.nx % 4 != 0 || S < 2) return false;
   if (packed && (sizeof(T) != 4 || g.nx > 512)) return false;
-  const StagedLayout<T> L{g.nx, S};
+  const StagedLayout<T> L{g.nx, S, g.sw};
   return L.total() <= 227 * 1024;
 }
 
@@ -453,7 +454,7 @@ template <typename T>
 bool plan_fused_staged(const Geometry& g, int S, int ctas_per_sm, bool packed, int groups,
                        StagedPlan* plan) {
   if (!staged_eligible<T>(g, S, packed)) return false;
-  const StagedLayout<T> L{g.nx, S};
+  const StagedLayout<T> L{g.nx, S, g.sw};
   int dev = 0, sms = 0, fit = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return false;
   const void* kern = staged_kernel<T>(g.channel != 0, packed);
