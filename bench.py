@@ -305,6 +305,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--fp32-report", default="10,100,2000",
+                    help="steps at which the FP32-shifted run is compared with FP64 "
+                         "('' to skip)")
     ap.add_argument("--variant", default=None,
                     help="stream+collide kernel as 'variant,stages,groups,ctas_per_sm' "
                          "(default: autotuned on the workload)")
@@ -431,6 +434,15 @@ def main():
             "error_after_steps": args.warmup + args.steps,
             "phase_ms_per_step": {k: (v[0] / args.steps) for k, v in ph32.items()}}
         del f32
+        if args.fp32_report and rank == 0:
+            from multiphase_flow_codes_gb300 import precision
+            cps = [int(v) for v in args.fp32_report.split(",") if v]
+            line["fp32_shifted"]["error_vs_fp64"] = {
+                "checkpoints": precision.error_report(wl.cfg, u, y, cps),
+                "target": 1e-5,
+                "how": "FP32-shifted and FP64 boxes stepped side by side from the same seeded state; "
+                       "E(k) and dissipation from lbm_statistics, slip on the R+1..R+3 fluid shell, "
+                       "fHIp RMS over particles"}
 
     if not args.no_e2e:
         f0 = initial_f(u)

@@ -173,6 +173,28 @@ int lbm_rhoupdat(lbm_ctx* ctx);           /* collision.f90:213 rhoupdat       */
  * entries above in that order. */
 int lbm_step(lbm_ctx* ctx, int nsteps);
 
+/* ---- statistics (saveload.f90:1111-1338) --------------------------------- */
+/* Energy spectrum, dissipation and velocity-derivative moments of the
+ * velocity left by the last macrovar, as statistc computes them: forward FFT
+ * normalised by 1/N per axis, shells ik = int(|k| + 1/2), ik = 1..nshell,
+ * nshell = int(nx/2 - 1.5), the kx = 0 plane weighted 1/2.
+ *   ek[ik-1]  energy of shell ik (statistc's e_t, lattice units)
+ *   dk[ik-1]  dissipation 2 nu |k|^2 E of shell ik with k = 2 pi (kx/nx,
+ *             ky/ny, kz/nz) (statistc's e_ts times (2 pi / n)^2)
+ *   out[0] nshell, out[1] kinetic energy sum ek, out[2] dissipation sum dk,
+ *   out[3] skewness, out[4] flatness (statistc's formulas, which use wx in
+ *   place of wz), out[5] u' = sqrt(2 out[1] / 3)
+ * nek: length of ek and dk (entries past it are not written).  The first
+ * call allocates FFT plans and work space (about 3 x 2 N doubles). */
+int lbm_statistics(lbm_ctx* ctx, int nek, double* ek, double* dk, double* out);
+/* Slip velocity of every particle, (3, npart) Fortran order: w_p minus the
+ * mean fluid velocity over the fluid nodes at distance r_in <= r <= r_out
+ * from the centre.  (Interpolating the velocity at the centre, as the
+ * reference's trilinear does for initpartvel, returns the particle's own
+ * rigid-body velocity once macrovar fills the solid nodes, so the slip is
+ * taken on a fluid shell instead.)  No counterpart in the reference. */
+int lbm_particle_slip(lbm_ctx* ctx, double r_in, double r_out, double* slip);
+
 /* ---- kernel selection (no counterpart in the reference) ------------------ */
 /* Variants of the fused stream + collide kernel of lbm_step.  Both compute
  * the same per-node arithmetic; they differ in how the populations move. */

@@ -109,6 +109,8 @@ SIGNATURES = {
     "lbm_get_variant": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                   C.POINTER(C.c_int)]),
     "lbm_autotune": (C.c_int, [_P, C.c_int, _D]),
+    "lbm_statistics": (C.c_int, [_P, C.c_int, _D, _D, _D]),
+    "lbm_particle_slip": (C.c_int, [_P, C.c_double, C.c_double, _D]),
 }
 
 PHASES = ("stream_collide", "bounce", "particles", "links", "filling", "forcing")

@@ -1,8 +1,8 @@
 """Build the engine's shared library, ``_lib/liblbm_gb300.so``, from ``csrc/``.
 
 The library is plain CUDA C++ for sm_103a behind the C ABI of
-``include/lbm.h``; it links the CUDA runtime statically and depends on
-nothing else.  Translation units compile in parallel.  The particle and
+``include/lbm.h``; it links the CUDA runtime statically and cuFFT (used only
+by the statistics entry) dynamically.  Translation units compile in parallel.  The particle and
 forcing units are built with ``-fmad=false`` so that the geometry deciding
 solid flags, links and refill events rounds exactly like the CPU restatement
 used by the tests.
@@ -34,6 +34,7 @@ UNITS = [
     ("lbm_capi.cu", []),
     ("lbm_noalloc.cu", []),
     ("lbm_probe.cu", []),
+    ("lbm_stats.cu", []),
 ]
 
 
@@ -82,7 +83,9 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         msg = "\n".join(f"--- {s}\n{o}" for s, o in failed)
         raise RuntimeError(f"nvcc failed:\n{msg}")
     if force or _stale(LIB, objs):
-        cmd = [exe, *ARCH, "-shared", "-o", str(LIB), *map(str, objs)]
+        cudalib = Path(exe).resolve().parent.parent / "lib64"
+        cmd = [exe, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcufft",
+               "-Xlinker", "-rpath", "-Xlinker", str(cudalib)]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)

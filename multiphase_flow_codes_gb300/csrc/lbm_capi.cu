@@ -57,6 +57,8 @@ struct lbm_ctx {
   bool macro_derived = true;   // macro arrays equal macrovar(f) (or pending)
   int32_t* flags[2] = {nullptr, nullptr};
   int fcur = 0;
+  // statistics work space (cuFFT plans, shell permutation), made on first use
+  SpectrumWork* spec = nullptr;
   // stream + collide kernel (lbm_set_variant / lbm_autotune)
   int variant = LBM_VARIANT_DIRECT;
   StagedPlan staged;
@@ -785,6 +787,8 @@ int lbm_destroy(lbm_ctx* ctx) {
   if (!ctx) return LBM_OK;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->side) cudaStreamSynchronize(ctx->side);
+  spectrum_free(ctx->spec);
+  ctx->spec = nullptr;
   void* ptrs[] = {ctx->f[0], ctx->f[1], ctx->macro, ctx->flags[0], ctx->flags[1], ctx->status,
                   ctx->staging, ctx->partial, ctx->xtw, ctx->d_forcing, ctx->d_kxr6,
                   ctx->d_kyr5, ctx->d_kzr5, ctx->ztab, ctx->ytw, ctx->ztw, ctx->d_forcing_backup,
@@ -888,6 +892,47 @@ int lbm_download_macro(lbm_ctx* ctx, double* rho, double* ux, double* uy, double
     if (rc) return rc;
   }
   CK(cudaGetLastError());
+  return LBM_OK;
+}
+
+static int poll_status(lbm_ctx* ctx);
+
+int lbm_statistics(lbm_ctx* ctx, int nek, double* ek, double* dk, double* out) {
+  if (!ctx || !out || nek < 0 || (nek > 0 && (!ek || !dk))) return LBM_ERR_ARG;
+  if (int rc = poll_status(ctx)) return rc;
+  materialize_macro(ctx);
+  int rc = ctx->f32 ? spectrum_stats<float>(ctx->g, ctx->cfg.visc, mbuf<float>(ctx, 1),
+                                            mbuf<float>(ctx, 2), mbuf<float>(ctx, 3), &ctx->spec,
+                                            nek, ek, dk, out, ctx->stream)
+                    : spectrum_stats<double>(ctx->g, ctx->cfg.visc, mbuf<double>(ctx, 1),
+                                             mbuf<double>(ctx, 2), mbuf<double>(ctx, 3), &ctx->spec,
+                                             nek, ek, dk, out, ctx->stream);
+  if (rc) {
+    cudaGetLastError();
+    return fail(ctx, rc, "statistics: FFT or allocation failed");
+  }
+  CK(cudaGetLastError());
+  return LBM_OK;
+}
+
+int lbm_particle_slip(lbm_ctx* ctx, double r_in, double r_out, double* slip) {
+  if (!ctx || !slip || !(r_out > r_in) || r_in < 0.0) return LBM_ERR_ARG;
+  if (ctx->npart <= 0) return LBM_OK;
+  if (int rc = poll_status(ctx)) return rc;
+  materialize_macro(ctx);
+  double* d = nullptr;
+  CK(cudaMalloc((void**)&d, 3 * (size_t)ctx->npart * sizeof(double)));
+  if (ctx->f32)
+    launch_slip<float>(ctx->g, pview(ctx), mbuf<float>(ctx, 1), mbuf<float>(ctx, 2),
+                       mbuf<float>(ctx, 3), ctx->flags[ctx->fcur], r_in, r_out, d, ctx->stream);
+  else
+    launch_slip<double>(ctx->g, pview(ctx), mbuf<double>(ctx, 1), mbuf<double>(ctx, 2),
+                        mbuf<double>(ctx, 3), ctx->flags[ctx->fcur], r_in, r_out, d, ctx->stream);
+  cudaError_t e = cudaMemcpyAsync(slip, d, 3 * (size_t)ctx->npart * sizeof(double),
+                                  cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(d);
+  CK(e);
   return LBM_OK;
 }
 
@@ -1153,7 +1198,7 @@ int lbm_rhoupdat(lbm_ctx* ctx) {
 
 // Report a device error raised by an earlier lbm_step without blocking:
 // the status word is copied back asynchronously at the end of each call.
-int poll_status(lbm_ctx* ctx) {
+static int poll_status(lbm_ctx* ctx) {
   if (!ctx->status_pending) return 0;
   if (cudaEventQuery(ctx->ev_status) != cudaSuccess) return 0;
   ctx->status_pending = false;

@@ -203,6 +203,15 @@ template <typename T>
 void launch_forcing_tables(const Geometry& g, const ForcingDev* st, const double* ytw,
                            const double* ztw, T* rowtab, double* ztab, cudaStream_t s);
 
+// statistics (lbm_stats.cu): spectrum, dissipation and derivative moments
+// of statistc; per-particle slip velocity
+struct SpectrumWork;
+void spectrum_free(SpectrumWork* w);
+template <typename T>
+int spectrum_stats(const Geometry& g, double visc, const T* ux, const T* uy, const T* uz,
+                   SpectrumWork** work, int nek_out, double* ek, double* dk, double* out,
+                   cudaStream_t s);
+
 // particles
 struct LinkSlab {
   int32_t* code;     // node*32 + ipop
@@ -224,6 +233,9 @@ void launch_bounce_back(const Geometry& g, const ParticleView& pv, const T* f,
 template <typename T>
 void launch_bounce_scatter(const Geometry& g, const ParticleView& pv, T* f,
                            int pushed_layout, LinkSlab ls, cudaStream_t s);
+template <typename T>
+void launch_slip(const Geometry& g, const ParticleView& pv, const T* ux, const T* uy, const T* uz,
+                 const int32_t* isnodes, double r_in, double r_out, double* slip, cudaStream_t s);
 struct MoveState {
   double* ypglb; double* ypglbp; double* ypold;
   double* wp; double* wpp; double* omgp; double* omgpp;

@@ -138,6 +138,27 @@ class LBMBox:
         self._ck(self._L.lbm_mass_momentum(self._h, dptr(out)), "mass_momentum")
         return out
 
+    def statistics(self, nshell: int | None = None) -> dict:
+        """statistc's spectrum and moments of the current velocity
+        (saveload.f90:1111-1338): ek, dk per shell and the totals."""
+        n = int(self.nx / 2 - 1.5) if nshell is None else int(nshell)
+        ek = np.zeros(max(n, 1))
+        dk = np.zeros(max(n, 1))
+        out = np.zeros(6)
+        self._ck(self._L.lbm_statistics(self._h, n, dptr(ek), dptr(dk), dptr(out)), "statistics")
+        nek = int(out[0])
+        return {"ek": ek[:min(n, nek)], "dk": dk[:min(n, nek)], "energy": out[1],
+                "dissipation": out[2], "skewness": out[3], "flatness": out[4], "uprime": out[5]}
+
+    def particle_slip(self, r_in: float, r_out: float) -> np.ndarray:
+        """(npart, 3) slip: w_p minus the mean fluid velocity on the shell
+        r_in <= r <= r_out around each centre."""
+        out = np.zeros((max(self.npart, 0), 3))
+        if self.npart:
+            self._ck(self._L.lbm_particle_slip(self._h, float(r_in), float(r_out), dptr(out)),
+                     "particle_slip")
+        return out
+
     # ---- particles -------------------------------------------------------
     def release_particles(self, ypglb: np.ndarray, wp: np.ndarray | None = None,
                           omgp: np.ndarray | None = None):

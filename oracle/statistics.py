@@ -1,0 +1,80 @@
+"""CPU restatement of statistc's spectrum and moments (numpy).
+
+TEST INFRASTRUCTURE ONLY: the GPU statistics entry (lbm_statistics) is
+checked against this.  It follows 3DBox_Forced_HI_Turbulence_Moving_Particles_LBM/
+saveload.f90:1111-1338 with the wavenumbers of gaussian.f90:40-73 and the
+forward transform of mpifft.f90:52-108 (normalised by 1/N per axis):
+
+  E(ik)  = sum over the half spectrum kx >= 0, shell int(|k| + 1/2) = ik,
+           of |u^|^2 with the kx = 0 plane weighted 1/2;
+  D(ik)  = the same sum of 2 nu |q|^2 |u^|^2, q = 2 pi (kx/nx, ky/ny, kz/nz)
+           (the reference keeps integer k and folds (2 pi / n)^2 into dscale);
+  ik = 1 .. nek, nek = int(nx/2 - 1.5) (para.f90:83);
+  skewness / flatness of statistc, which sums wx^p + wy^p + wx^p
+  (saveload.f90:1181-1193) with w_a the spectral derivative d u_a / d x_a
+  (the Nyquist wavenumber of each axis dropped, so w_a is real).
+Parity unpinned against the reference itself (FFTW 2 and MPI are absent).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+
+def _signed(n: int) -> np.ndarray:
+    k = np.arange(n)
+    return np.where(k <= n // 2, k, k - n)
+
+
+def spectrum(ux: np.ndarray, uy: np.ndarray, uz: np.ndarray, visc: float):
+    """(ek, dk, out) as lbm_statistics returns them; fields are (nz, ny, nx)."""
+    nz, ny, nx = ux.shape
+    N = nx * ny * nz
+    nek = int(nx / 2 - 1.5)
+    v = [np.fft.rfftn(u, axes=(0, 1, 2)) / N for u in (ux, uy, uz)]
+    kx = np.arange(nx // 2 + 1)[None, None, :]
+    ky = _signed(ny)[None, :, None]
+    kz = _signed(nz)[:, None, None]
+    k2 = kx * kx + ky * ky + kz * kz
+    shell = (np.sqrt(k2.astype(np.float64)) + 0.5).astype(np.int64)
+    s = sum(np.abs(c) ** 2 for c in v)
+    s = np.where(kx == 0, 0.5 * s, s)
+    q2 = (2 * np.pi * kx / nx) ** 2 + (2 * np.pi * ky / ny) ** 2 + (2 * np.pi * kz / nz) ** 2
+    d = 2.0 * visc * q2 * s
+    sh = np.broadcast_to(shell, s.shape)
+    ek = np.zeros(nek)
+    dk = np.zeros(nek)
+    for ik in range(1, nek + 1):
+        m = sh == ik
+        ek[ik - 1] = s[m].sum()
+        dk[ik - 1] = d[m].sum()
+    # derivative moments (integer wavenumbers, as statistc; Nyquist dropped)
+    kxd = np.where(2 * kx == nx, 0, kx)
+    kyd = np.where(2 * ky == ny, 0, ky)
+    wx = np.fft.irfftn(1j * np.broadcast_to(kxd, v[0].shape) * v[0] * N, s=(nz, ny, nx), axes=(0, 1, 2))
+    wy = np.fft.irfftn(1j * np.broadcast_to(kyd, v[1].shape) * v[1] * N, s=(nz, ny, nx), axes=(0, 1, 2))
+    cc2 = ((wx ** 2 + wy ** 2 + wx ** 2) / 3.0).mean()
+    cc3 = ((wx ** 3 + wy ** 3 + wx ** 3) / 3.0).mean()
+    cc4 = ((wx ** 4 + wy ** 4 + wx ** 4) / 3.0).mean()
+    qq = ek.sum()
+    out = np.array([nek, qq, dk.sum(), cc3 / cc2 ** 1.5 if cc2 > 0 else 0.0,
+                    cc4 / cc2 ** 2 if cc2 > 0 else 0.0, np.sqrt(2.0 * qq / 3.0)])
+    return ek, dk, out
+
+
+def particle_slip(ux, uy, uz, isnodes, ypglb, wp, r_in, r_out, channel=False):
+    """w_p minus the mean fluid velocity on the shell r_in <= r <= r_out."""
+    nz, ny, nx = ux.shape
+    zc, yc, xc = np.meshgrid(np.arange(nz) + 0.5, np.arange(ny) + 0.5, np.arange(nx) + 0.5,
+                             indexing="ij")
+    out = np.zeros_like(np.asarray(ypglb, dtype=np.float64))
+    for p, (x0, y0, z0) in enumerate(ypglb):
+        def near(d, n):
+            return np.where(d > 0.5 * n, d - n, np.where(d < -0.5 * n, d + n, d))
+        dx = (xc - x0) if channel else near(xc - x0, nx)
+        dy, dz = near(yc - y0, ny), near(zc - z0, nz)
+        r2 = dx * dx + dy * dy + dz * dz
+        m = (r2 >= r_in * r_in) & (r2 <= r_out * r_out) & (isnodes < 0)
+        cnt = max(int(m.sum()), 1)
+        out[p] = np.asarray(wp[p]) - np.array([ux[m].sum(), uy[m].sum(), uz[m].sum()]) / cnt
+    return out

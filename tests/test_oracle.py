@@ -245,3 +245,22 @@ def test_channel_poiseuille(engine_lib, oracle_mod):
     ref = cfg.force_y * x * (nx - x) / (2 * cfg.visc)
     assert np.abs(uy - ref).max() <= 1e-12 * ref.max()
     assert np.abs(o.ux).max() <= 1e-18 and np.abs(o.uz).max() <= 1e-18
+
+
+def test_statistics_single_mode():
+    """One Fourier mode u_x = A cos(2 pi (k1 y + k2 z) / n): all energy A^2/4
+    in shell int(|k| + 1/2), dissipation 2 nu |q|^2 E."""
+    from oracle import statistics
+    n = 16
+    z, y, x = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    A, k1, k2 = 0.03, 2, 1
+    ux = A * np.cos(2 * np.pi * (k1 * y + k2 * z) / n)
+    zero = np.zeros_like(ux)
+    ek, dk, out = statistics.spectrum(ux, zero, zero, visc=0.0036)
+    shell = int(np.sqrt(k1 * k1 + k2 * k2) + 0.5)
+    assert abs(ek[shell - 1] - A * A / 4) < 1e-15
+    assert np.abs(np.delete(ek, shell - 1)).max() < 1e-18
+    q2 = (2 * np.pi / n) ** 2 * (k1 * k1 + k2 * k2)
+    assert abs(dk[shell - 1] - 2 * 0.0036 * q2 * A * A / 4) < 1e-16
+    assert abs(out[1] - 0.5 * (ux ** 2).mean()) < 1e-15   # Parseval: E = <u^2>/2
+    assert out[0] == int(n / 2 - 1.5)
