@@ -308,6 +308,8 @@ def main():
     ap.add_argument("--fp32-report", default="10,100,2000",
                     help="steps at which the FP32-shifted run is compared with FP64 "
                          "('' to skip)")
+    ap.add_argument("--batch-steps", type=int, default=500,
+                    help="steps of the 48-box batched ensemble (0: skip it)")
     ap.add_argument("--variant", default=None,
                     help="stream+collide kernel as 'variant,stages,groups,ctas_per_sm' "
                          "(default: autotuned on the workload)")
@@ -443,6 +445,14 @@ def main():
                 "how": "FP32-shifted and FP64 boxes stepped side by side from the same seeded state; "
                        "E(k) and dissipation from lbm_statistics, slip on the R+1..R+3 fluid shell, "
                        "fHIp RMS over particles"}
+
+    if args.batch_steps > 0 and rank == 0 and args.workload in ("config1", "box256_p1000_f64"):
+        from multiphase_flow_codes_gb300 import ensemble
+        be = ensemble.run(steps=args.batch_steps)
+        k = be["kernel"]
+        k["roofline"] = {"bound": "hbm", "achieved": k["achieved_gbs"], "peak": hbm, "unit": "GB/s",
+                         "frac": k["achieved_gbs"] / hbm}
+        line["batched_ensemble"] = be
 
     if not args.no_e2e:
         f0 = initial_f(u)

@@ -219,6 +219,40 @@ int lbm_get_variant(lbm_ctx* ctx, int* variant, int* stages, int* groups, int* c
  * report its mean milliseconds per launch.  Synchronises the stream. */
 int lbm_autotune(lbm_ctx* ctx, int reps, double* best_ms);
 
+/* ---- many boxes at once (no counterpart in the reference) ----------------- */
+/* A batch advances several independent contexts together: each box's
+ * FORCING and particle subroutines run on the box's own stream, and one
+ * persistent kernel streams and collides every box.  Boxes must be FP32,
+ * have nx a multiple of 4 and at most 128, share boundary, viscosity, MRT
+ * rates and forcing kind, and be at the same step (all advanced equally
+ * since creation).  A box gives the same result in a batch as alone through
+ * a batch of one.  While batched, a context must not be stepped on its own;
+ * reading its state (downloads, statistics) is allowed after
+ * lbm_batch_synchronize.  lbm_batch_destroy returns the contexts to
+ * standalone use. */
+typedef struct lbm_batch lbm_batch;
+int lbm_batch_create(lbm_ctx** ctxs, int n, lbm_batch** out);
+int lbm_batch_destroy(lbm_batch* batch);
+const char* lbm_batch_last_error(const lbm_batch* batch);
+/* Advance every box nsteps steps.  use_graph = 1: whole cycles of 6 steps
+ * (buffer parity x forcing-table rotation) are captured once into a CUDA
+ * graph and replayed; the remainder runs directly.  Does not block. */
+int lbm_batch_step(lbm_batch* batch, int nsteps, int use_graph);
+/* Wait for the batch's work and report any device-side error of any box. */
+int lbm_batch_synchronize(lbm_batch* batch);
+/* Schedule of the batched stream + collide kernel: stages (2..8), consumer
+ * groups (1, 2 or 4; stages a multiple of groups), CTAs per SM (0: as many
+ * as fit).  lbm_batch_autotune times every schedule on the current state
+ * (without advancing it) and keeps the fastest. */
+int lbm_batch_set_schedule(lbm_batch* batch, int stages, int groups, int ctas_per_sm);
+int lbm_batch_get_schedule(lbm_batch* batch, int* stages, int* groups, int* ctas_per_sm);
+int lbm_batch_autotune(lbm_batch* batch, int reps, double* best_ms);
+/* total lattice nodes of the batch's boxes */
+int64_t lbm_batch_nodes(const lbm_batch* batch);
+/* Stream on which lbm_batch_step enqueues and finishes each call (the boxes'
+ * own streams fork from and join back into it); NULL: the batch's own. */
+int lbm_batch_set_stream(lbm_batch* batch, void* stream);
+
 /* ---- diagnostics --------------------------------------------------------- */
 /* FP64 totals over all nodes: out[0] = sum f (mass), out[1..3] = momentum
  * sum c f. */

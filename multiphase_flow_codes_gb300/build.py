@@ -29,6 +29,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relax
 UNITS = [
     ("lbm_fluid.cu", []),
     ("lbm_staged.cu", []),
+    ("lbm_batch.cu", []),
     ("lbm_forcing.cu", ["-fmad=false"]),
     ("lbm_particles.cu", ["-fmad=false"]),
     ("lbm_capi.cu", []),

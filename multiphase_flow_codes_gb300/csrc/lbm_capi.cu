@@ -59,6 +59,11 @@ struct lbm_ctx {
   int fcur = 0;
   // statistics work space (cuFFT plans, shell permutation), made on first use
   SpectrumWork* spec = nullptr;
+  // member of an lbm_batch (stepped only through the batch); batch_ready:
+  // the next step's FORCING already ran, into slot batch_slot
+  bool in_batch = false;
+  bool batch_ready = false;
+  int batch_slot = 0;
   // stream + collide kernel (lbm_set_variant / lbm_autotune)
   int variant = LBM_VARIANT_DIRECT;
   StagedPlan staged;
@@ -351,6 +356,25 @@ bool plan_staged(lbm_ctx* c, int variant, int stages, int ctas_per_sm, StagedPla
   }
   return c->f32 ? plan_fused_staged<float>(c->g, stages, ctas_per_sm, packed, groups, p)
                 : plan_fused_staged<double>(c->g, stages, ctas_per_sm, packed, groups, p);
+}
+
+// the part of a fused step after stream + collide: bounce-back, the
+// particle subroutines, and the host-side state of the step
+template <typename T>
+void step_post_t(lbm_ctx* c) {
+  T* fout = fbuf<T>(c, 1 - c->cur);
+  if (c->particles_on) {
+    prof_begin(c);
+    launch_bounce_back<T>(c->g, pview(c), fout, 1, c->flags[c->fcur], c->links, c->fHIp,
+                          c->torqp, c->stream);
+    launch_bounce_scatter<T>(c->g, pview(c), fout, 1, c->links, c->stream);
+    prof_end(c, LBM_PHASE_BOUNCE);
+    particle_phase<T>(c, fout);
+  }
+  c->cur = 1 - c->cur;
+  c->fmacro = c->latest;
+  c->macro_pending = true;
+  c->macro_derived = true;
 }
 
 template <typename T>
@@ -1045,10 +1069,16 @@ int lbm_download_links(lbm_ctx* ctx, int64_t capacity, int64_t* nlinks, int32_t*
 int lbm_forcing_state(lbm_ctx* ctx, int dir, int32_t* iseedf, int32_t* iyf, int32_t* ivf,
                       double* b) {
   if (!ctx) return LBM_ERR_ARG;
+  if (ctx->in_batch && dir != 0)
+    return fail(ctx, LBM_ERR_STATE, "the forcing state of a batched context is read-only");
   cancel_prefetch(ctx);
   if (ctx->cfg.forcing != LBM_FORCING_STOCHASTIC) return fail(ctx, LBM_ERR_STATE, "no stochastic forcing");
   ForcingDev st;
-  CK(cudaMemcpyAsync(&st, ctx->d_forcing, sizeof st, cudaMemcpyDeviceToHost, ctx->stream));
+  if (ctx->side) CK(cudaStreamSynchronize(ctx->side));
+  // in a batch the next step's FORCING may have run ahead: report the state
+  // after the last completed step
+  CK(cudaMemcpyAsync(&st, ctx->batch_ready ? ctx->d_forcing_backup : ctx->d_forcing, sizeof st,
+                     cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   if (dir == 0) {
     if (iseedf) *iseedf = st.iseedf;
@@ -1208,6 +1238,7 @@ static int poll_status(lbm_ctx* ctx) {
 
 int lbm_step(lbm_ctx* ctx, int nsteps) {
   if (!ctx || nsteps < 0) return LBM_ERR_ARG;
+  if (ctx->in_batch) return fail(ctx, LBM_ERR_STATE, "the context is stepped by its batch");
   if (int rc = poll_status(ctx)) return rc;
   for (int s = 0; s < nsteps; ++s) {
     if (!ctx->macro_derived) {
@@ -1355,6 +1386,398 @@ int lbm_mass_momentum(lbm_ctx* ctx, double out[4]) {
   for (int c = 0; c < 4; ++c) out[c] = 0.0;
   for (int b = 0; b < nb; ++b)
     for (int c = 0; c < 4; ++c) out[c] += ctx->partial_host[4 * b + c];
+  return LBM_OK;
+}
+
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// lbm_batch: many contexts advanced together
+struct lbm_batch {
+  std::vector<lbm_ctx*> ctx;
+  cudaStream_t main = nullptr;
+  bool own_main = false;
+  bool channel = false;
+  Rates r;
+  BatchBox* d_boxes = nullptr;
+  BatchTask* d_tasks = nullptr;
+  int ntasks = 0;
+  long long nodes = 0;
+  StagedPlan plan;
+  DevStatus* status = nullptr;
+  cudaEvent_t ev_fork = nullptr;
+  std::vector<cudaEvent_t> ev_join;
+  cudaGraphExec_t graph = nullptr;
+  int graph_key[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
+  std::vector<cudaEvent_t> ev_side;
+  int64_t graph_kernels = 0;
+  std::string err;
+};
+
+namespace {
+
+constexpr int kBatchCycle = 6;  // buffer parity (2) x forcing slot rotation (3)
+
+int bfail(lbm_batch* b, int code, const std::string& m) {
+  if (b) b->err = m;
+  return code;
+}
+#define BK(call)                                                                     \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess)                                                           \
+      return bfail(b, LBM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+constexpr int kKey = 8;
+void phase_key(const lbm_ctx* c, int k[kKey]) {
+  k[0] = c->cur; k[1] = c->fcur;
+  k[2] = c->latest.mode; k[3] = c->latest.slot;
+  k[4] = c->fmacro.mode; k[5] = c->fmacro.slot;
+  k[6] = c->batch_ready; k[7] = c->batch_slot;
+}
+
+bool same_phase(const lbm_batch* b) {
+  int k0[kKey], k[kKey];
+  phase_key(b->ctx[0], k0);
+  for (lbm_ctx* c : b->ctx) {
+    phase_key(c, k);
+    for (int i = 0; i < kKey; ++i)
+      if (k[i] != k0[i]) return false;
+    if (!c->macro_derived || c->prefetched) return false;
+  }
+  return true;
+}
+
+// One step of every box: the box's FORCING (prefetched during the previous
+// step, else run now) on its stream, one stream + collide kernel for all
+// boxes on the batch stream, then per box the next step's FORCING on its
+// side stream alongside bounce-back and the particle subroutines on its
+// stream; everything joins back into the batch stream.
+// returns "" or the first call that failed (capture included)
+std::string batch_step_eager(lbm_batch* b) {
+  auto chk = [&](cudaError_t e, const char* what, size_t i) -> std::string {
+    if (e != cudaSuccess)
+      return std::string(what) + " (box " + std::to_string(i) + "): " + cudaGetErrorString(e);
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(b->main, &cs);
+    if (cs == cudaStreamCaptureStatusInvalidated)
+      return std::string("capture invalidated after ") + what + " (box " + std::to_string(i) + ")";
+    return "";
+  };
+  std::string err;
+  if (!(err = chk(cudaEventRecord(b->ev_fork, b->main), "fork", 0)).empty()) return err;
+  for (size_t i = 0; i < b->ctx.size(); ++i) {
+    lbm_ctx* c = b->ctx[i];
+    if (!(err = chk(cudaStreamWaitEvent(c->stream, b->ev_fork, 0), "box wait", i)).empty()) return err;
+    if (c->batch_ready) {  // ran during the previous step, joined since
+      c->latest = {FM_TABLE, c->batch_slot};
+      c->batch_ready = false;
+    } else {
+      do_forcing(c);
+    }
+    if (!(err = chk(cudaGetLastError(), "forcing", i)).empty()) return err;
+    if (!(err = chk(cudaEventRecord(b->ev_join[i], c->stream), "join record", i)).empty()) return err;
+    if (!(err = chk(cudaStreamWaitEvent(b->main, b->ev_join[i], 0), "join wait", i)).empty()) return err;
+  }
+  const lbm_ctx* c0 = b->ctx[0];
+  BatchPhase ph{c0->cur, c0->fcur, c0->fmacro.mode, c0->fmacro.slot, c0->latest.mode,
+                c0->latest.slot};
+  launch_fused_batch(b->channel, b->d_boxes, b->d_tasks, b->ntasks, ph, b->r, b->plan, b->status,
+                     b->main);
+  if (!(err = chk(cudaGetLastError(), "batch kernel", 0)).empty()) return err;
+  if (!(err = chk(cudaEventRecord(b->ev_fork, b->main), "fork 2", 0)).empty()) return err;
+  for (size_t i = 0; i < b->ctx.size(); ++i) {
+    lbm_ctx* c = b->ctx[i];
+    if (!(err = chk(cudaStreamWaitEvent(c->stream, b->ev_fork, 0), "box wait 2", i)).empty()) return err;
+    if (c->cfg.forcing == LBM_FORCING_STOCHASTIC) {
+      // the next step's FORCING on the side stream, beside the particles;
+      // the state before it is kept so that leaving the batch can undo it
+      int slot = 0;
+      for (int q = 0; q < 3; ++q)
+        if (q != c->latest.slot) { slot = q; break; }
+      if (!(err = chk(cudaStreamWaitEvent(c->side, b->ev_fork, 0), "side wait", i)).empty()) return err;
+      cudaMemcpyAsync(c->d_forcing_backup, c->d_forcing, sizeof(ForcingDev),
+                      cudaMemcpyDeviceToDevice, c->side);
+      launch_forcing_into(c, slot, c->side);
+      if (!(err = chk(cudaGetLastError(), "next forcing", i)).empty()) return err;
+      if (!(err = chk(cudaEventRecord(b->ev_side[i], c->side), "side record", i)).empty()) return err;
+      if (!(err = chk(cudaStreamWaitEvent(b->main, b->ev_side[i], 0), "side join", i)).empty()) return err;
+      c->batch_ready = true;
+      c->batch_slot = slot;
+    }
+    step_post_t<float>(c);
+    if (!(err = chk(cudaGetLastError(), "particles", i)).empty()) return err;
+    if (!(err = chk(cudaEventRecord(b->ev_join[i], c->stream), "join record 2", i)).empty()) return err;
+    if (!(err = chk(cudaStreamWaitEvent(b->main, b->ev_join[i], 0), "join wait 2", i)).empty()) return err;
+  }
+  return "";
+}
+
+}  // namespace
+
+extern "C" {
+
+int lbm_batch_create(lbm_ctx** ctxs, int n, lbm_batch** out) {
+  if (!ctxs || n < 1 || !out) return LBM_ERR_ARG;
+  *out = nullptr;
+  lbm_ctx* c0 = ctxs[0];
+  if (!c0) return LBM_ERR_ARG;
+  for (int i = 0; i < n; ++i) {
+    lbm_ctx* c = ctxs[i];
+    if (!c || !c->f32 || !batch_box_ok(c->g) || c->g.channel != c0->g.channel ||
+        c->cfg.visc != c0->cfg.visc || c->cfg.mrt_type != c0->cfg.mrt_type ||
+        c->cfg.forcing != c0->cfg.forcing || c->in_batch)
+      return fail(c0, LBM_ERR_ARG,
+                  "batch: every box must be FP32, nx a multiple of 4 and at most 128, with the "
+                  "same boundary, viscosity, MRT rates and forcing, and in no other batch");
+    for (int j = 0; j < i; ++j)
+      if (ctxs[j] == c) return fail(c0, LBM_ERR_ARG, "batch: a context appears twice");
+  }
+  lbm_batch* b = new lbm_batch();
+  b->ctx.assign(ctxs, ctxs + n);
+  b->channel = c0->g.channel != 0;
+  b->r = c0->r;
+  for (lbm_ctx* c : b->ctx) {
+    cancel_prefetch(c);
+    cudaStreamSynchronize(c->stream);
+    c->in_batch = true;
+  }
+  // boxes and tasks
+  std::vector<BatchBox> boxes(n);
+  std::vector<BatchTask> tasks;
+  for (int i = 0; i < n; ++i) {
+    lbm_ctx* c = b->ctx[i];
+    BatchBox& x = boxes[i];
+    x.nx = c->g.nx; x.ny = c->g.ny; x.nz = c->g.nz; x.sw = c->g.sw; x.N = (int)c->g.N;
+    x.f[0] = static_cast<float*>(c->f[0]);
+    x.f[1] = static_cast<float*>(c->f[1]);
+    x.flags[0] = c->flags[0];
+    x.flags[1] = c->flags[1];
+    for (int s = 0; s < 3; ++s) x.rowtab[s] = static_cast<const float*>(c->rowtab[s]);
+    x.xtw = static_cast<const float*>(c->xtw);
+    x.cfx = 0.f; x.cfy = (float)c->cfg.force_y; x.cfz = 0.f;
+    const int k = batch_task_rows(c->g.nx, c->g.ny);
+    const int rows = c->g.ny * c->g.nz;
+    for (int r0 = 0; r0 < rows; r0 += k) tasks.push_back({i, r0, k});
+    b->nodes += c->g.N;
+  }
+  b->ntasks = (int)tasks.size();
+  int rc = 0;
+  if (cudaStreamCreateWithFlags(&b->main, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaMalloc((void**)&b->d_boxes, boxes.size() * sizeof(BatchBox)) != cudaSuccess ||
+      cudaMalloc((void**)&b->d_tasks, tasks.size() * sizeof(BatchTask)) != cudaSuccess ||
+      cudaMalloc((void**)&b->status, sizeof(DevStatus)) != cudaSuccess)
+    rc = LBM_ERR_CUDA;
+  b->own_main = true;
+  b->ev_join.resize(n, nullptr);
+  b->ev_side.resize(n, nullptr);
+  for (int i = 0; i < n && !rc; ++i)
+    if (cudaEventCreateWithFlags(&b->ev_join[i], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_side[i], cudaEventDisableTiming) != cudaSuccess)
+      rc = LBM_ERR_CUDA;
+  if (!rc) {
+    cudaMemcpy(b->d_boxes, boxes.data(), boxes.size() * sizeof(BatchBox), cudaMemcpyHostToDevice);
+    cudaMemcpy(b->d_tasks, tasks.data(), tasks.size() * sizeof(BatchTask), cudaMemcpyHostToDevice);
+    cudaMemset(b->status, 0, sizeof(DevStatus));
+    if (!plan_batch(b->channel, 4, 2, 0, b->ntasks, &b->plan) &&
+        !plan_batch(b->channel, 2, 1, 0, b->ntasks, &b->plan))
+      rc = LBM_ERR_ARG;
+  }
+  if (!rc && cudaDeviceSynchronize() != cudaSuccess) rc = LBM_ERR_CUDA;
+  if (rc) {
+    cudaGetLastError();
+    lbm_batch_destroy(b);
+    return rc;
+  }
+  *out = b;
+  return LBM_OK;
+}
+
+int lbm_batch_destroy(lbm_batch* b) {
+  if (!b) return LBM_OK;
+  if (b->main) cudaStreamSynchronize(b->main);
+  for (lbm_ctx* c : b->ctx) {
+    if (c->side) cudaStreamSynchronize(c->side);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->batch_ready) {
+      // the next step's FORCING ran ahead: restore the state before it
+      cudaMemcpy(c->d_forcing, c->d_forcing_backup, sizeof(ForcingDev), cudaMemcpyDeviceToDevice);
+      c->batch_ready = false;
+    }
+    c->in_batch = false;
+  }
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  for (cudaEvent_t e : b->ev_join)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : b->ev_side)
+    if (e) cudaEventDestroy(e);
+  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+  cudaFree(b->d_boxes);
+  cudaFree(b->d_tasks);
+  cudaFree(b->status);
+  if (b->own_main && b->main) cudaStreamDestroy(b->main);
+  delete b;
+  return LBM_OK;
+}
+
+const char* lbm_batch_last_error(const lbm_batch* b) { return b ? b->err.c_str() : "no batch"; }
+
+int lbm_batch_step(lbm_batch* b, int nsteps, int use_graph) {
+  if (!b || nsteps < 0) return LBM_ERR_ARG;
+  if (!same_phase(b))
+    return bfail(b, LBM_ERR_STATE, "batch: the boxes are not at the same step phase");
+  for (lbm_ctx* c : b->ctx) {
+    if (c->prof_on) return bfail(b, LBM_ERR_STATE, "batch: profiling is on for a box");
+  }
+  BK(cudaGetLastError());  // nothing pending from earlier calls
+  while (nsteps > 0) {
+    if (use_graph && nsteps >= kBatchCycle) {
+      int key[kKey];
+      phase_key(b->ctx[0], key);
+      bool match = b->graph != nullptr;
+      for (int i = 0; i < kKey && match; ++i) match = key[i] == b->graph_key[i];
+      if (!match) {
+        if (b->graph) {
+          cudaGraphExecDestroy(b->graph);
+          b->graph = nullptr;
+        }
+        const int64_t l0 = g_launches.load();
+        BK(cudaStreamBeginCapture(b->main, cudaStreamCaptureModeRelaxed));
+        std::string err;
+        for (int k = 0; k < kBatchCycle && err.empty(); ++k) err = batch_step_eager(b);
+        cudaGraph_t gr = nullptr;
+        cudaError_t ee = cudaStreamEndCapture(b->main, &gr);
+        if (!err.empty() || ee != cudaSuccess) {
+          if (gr) cudaGraphDestroy(gr);
+          cudaGetLastError();
+          return bfail(b, LBM_ERR_CUDA, "batch graph capture: " +
+                                            (err.empty() ? std::string(cudaGetErrorString(ee)) : err));
+        }
+        cudaError_t e = cudaGraphInstantiate(&b->graph, gr, 0);
+        cudaGraphDestroy(gr);
+        BK(e);
+        b->graph_kernels = g_launches.load() - l0;
+        for (int i = 0; i < kKey; ++i) b->graph_key[i] = key[i];
+        // capturing advanced the host state by one cycle; the replay below
+        // performs that cycle on the device
+        BK(cudaGraphLaunch(b->graph, b->main));
+      } else {
+        BK(cudaGraphLaunch(b->graph, b->main));
+        g_launches.fetch_add(b->graph_kernels);
+      }
+      nsteps -= kBatchCycle;
+    } else {
+      const std::string err = batch_step_eager(b);
+      if (!err.empty()) return bfail(b, LBM_ERR_CUDA, "batch step: " + err);
+      --nsteps;
+    }
+  }
+  BK(cudaGetLastError());
+  return LBM_OK;
+}
+
+int lbm_batch_synchronize(lbm_batch* b) {
+  if (!b) return LBM_ERR_ARG;
+  BK(cudaStreamSynchronize(b->main));
+  DevStatus st;
+  BK(cudaMemcpy(&st, b->status, sizeof st, cudaMemcpyDeviceToHost));
+  if (st.code) {
+    cudaMemset(b->status, 0, sizeof(DevStatus));
+    return bfail(b, st.code, "batch stream+collide kernel: a bounded wait ran out");
+  }
+  for (lbm_ctx* c : b->ctx) {
+    if (int rc = lbm_synchronize(c)) return bfail(b, rc, c->err);
+  }
+  return LBM_OK;
+}
+
+int lbm_batch_set_schedule(lbm_batch* b, int stages, int groups, int ctas_per_sm) {
+  if (!b) return LBM_ERR_ARG;
+  StagedPlan p;
+  if (!plan_batch(b->channel, stages, groups, ctas_per_sm, b->ntasks, &p)) {
+    cudaGetLastError();
+    return bfail(b, LBM_ERR_ARG, "batch: schedule does not apply");
+  }
+  b->plan = p;
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  return LBM_OK;
+}
+
+int lbm_batch_get_schedule(lbm_batch* b, int* stages, int* groups, int* ctas_per_sm) {
+  if (!b) return LBM_ERR_ARG;
+  if (stages) *stages = b->plan.S;
+  if (groups) *groups = b->plan.groups;
+  if (ctas_per_sm) *ctas_per_sm = b->plan.ctas_per_sm;
+  return LBM_OK;
+}
+
+int lbm_batch_autotune(lbm_batch* b, int reps, double* best_ms) {
+  if (!b || reps < 1) return LBM_ERR_ARG;
+  if (!same_phase(b)) return bfail(b, LBM_ERR_STATE, "batch: the boxes are not at the same step phase");
+  BK(cudaDeviceSynchronize());
+  const lbm_ctx* c0 = b->ctx[0];
+  // the stream + collide of the current state (fin -> fout, nothing advances)
+  BatchPhase ph{c0->cur, c0->fcur, c0->fmacro.mode, c0->fmacro.slot, c0->latest.mode,
+                c0->latest.slot};
+  cudaEvent_t e0, e1;
+  BK(cudaEventCreate(&e0));
+  BK(cudaEventCreate(&e1));
+  const StagedPlan keep = b->plan;
+  double best = 1e30;
+  StagedPlan bestp = keep;
+  for (int groups : {1, 2, 4})
+    for (int S = 2; S <= 8; ++S)
+      for (int per_sm : {1, 2, 3, 4, 6}) {
+        StagedPlan p;
+        if (!plan_batch(b->channel, S, groups, per_sm, b->ntasks, &p)) continue;
+        if (p.ctas_per_sm != per_sm) continue;
+        launch_fused_batch(b->channel, b->d_boxes, b->d_tasks, b->ntasks, ph, b->r, p, b->status,
+                           b->main);
+        cudaEventRecord(e0, b->main);
+        for (int k = 0; k < reps; ++k)
+          launch_fused_batch(b->channel, b->d_boxes, b->d_tasks, b->ntasks, ph, b->r, p,
+                             b->status, b->main);
+        cudaEventRecord(e1, b->main);
+        if (cudaEventSynchronize(e1) != cudaSuccess) break;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms / reps < best) {
+          best = ms / reps;
+          bestp = p;
+        }
+      }
+  cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->plan = best < 1e30 ? bestp : keep;
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  if (int rc = lbm_batch_synchronize(b)) return rc;
+  if (best_ms) *best_ms = best;
+  return LBM_OK;
+}
+
+int64_t lbm_batch_nodes(const lbm_batch* b) { return b ? b->nodes : 0; }
+
+int lbm_batch_set_stream(lbm_batch* b, void* stream) {
+  if (!b) return LBM_ERR_ARG;
+  BK(cudaStreamSynchronize(b->main));
+  if (b->own_main) cudaStreamDestroy(b->main);
+  if (stream) {
+    b->main = static_cast<cudaStream_t>(stream);
+    b->own_main = false;
+  } else {
+    BK(cudaStreamCreateWithFlags(&b->main, cudaStreamNonBlocking));
+    b->own_main = true;
+  }
   return LBM_OK;
 }
 

@@ -94,6 +94,10 @@ __host__ __device__ __forceinline__ const uint32_t* solid_mask(const int32_t* is
                                                                const Geometry& g) {
   return reinterpret_cast<const uint32_t*>(isnodes + g.N);
 }
+__host__ __device__ __forceinline__ const uint32_t* solid_mask_raw(const int32_t* isnodes,
+                                                                   long long N) {
+  return reinterpret_cast<const uint32_t*>(isnodes + N);
+}
 __device__ __forceinline__ bool is_solid(const uint32_t* mask, const Geometry& g, int row, int x) {
   return (mask[(size_t)row * g.sw + (x >> 5)] >> (x & 31)) & 1u;
 }
@@ -155,6 +159,26 @@ void launch_fused_staged(const Geometry& g, const Rates& r, const T* fin, T* fou
                          const int32_t* isnodes, const ForceView<T>& fprev,
                          const ForceView<T>& fnew, const StagedPlan& p, DevStatus* st,
                          cudaStream_t s);
+// many boxes in one persistent FP32 kernel (lbm_batch.cu)
+struct BatchBox {
+  int nx, ny, nz, sw, N;
+  float* f[2];                // population buffers
+  const int32_t* flags[2];    // flag buffers (ids, then the solid mask)
+  const float* rowtab[3];     // force coefficient slots
+  const float* xtw;
+  float cfx, cfy, cfz;        // constant force
+};
+struct BatchTask { int box, row0, nrows; };
+// the step-dependent buffer and forcing choices, the same for every box of
+// a batch advanced in lockstep
+struct BatchPhase { int cur, fcur, prev_mode, prev_slot, new_mode, new_slot; };
+int batch_task_rows(int nx, int ny);
+bool batch_box_ok(const Geometry& g);
+bool plan_batch(bool channel, int S, int groups, int ctas_per_sm, int ntasks, StagedPlan* plan);
+void launch_fused_batch(bool channel, const BatchBox* boxes, const BatchTask* tasks, int ntasks,
+                        const BatchPhase& ph, const Rates& r, const StagedPlan& p, DevStatus* st,
+                        cudaStream_t s);
+
 template <typename T>
 void launch_macrovar(const Geometry& g, const T* f, const int32_t* isnodes,
                      const ForceView<T>& fv, const ParticleView& pv, T* rho, T* ux,

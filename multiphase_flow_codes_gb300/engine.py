@@ -290,3 +290,72 @@ class LBMBox:
                 self.beads_links()
                 self.beads_filling()
             self.macrovar()
+
+
+class LBMBatch:
+    """Several LBMBox contexts advanced together (lbm_batch_*): one persistent
+    stream + collide kernel for all boxes, FORCING and the particle
+    subroutines of each box on the box's own stream, whole cycles of steps
+    replayed from a captured CUDA graph."""
+
+    def __init__(self, boxes: list):
+        self.boxes = list(boxes)          # keeps the contexts alive
+        self._L = capi.lib()
+        arr = (C.c_void_p * len(self.boxes))(*[b.handle.value for b in self.boxes])
+        h = C.c_void_p()
+        rc = self._L.lbm_batch_create(arr, len(self.boxes), C.byref(h))
+        if rc != capi.LBM_OK:
+            msg = self._L.lbm_last_error(self.boxes[0].handle)
+            raise LBMError(rc, f"lbm_batch_create: {msg.decode() if msg else ''}")
+        self._h = h
+
+    def _ck(self, rc: int, what: str):
+        if rc != capi.LBM_OK:
+            msg = self._L.lbm_batch_last_error(self._h)
+            raise LBMError(rc, f"{what}: {msg.decode() if msg else ''}")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.lbm_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def nodes(self) -> int:
+        return int(self._L.lbm_batch_nodes(self._h))
+
+    def step(self, nsteps: int = 1, graph: bool = True):
+        self._ck(self._L.lbm_batch_step(self._h, int(nsteps), 1 if graph else 0), "batch_step")
+
+    def synchronize(self):
+        self._ck(self._L.lbm_batch_synchronize(self._h), "batch_synchronize")
+
+    def set_stream(self, stream_ptr: int):
+        """Enqueue batch steps on this cudaStream_t (an integer)."""
+        self._ck(self._L.lbm_batch_set_stream(self._h, C.c_void_p(stream_ptr)), "batch_set_stream")
+
+    def set_schedule(self, stages: int, groups: int, ctas_per_sm: int = 0):
+        self._ck(self._L.lbm_batch_set_schedule(self._h, int(stages), int(groups), int(ctas_per_sm)),
+                 "batch_set_schedule")
+
+    def schedule(self) -> tuple:
+        s, g, c = C.c_int(0), C.c_int(0), C.c_int(0)
+        self._ck(self._L.lbm_batch_get_schedule(self._h, C.byref(s), C.byref(g), C.byref(c)),
+                 "batch_get_schedule")
+        return s.value, g.value, c.value
+
+    def autotune(self, reps: int = 3) -> float:
+        ms = C.c_double(0.0)
+        self._ck(self._L.lbm_batch_autotune(self._h, int(reps), C.byref(ms)), "batch_autotune")
+        return ms.value
