@@ -310,6 +310,9 @@ def main():
                          "('' to skip)")
     ap.add_argument("--batch-steps", type=int, default=500,
                     help="steps of the 48-box batched ensemble (0: skip it)")
+    ap.add_argument("--serve-seconds", type=float, default=20.0,
+                    help="window of the Poisson serving run (0: skip it)")
+    ap.add_argument("--serve-rate", type=float, default=20.0, help="requests per second")
     ap.add_argument("--variant", default=None,
                     help="stream+collide kernel as 'variant,stages,groups,ctas_per_sm' "
                          "(default: autotuned on the workload)")
@@ -453,6 +456,15 @@ def main():
         k["roofline"] = {"bound": "hbm", "achieved": k["achieved_gbs"], "peak": hbm, "unit": "GB/s",
                          "frac": k["achieved_gbs"] / hbm}
         line["batched_ensemble"] = be
+
+    if args.serve_seconds > 0 and rank == 0 and args.workload in ("config1", "box256_p1000_f64"):
+        from multiphase_flow_codes_gb300 import serving
+        sv = serving.poisson_run(rate=args.serve_rate, duration=args.serve_seconds)
+        sv["how"] = ("native lbm_server loop: Poisson arrivals, admission by lbm_footprint within a "
+                     "96 GiB budget, up to 96 resident solves, continuous batching of the FP32 channel "
+                     "solves into batched stream+collide launches, 50-step chunks; latency = done - "
+                     "submit; after the window the queue is drained and counted")
+        line["serving"] = sv
 
     if not args.no_e2e:
         f0 = initial_f(u)

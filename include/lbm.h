@@ -173,6 +173,23 @@ int lbm_rhoupdat(lbm_ctx* ctx);           /* collision.f90:213 rhoupdat       */
  * entries above in that order. */
 int lbm_step(lbm_ctx* ctx, int nsteps);
 
+/* ---- initial conditions on the device (no counterpart in the reference) --- */
+/* initpop (initial.f90:3-28) from a seeded divergence-free Gaussian velocity
+ * field with energy spectrum E(k) ~ k^4 exp(-2 (k/k0)^2), rescaled to a
+ * per-component rms u_rms, generated on the GPU (counter-based generator,
+ * cuFFT inverse transform): the role of initvel (initial.f90:55-116)
+ * without host FFTs.  Same seed, same field. */
+int lbm_init_spectral(lbm_ctx* ctx, double k0, double u_rms, uint64_t seed);
+/* initpartpos (partlib.f90:1-80) with the ranpp generator and seed `seed`,
+ * then lbm_upload_particles at rest.  LBM_ERR_OVERLAP if no placement is
+ * found in max_rounds rounds (0: 100000). */
+int lbm_init_particles(lbm_ctx* ctx, int npart, int seed, int max_rounds);
+/* Deterministic summary of the current state: out[0] mass (sum f), out[1..3]
+ * momentum, out[4] checksum sum_q,n (1 + q/19 + (n mod 97)/97) f, out[5]
+ * kinetic energy sum (u.u)/2 of the last macrovar.  Bitwise equal for
+ * bitwise equal states. */
+int lbm_summary(lbm_ctx* ctx, double out[6]);
+
 /* ---- statistics (saveload.f90:1111-1338) --------------------------------- */
 /* Energy spectrum, dissipation and velocity-derivative moments of the
  * velocity left by the last macrovar, as statistc computes them: forward FFT
@@ -240,6 +257,9 @@ const char* lbm_batch_last_error(const lbm_batch* batch);
 int lbm_batch_step(lbm_batch* batch, int nsteps, int use_graph);
 /* Wait for the batch's work and report any device-side error of any box. */
 int lbm_batch_synchronize(lbm_batch* batch);
+/* Wait for the batch's work and report only the batched kernel's own
+ * status; each box's errors are then read with lbm_synchronize(box). */
+int lbm_batch_wait(lbm_batch* batch);
 /* Schedule of the batched stream + collide kernel: stages (2..8), consumer
  * groups (1, 2 or 4; stages a multiple of groups), CTAs per SM (0: as many
  * as fit).  lbm_batch_autotune times every schedule on the current state
@@ -252,6 +272,59 @@ int64_t lbm_batch_nodes(const lbm_batch* batch);
 /* Stream on which lbm_batch_step enqueues and finishes each call (the boxes'
  * own streams fork from and join back into it); NULL: the batch's own. */
 int lbm_batch_set_stream(lbm_batch* batch, void* stream);
+
+/* ---- serving (no counterpart in the reference) --------------------------- */
+/* A request loop that keeps many solves resident on the GPU and advances
+ * them together.  A request: grid (nx, ny, nz), wall_axis (-1: periodic box
+ * with the stochastic forcing of the box preset; 0, 1, 2: halfway
+ * bounce-back walls normal to x, y or z with the channel preset's constant
+ * force), npart spheres of radius rad and density ratio rhopart placed by
+ * initpartpos, precision, nsteps, and an initial field from
+ * lbm_init_spectral(k0, u_rms, seed).  Requests are admitted in arrival
+ * order (skipping ahead over requests that do not fit) while the sum of
+ * lbm_footprint of the resident solves stays within hbm_budget bytes and at
+ * most max_active are resident; FP32 boxes with constant forcing, wall-axis
+ * extent a multiple of 4 and at most 128 are advanced by batches (one
+ * persistent stream + collide kernel), the others on their own streams;
+ * chunk_steps (even) bounds how many steps run between admissions.  A
+ * request gives the same result alone and in any mix.  The loop runs on a
+ * host thread of its own; submit, result, wait and stats may be called from
+ * any thread. */
+typedef struct lbm_server lbm_server;
+typedef struct lbm_request {
+  int32_t nx, ny, nz;
+  int32_t wall_axis;
+  int32_t npart;
+  int32_t nsteps;
+  int32_t precision;
+  int32_t mrt_type;      /* 0: the preset's MRT rates; 1..3: MRTtype of para.f90 */
+  double rad, rhopart;
+  double k0, u_rms;
+  uint64_t seed;
+} lbm_request;
+enum { LBM_REQ_QUEUED = 0, LBM_REQ_RUNNING = 1, LBM_REQ_DONE = 2, LBM_REQ_FAILED = 3 };
+typedef struct lbm_result {
+  int64_t id;
+  int32_t state;       /* LBM_REQ_*                                             */
+  int32_t error;       /* LBM_ERR_* when FAILED                                 */
+  int32_t steps_done;
+  int32_t batched;     /* 1 if some steps ran in a batch                        */
+  double t_submit, t_start, t_done;  /* seconds since lbm_server_create       */
+  double summary[6];   /* lbm_summary of the final state (momentum in the
+                          request's axes)                                       */
+} lbm_result;
+int lbm_server_create(uint64_t hbm_budget, int max_active, int chunk_steps, lbm_server** out);
+int lbm_server_submit(lbm_server* server, const lbm_request* req, int64_t* id);
+int lbm_server_result(lbm_server* server, int64_t id, lbm_result* out);
+/* block until request id is done or failed, at most timeout_s seconds
+ * (LBM_ERR_TIMEOUT otherwise) */
+int lbm_server_wait(lbm_server* server, int64_t id, double timeout_s);
+/* out[10]: submitted, done, failed, resident, queued, HBM bytes in use,
+ * batch regroupings, chunks advanced, seconds spent advancing, seconds since
+ * creation */
+int lbm_server_stats(lbm_server* server, double* out);
+/* stop the loop; resident solves end as LBM_REQ_FAILED (LBM_ERR_STATE) */
+int lbm_server_destroy(lbm_server* server);
 
 /* ---- diagnostics --------------------------------------------------------- */
 /* FP64 totals over all nodes: out[0] = sum f (mass), out[1..3] = momentum

@@ -110,18 +110,28 @@ SIGNATURES = {
                                   C.POINTER(C.c_int)]),
     "lbm_autotune": (C.c_int, [_P, C.c_int, _D]),
     "lbm_statistics": (C.c_int, [_P, C.c_int, _D, _D, _D]),
+    "lbm_init_spectral": (C.c_int, [_P, C.c_double, C.c_double, C.c_uint64]),
+    "lbm_init_particles": (C.c_int, [_P, C.c_int, C.c_int, C.c_int]),
+    "lbm_summary": (C.c_int, [_P, _D]),
     "lbm_particle_slip": (C.c_int, [_P, C.c_double, C.c_double, _D]),
     "lbm_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]),
     "lbm_batch_destroy": (C.c_int, [_P]),
     "lbm_batch_last_error": (C.c_char_p, [_P]),
     "lbm_batch_step": (C.c_int, [_P, C.c_int, C.c_int]),
     "lbm_batch_synchronize": (C.c_int, [_P]),
+    "lbm_batch_wait": (C.c_int, [_P]),
     "lbm_batch_set_schedule": (C.c_int, [_P, C.c_int, C.c_int, C.c_int]),
     "lbm_batch_get_schedule": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                          C.POINTER(C.c_int)]),
     "lbm_batch_autotune": (C.c_int, [_P, C.c_int, _D]),
     "lbm_batch_nodes": (C.c_int64, [_P]),
     "lbm_batch_set_stream": (C.c_int, [_P, _P]),
+    "lbm_server_create": (C.c_int, [C.c_uint64, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "lbm_server_submit": (C.c_int, [_P, _P, C.POINTER(C.c_int64)]),
+    "lbm_server_result": (C.c_int, [_P, C.c_int64, _P]),
+    "lbm_server_wait": (C.c_int, [_P, C.c_int64, C.c_double]),
+    "lbm_server_stats": (C.c_int, [_P, _D]),
+    "lbm_server_destroy": (C.c_int, [_P]),
 }
 
 PHASES = ("stream_collide", "bounce", "particles", "links", "filling", "forcing")

@@ -36,6 +36,7 @@ UNITS = [
     ("lbm_noalloc.cu", []),
     ("lbm_probe.cu", []),
     ("lbm_stats.cu", []),
+    ("lbm_server.cu", []),
 ]
 
 

@@ -195,6 +195,76 @@ cudaError_t reset_flags(lbm_ctx* c, int i) {
                          (size_t)c->g.ny * c->g.nz * c->g.sw * sizeof(uint32_t), c->stream);
 }
 
+// ranpp / ranff: Numerical Recipes ran1 (Park-Miller with Bays-Durham
+// shuffle) as B/partlib.f90:83-115 states it
+struct Ran1 {
+  int32_t idum, iy = 0, iv[32] = {0};
+  explicit Ran1(int seed) : idum(-std::abs(seed)) {}
+  double operator()() {
+    const int32_t IA = 16807, IM = 2147483647, IQ = 127773, IR = 2836, NTAB = 32;
+    const int32_t NDIV = 1 + (IM - 1) / NTAB;
+    if (idum <= 0 || iy == 0) {
+      idum = std::max(-idum, 1);
+      for (int j = NTAB + 8; j >= 1; --j) {
+        const int32_t k = idum / IQ;
+        idum = IA * (idum - k * IQ) - IR * k;
+        if (idum < 0) idum += IM;
+        if (j <= NTAB) iv[j - 1] = idum;
+      }
+      iy = iv[0];
+    }
+    const int32_t k = idum / IQ;
+    idum = IA * (idum - k * IQ) - IR * k;
+    if (idum < 0) idum += IM;
+    const int32_t j = iy / NDIV;
+    iy = iv[j];
+    iv[j] = idum;
+    return std::min((1.0 / IM) * (double)iy, 1.0 - 1.2e-7);
+  }
+};
+
+// initpartpos (B/partlib.f90:1-80, C/partlib.f90:10-24): uniform centres,
+// every particle that comes within mingap of a later one drawn again
+// (ovlpchk with istep00 = 0, B/partlib.f90:118-171); y is (3, npart)
+bool init_particle_positions(const Geometry& g, int npart, double rad, double mingap,
+                             double mingap_w, int seed, int max_rounds, double* y) {
+  Ran1 rng(seed);
+  std::vector<int> flag(npart, 1);
+  const double radpgap = rad + mingap_w;
+  auto near = [](double c, double p, int n, int nh) {
+    if (c - p > nh) c -= n;
+    if (c - p < -nh) c += n;
+    return c;
+  };
+  for (int round = 0; round < max_rounds; ++round) {
+    for (int ip = 0; ip < npart; ++ip) {
+      if (!flag[ip]) continue;
+      y[3 * ip] = g.channel ? radpgap + ((double)g.nx - 2.0 * radpgap) * rng() : (double)g.nx * rng();
+      y[3 * ip + 1] = (double)g.ny * rng();
+      y[3 * ip + 2] = (double)g.nz * rng();
+    }
+    std::fill(flag.begin(), flag.end(), 0);
+    bool any = false;
+    for (int a = 0; a + 1 < npart; ++a) {
+      const double xc = y[3 * a], yc = y[3 * a + 1], zc = y[3 * a + 2];
+      for (int b = a + 1; b < npart; ++b) {
+        double xb = y[3 * b], yb = y[3 * b + 1], zb = y[3 * b + 2];
+        if (!g.channel) xb = near(xb, xc, g.nx, g.nxh);
+        yb = near(yb, yc, g.ny, g.nyh);
+        zb = near(zb, zc, g.nz, g.nzh);
+        const double dx = xc - xb, dy = yc - yb, dz = zc - zb;
+        if (std::sqrt(dx * dx + dy * dy + dz * dz) - 2.0 * rad - mingap < 0.0) {
+          flag[a] = 1;
+          any = true;
+          break;
+        }
+      }
+    }
+    if (!any) return true;
+  }
+  return false;
+}
+
 int check_status(lbm_ctx* ctx) {
   CK(cudaMemcpyAsync(ctx->status_host, ctx->status, sizeof(DevStatus), cudaMemcpyDeviceToHost,
                      ctx->stream));
@@ -370,6 +440,10 @@ void step_post_t(lbm_ctx* c) {
     launch_bounce_scatter<T>(c->g, pview(c), fout, 1, c->links, c->stream);
     prof_end(c, LBM_PHASE_BOUNCE);
     particle_phase<T>(c, fout);
+  } else {
+    // without particles both flag buffers say "all fluid"; flipping keeps
+    // the buffer parity the same for every box of a batch
+    c->fcur = 1 - c->fcur;
   }
   c->cur = 1 - c->cur;
   c->fmacro = c->latest;
@@ -393,6 +467,8 @@ void fused_step_t(lbm_ctx* c) {
     launch_bounce_scatter<T>(c->g, pview(c), fout, 1, c->links, c->stream);
     prof_end(c, LBM_PHASE_BOUNCE);
     particle_phase<T>(c, fout);
+  } else {
+    c->fcur = 1 - c->fcur;  // as step_post_t
   }
   c->cur = 1 - c->cur;
   c->fmacro = c->latest;
@@ -416,6 +492,7 @@ void unfused_step_t(lbm_ctx* c) {
   launch_streaming<T>(c->g, fbuf<T>(c, c->cur), fbuf<T>(c, 1 - c->cur), c->stream);
   c->cur = 1 - c->cur;
   if (c->particles_on) particle_phase<T>(c, fbuf<T>(c, c->cur));
+  else c->fcur = 1 - c->fcur;  // as step_post_t
   c->fmacro = c->latest;
   c->macro_pending = true;
   c->macro_derived = true;
@@ -673,7 +750,7 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
   al((void**)&ctx->flags[1], flag_bytes(g));
   al((void**)&ctx->status, sizeof(DevStatus));
   al((void**)&ctx->staging, std::min<long long>(19 * N, kStagingDoubles) * sizeof(double));
-  al((void**)&ctx->partial, 4 * 1024 * sizeof(double));
+  al((void**)&ctx->partial, 6 * 1024 * sizeof(double));
   al(&ctx->xtw, 4 * g.nx * ctx->esz);
   if (!rc && cudaMallocHost((void**)&ctx->status_host, sizeof(DevStatus)) != cudaSuccess)
     rc = fail(ctx, LBM_ERR_NOMEM, "cudaMallocHost");
@@ -878,14 +955,9 @@ int lbm_download_f_soa(lbm_ctx* ctx, double* f) {
   return ctx->f32 ? download_soa_t<float>(ctx, f, false) : download_soa_t<double>(ctx, f, false);
 }
 
-int lbm_initpop(lbm_ctx* ctx, const double* ux, const double* uy, const double* uz) {
-  if (!ctx || !ux || !uy || !uz) return LBM_ERR_ARG;
+// initpop from a device velocity field dv[3][N]; frees dv
+static int initpop_device(lbm_ctx* ctx, double* dv) {
   const long long N = ctx->g.N;
-  double* dv = nullptr;
-  CK(cudaMalloc((void**)&dv, 3 * N * sizeof(double)));
-  cudaMemcpyAsync(dv, ux, N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
-  cudaMemcpyAsync(dv + N, uy, N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
-  cudaMemcpyAsync(dv + 2 * N, uz, N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
   if (ctx->f32) {
     launch_initpop<float>(ctx->g, dv, dv + N, dv + 2 * N, fbuf<float>(ctx, ctx->cur),
                           mbuf<float>(ctx, 0), ctx->stream);
@@ -902,6 +974,61 @@ int lbm_initpop(lbm_ctx* ctx, const double* ux, const double* uy, const double* 
   CK(cudaGetLastError());
   ctx->macro_pending = false;
   ctx->macro_derived = false;
+  return LBM_OK;
+}
+
+int lbm_initpop(lbm_ctx* ctx, const double* ux, const double* uy, const double* uz) {
+  if (!ctx || !ux || !uy || !uz) return LBM_ERR_ARG;
+  const long long N = ctx->g.N;
+  double* dv = nullptr;
+  CK(cudaMalloc((void**)&dv, 3 * N * sizeof(double)));
+  cudaMemcpyAsync(dv, ux, N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+  cudaMemcpyAsync(dv + N, uy, N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+  cudaMemcpyAsync(dv + 2 * N, uz, N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
+  return initpop_device(ctx, dv);
+}
+
+int lbm_init_spectral(lbm_ctx* ctx, double k0, double u_rms, uint64_t seed) {
+  if (!ctx || !(k0 > 0.0) || u_rms < 0.0) return LBM_ERR_ARG;
+  const long long N = ctx->g.N;
+  double* dv = nullptr;
+  CK(cudaMalloc((void**)&dv, 3 * N * sizeof(double)));
+  if (int rc = spectral_field(ctx->g, k0, u_rms, seed, dv, ctx->stream)) {
+    cudaFree(dv);
+    cudaGetLastError();
+    return fail(ctx, rc, "init_spectral: FFT or allocation failed");
+  }
+  return initpop_device(ctx, dv);
+}
+
+int lbm_init_particles(lbm_ctx* ctx, int npart, int seed, int max_rounds) {
+  if (!ctx || npart < 0 || npart > ctx->npmax) return LBM_ERR_ARG;
+  std::vector<double> y(3 * (size_t)npart), zero(3 * (size_t)npart, 0.0);
+  if (npart > 0 &&
+      !init_particle_positions(ctx->g, npart, ctx->cfg.rad, ctx->cfg.mingap, ctx->cfg.mingap_w,
+                               seed, max_rounds > 0 ? max_rounds : 100000, y.data()))
+    return fail(ctx, LBM_ERR_OVERLAP, "init_particles: no placement without overlap");
+  return lbm_upload_particles(ctx, npart, y.data(), zero.data(), zero.data());
+}
+
+int lbm_summary(lbm_ctx* ctx, double out[6]) {
+  if (!ctx || !out) return LBM_ERR_ARG;
+  materialize_macro(ctx);
+  const int nb = 1024;
+  if (ctx->f32)
+    launch_summary<float>(fbuf<float>(ctx, ctx->cur), ctx->g.N, mbuf<float>(ctx, 1),
+                          mbuf<float>(ctx, 2), mbuf<float>(ctx, 3), ctx->partial, nb, ctx->stream);
+  else
+    launch_summary<double>(fbuf<double>(ctx, ctx->cur), ctx->g.N, mbuf<double>(ctx, 1),
+                           mbuf<double>(ctx, 2), mbuf<double>(ctx, 3), ctx->partial, nb,
+                           ctx->stream);
+  std::vector<double> h(6 * (size_t)nb);
+  CK(cudaMemcpyAsync(h.data(), ctx->partial, h.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (int c = 0; c < 6; ++c) out[c] = 0.0;
+  for (int b = 0; b < nb; ++b)
+    for (int c = 0; c < 6; ++c) out[c] += h[6 * (size_t)b + c];
   return LBM_OK;
 }
 
@@ -1457,6 +1584,7 @@ bool same_phase(const lbm_batch* b) {
 // stream; everything joins back into the batch stream.
 // returns "" or the first call that failed (capture included)
 std::string batch_step_eager(lbm_batch* b) {
+  if (!same_phase(b)) return "the boxes are not at the same step phase";
   auto chk = [&](cudaError_t e, const char* what, size_t i) -> std::string {
     if (e != cudaSuccess)
       return std::string(what) + " (box " + std::to_string(i) + "): " + cudaGetErrorString(e);
@@ -1579,14 +1707,16 @@ int lbm_batch_create(lbm_ctx** ctxs, int n, lbm_batch** out) {
         cudaEventCreateWithFlags(&b->ev_side[i], cudaEventDisableTiming) != cudaSuccess)
       rc = LBM_ERR_CUDA;
   if (!rc) {
-    cudaMemcpy(b->d_boxes, boxes.data(), boxes.size() * sizeof(BatchBox), cudaMemcpyHostToDevice);
-    cudaMemcpy(b->d_tasks, tasks.data(), tasks.size() * sizeof(BatchTask), cudaMemcpyHostToDevice);
-    cudaMemset(b->status, 0, sizeof(DevStatus));
+    cudaMemcpyAsync(b->d_boxes, boxes.data(), boxes.size() * sizeof(BatchBox),
+                    cudaMemcpyHostToDevice, b->main);
+    cudaMemcpyAsync(b->d_tasks, tasks.data(), tasks.size() * sizeof(BatchTask),
+                    cudaMemcpyHostToDevice, b->main);
+    cudaMemsetAsync(b->status, 0, sizeof(DevStatus), b->main);
     if (!plan_batch(b->channel, 4, 2, 0, b->ntasks, &b->plan) &&
         !plan_batch(b->channel, 2, 1, 0, b->ntasks, &b->plan))
       rc = LBM_ERR_ARG;
   }
-  if (!rc && cudaDeviceSynchronize() != cudaSuccess) rc = LBM_ERR_CUDA;
+  if (!rc && cudaStreamSynchronize(b->main) != cudaSuccess) rc = LBM_ERR_CUDA;
   if (rc) {
     cudaGetLastError();
     lbm_batch_destroy(b);
@@ -1679,7 +1809,7 @@ int lbm_batch_step(lbm_batch* b, int nsteps, int use_graph) {
   return LBM_OK;
 }
 
-int lbm_batch_synchronize(lbm_batch* b) {
+int lbm_batch_wait(lbm_batch* b) {
   if (!b) return LBM_ERR_ARG;
   BK(cudaStreamSynchronize(b->main));
   DevStatus st;
@@ -1688,6 +1818,11 @@ int lbm_batch_synchronize(lbm_batch* b) {
     cudaMemset(b->status, 0, sizeof(DevStatus));
     return bfail(b, st.code, "batch stream+collide kernel: a bounded wait ran out");
   }
+  return LBM_OK;
+}
+
+int lbm_batch_synchronize(lbm_batch* b) {
+  if (int rc = lbm_batch_wait(b)) return rc;
   for (lbm_ctx* c : b->ctx) {
     if (int rc = lbm_synchronize(c)) return bfail(b, rc, c->err);
   }

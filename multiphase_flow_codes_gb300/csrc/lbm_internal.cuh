@@ -236,6 +236,15 @@ int spectrum_stats(const Geometry& g, double visc, const T* ux, const T* uy, con
                    SpectrumWork** work, int nek_out, double* ek, double* dk, double* out,
                    cudaStream_t s);
 
+// seeded divergence-free Gaussian velocity, E(k) ~ k^4 exp(-2 (k/k0)^2),
+// per-component rms urms, into u[3][N] (device); synchronises s
+int spectral_field(const Geometry& g, double k0, double urms, uint64_t seed, double* u,
+                   cudaStream_t s);
+// per-block sums: mass, momentum x/y/z, population checksum, kinetic energy
+template <typename T>
+void launch_summary(const T* f, long long N, const T* ux, const T* uy, const T* uz,
+                    double* partial, int nblocks, cudaStream_t s);
+
 // particles
 struct LinkSlab {
   int32_t* code;     // node*32 + ipop

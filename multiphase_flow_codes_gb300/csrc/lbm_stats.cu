@@ -153,7 +153,180 @@ __global__ void __launch_bounds__(256) k_slip(Geometry g, ParticleView pv, const
 
 inline unsigned blocks(long long n, int b) { return (unsigned)((n + b - 1) / b); }
 
+// ---- seeded solenoidal initial velocity --------------------------------
+// counter-based generator: a splitmix64 hash of (seed, counter)
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ double unit_open(uint64_t h) {  // (0, 1]
+  return ((double)(h >> 11) + 1.0) * (1.0 / 9007199254740992.0);
+}
+// standard complex Gaussian of (seed, mode, component) by Box-Muller
+__device__ __forceinline__ double2 gauss2(uint64_t seed, long long mode, int comp) {
+  const uint64_t h1 = mix64(seed ^ mix64((uint64_t)mode * 8 + 2 * comp));
+  const uint64_t h2 = mix64(seed ^ mix64((uint64_t)mode * 8 + 2 * comp + 1));
+  const double r = sqrt(-2.0 * log(unit_open(h1)));
+  const double t = 6.283185307179586 * unit_open(h2);
+  return make_double2(r * cos(t), r * sin(t));
+}
+
+// Half-spectrum coefficients (kx >= 0) of a divergence-free Gaussian field
+// with E(k) ~ k^4 exp(-2 (k/k0)^2): per mode a complex Gaussian vector,
+// projected off k, scaled by sqrt(E(k) / (4 pi k^2)).  The kx = 0 and
+// kx = nx/2 planes are made Hermitian (a mode and its mirror -k share one
+// draw, conjugated), so the inverse real transform is exact.
+__global__ void k_spectral_modes(int nx, int ny, int nz, double k0, uint64_t seed,
+                                 double2* __restrict__ vx, double2* __restrict__ vy,
+                                 double2* __restrict__ vz) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int nxc = nx / 2 + 1;
+  const long long total = (long long)nxc * ny * nz;
+  if (t >= total) return;
+  const int kx = (int)(t % nxc);
+  const long long r = t / nxc;
+  int jy = (int)(r % ny), jz = (int)(r / ny);
+  int ky = signed_k(jy, ny), kz = signed_k(jz, nz);
+  const double k2 = (double)kx * kx + (double)ky * ky + (double)kz * kz;
+  if (k2 == 0.0) {
+    vx[t] = vy[t] = vz[t] = make_double2(0.0, 0.0);
+    return;
+  }
+  // Hermitian planes: draw from the canonical member of the pair (k, -k)
+  bool conj = false;
+  if (kx == 0 || 2 * kx == nx) {
+    const int my = (ny - jy) % ny, mz = (nz - jz) % nz;  // index of -k
+    if (my > jy || (my == jy && mz > jz)) {
+      conj = true;
+      jy = my;
+      jz = mz;
+      ky = signed_k(jy, ny);
+      kz = signed_k(jz, nz);
+    }
+  }
+  const long long canon = ((long long)jz * ny + jy) * nxc + kx;
+  double2 a[3] = {gauss2(seed, canon, 0), gauss2(seed, canon, 1), gauss2(seed, canon, 2)};
+  const double kv[3] = {(double)kx, (double)ky, (double)kz};
+  // solenoidal projection a - k (k.a) / k^2, real and imaginary parts
+  const double kr = (kv[0] * a[0].x + kv[1] * a[1].x + kv[2] * a[2].x) / k2;
+  const double ki = (kv[0] * a[0].y + kv[1] * a[1].y + kv[2] * a[2].y) / k2;
+  const double k = sqrt(k2), q = k / k0;
+  const double amp = sqrt(k2 * k2 * exp(-2.0 * q * q) / (4.0 * 3.141592653589793 * k2));
+  double2 out[3];
+  for (int c = 0; c < 3; ++c) {
+    out[c] = make_double2(amp * (a[c].x - kv[c] * kr), amp * (a[c].y - kv[c] * ki));
+    if (conj) out[c].y = -out[c].y;
+  }
+  // self-mirror modes (k = -k on the grid) must be real
+  if ((kx == 0 || 2 * kx == nx) && ((ny - jy) % ny) == jy && ((nz - jz) % nz) == jz)
+    for (int c = 0; c < 3; ++c) out[c].y = 0.0;
+  vx[t] = out[0];
+  vy[t] = out[1];
+  vz[t] = out[2];
+}
+
+__global__ void k_square(const double* __restrict__ a, double* __restrict__ b, long long n) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t < n) b[t] = a[t] * a[t];
+}
+__global__ void k_scale(double* __restrict__ a, long long n, const double* __restrict__ sumsq,
+                        double urms) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t < n) {
+    const double ms = *sumsq / (double)n;
+    a[t] = ms > 0.0 ? a[t] * (urms / sqrt(ms)) : 0.0;
+  }
+}
+
+// Deterministic summary of a state: per block partial sums of mass, x/y/z
+// momentum, a position-weighted population checksum, and (from the macro
+// arrays) the kinetic energy.
+template <typename T>
+__global__ void __launch_bounds__(256) k_summary(const T* __restrict__ f, long long N,
+                                                 const T* __restrict__ ux, const T* __restrict__ uy,
+                                                 const T* __restrict__ uz,
+                                                 double* __restrict__ partial) {
+  using Red = cub::BlockReduce<double, 256>;
+  __shared__ typename Red::TempStorage tmp;
+  double s[6] = {0, 0, 0, 0, 0, 0};
+  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < N;
+       n += (long long)gridDim.x * blockDim.x) {
+    double rho = 0.0, jx = 0.0, jy = 0.0, jz = 0.0, ck = 0.0;
+#pragma unroll
+    for (int q = 0; q < NPOP; ++q) {
+      const double v = (double)f[(long long)q * N + n];
+      rho += v;
+      jx += cix(q) * v;
+      jy += ciy(q) * v;
+      jz += ciz(q) * v;
+      ck += (1.0 + q / 19.0 + (double)(n % 97) / 97.0) * v;
+    }
+    s[0] += rho; s[1] += jx; s[2] += jy; s[3] += jz; s[4] += ck;
+    const double a = (double)ux[n], b = (double)uy[n], c = (double)uz[n];
+    s[5] += 0.5 * (a * a + b * b + c * c);
+  }
+  for (int c = 0; c < 6; ++c) {
+    const double t = Red(tmp).Sum(s[c]);
+    __syncthreads();
+    if (threadIdx.x == 0) partial[6 * blockIdx.x + c] = t;
+  }
+}
+
 }  // namespace
+
+int spectral_field(const Geometry& g, double k0, double urms, uint64_t seed, double* u,
+                   cudaStream_t s) {
+  const long long N = g.N;
+  const long long nc = (long long)(g.nx / 2 + 1) * g.ny * g.nz;
+  double2* spec = nullptr;
+  double* tmp = nullptr;
+  void* cub_tmp = nullptr;
+  size_t cub_bytes = 0;
+  cufftHandle plan = 0;
+  int rc = LBM_OK;
+  cub::DeviceReduce::Sum(nullptr, cub_bytes, tmp, tmp, N);
+  if (cudaMalloc((void**)&spec, 3 * nc * sizeof(double2)) != cudaSuccess ||
+      cudaMalloc((void**)&tmp, (N + 1) * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&cub_tmp, cub_bytes) != cudaSuccess) {
+    rc = LBM_ERR_NOMEM;
+  } else if (cufftPlan3d(&plan, g.nz, g.ny, g.nx, CUFFT_Z2D) != CUFFT_SUCCESS) {
+    rc = LBM_ERR_CUDA;
+    plan = 0;
+  } else {
+    cufftSetStream(plan, s);
+    k_spectral_modes<<<blocks(nc, 256), 256, 0, s>>>(g.nx, g.ny, g.nz, k0, seed, spec,
+                                                      spec + nc, spec + 2 * nc);
+    count_launch();
+    for (int c = 0; c < 3 && !rc; ++c) {
+      if (cufftExecZ2D(plan, spec + c * nc, u + c * N) != CUFFT_SUCCESS) {
+        rc = LBM_ERR_CUDA;
+        break;
+      }
+      // per-component rms -> urms
+      k_square<<<blocks(N, 256), 256, 0, s>>>(u + c * N, tmp, N);
+      count_launch();
+      size_t b = cub_bytes;
+      cub::DeviceReduce::Sum(cub_tmp, b, tmp, tmp + N, N, s);
+      k_scale<<<blocks(N, 256), 256, 0, s>>>(u + c * N, N, tmp + N, urms);
+      count_launch();
+    }
+  }
+  if (cudaStreamSynchronize(s) != cudaSuccess && !rc) rc = LBM_ERR_CUDA;
+  if (plan) cufftDestroy(plan);
+  cudaFree(spec);
+  cudaFree(tmp);
+  cudaFree(cub_tmp);
+  return rc;
+}
+
+template <typename T>
+void launch_summary(const T* f, long long N, const T* ux, const T* uy, const T* uz,
+                    double* partial, int nblocks, cudaStream_t s) {
+  k_summary<T><<<nblocks, 256, 0, s>>>(f, N, ux, uy, uz, partial);
+  count_launch();
+}
 
 // ---------------------------------------------------------------------------
 struct SpectrumWork {
@@ -322,7 +495,9 @@ void launch_slip(const Geometry& g, const ParticleView& pv, const T* ux, const T
   template int spectrum_stats<T>(const Geometry&, double, const T*, const T*, const T*,       \
                                  SpectrumWork**, int, double*, double*, double*, cudaStream_t); \
   template void launch_slip<T>(const Geometry&, const ParticleView&, const T*, const T*,      \
-                               const T*, const int32_t*, double, double, double*, cudaStream_t);
+                               const T*, const int32_t*, double, double, double*, cudaStream_t); \
+  template void launch_summary<T>(const T*, long long, const T*, const T*, const T*, double*,  \
+                                  int, cudaStream_t);
 LBM_STATS_INSTANTIATE(float)
 LBM_STATS_INSTANTIATE(double)
 

@@ -138,6 +138,23 @@ class LBMBox:
         self._ck(self._L.lbm_mass_momentum(self._h, dptr(out)), "mass_momentum")
         return out
 
+    def init_spectral(self, k0: float, u_rms: float, seed: int):
+        """initpop from a seeded divergence-free Gaussian field made on the GPU."""
+        self._ck(self._L.lbm_init_spectral(self._h, float(k0), float(u_rms), int(seed)),
+                 "init_spectral")
+
+    def init_particles(self, npart: int, seed: int = 12345, max_rounds: int = 0):
+        """initpartpos with the ranpp generator, particles at rest."""
+        self._ck(self._L.lbm_init_particles(self._h, int(npart), int(seed), int(max_rounds)),
+                 "init_particles")
+        self.npart = int(npart)
+
+    def summary(self) -> np.ndarray:
+        """[mass, momentum x, y, z, population checksum, kinetic energy]."""
+        out = np.zeros(6)
+        self._ck(self._L.lbm_summary(self._h, dptr(out)), "summary")
+        return out
+
     def statistics(self, nshell: int | None = None) -> dict:
         """statistc's spectrum and moments of the current velocity
         (saveload.f90:1111-1338): ek, dk per shell and the totals."""

@@ -1,0 +1,183 @@
+"""Serving: many solves resident on the GPU, advanced together.
+
+``LBMServer`` wraps the native request loop of the library (lbm_server_*):
+admission by HBM footprint, continuous batching of the resident FP32 solves
+into batched stream + collide launches, per-request latency.  ``poisson_run``
+drives it with a Poisson stream of channel solves (walls normal to y) and
+reports throughput and latency percentiles.
+
+The channel workload: grid X x Y x Z with X, Z uniform in 64..192 and the
+wall-normal Y uniform in 64..128 (multiples of 8), 0..400 spheres of radius 4
+(capped at a 5 % solid fraction), density ratio 1 (the channel's var_inc.f90:29),
+FP32 populations, 200..2000 steps, started from stagnant flow and driven by
+the channel preset's constant force as the reference channel is
+(C/para.f90:20-22).  The collision uses MRTtype 1 (para.f90's rates "for
+stability"): with the channel's default LBGK rates (MRTtype 2) at
+tau = 0.5108 these small channels accelerate to velocities at which the
+flow diverges within ~500 steps, in the CPU oracle as on the GPU.  A request
+whose spheres come to overlap fails with LBM_ERR_OVERLAP, as the reference
+stops (partlib.f90:2634-2646); such failures are counted apart.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import math
+import threading
+import time
+
+import numpy as np
+
+from . import _capi as capi
+from ._capi import LBMError
+
+
+class lbm_request(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+                ("wall_axis", C.c_int32), ("npart", C.c_int32), ("nsteps", C.c_int32),
+                ("precision", C.c_int32), ("mrt_type", C.c_int32),
+                ("rad", C.c_double), ("rhopart", C.c_double), ("k0", C.c_double),
+                ("u_rms", C.c_double), ("seed", C.c_uint64)]
+
+
+class lbm_result(C.Structure):
+    _fields_ = [("id", C.c_int64), ("state", C.c_int32), ("error", C.c_int32),
+                ("steps_done", C.c_int32), ("batched", C.c_int32),
+                ("t_submit", C.c_double), ("t_start", C.c_double), ("t_done", C.c_double),
+                ("summary", C.c_double * 6)]
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
+
+
+def request(nx, ny, nz, nsteps, wall_axis=1, npart=0, rad=4.0, rhopart=1.0, k0=4.0,
+            u_rms=0.03, seed=1, precision=capi.LBM_PREC_F32, mrt_type=0) -> lbm_request:
+    return lbm_request(nx, ny, nz, wall_axis, npart, nsteps, precision, mrt_type, rad, rhopart,
+                       k0, u_rms, seed)
+
+
+class LBMServer:
+    def __init__(self, hbm_budget: int, max_active: int = 64, chunk_steps: int = 50):
+        self._L = capi.lib()
+        h = C.c_void_p()
+        rc = self._L.lbm_server_create(C.c_uint64(int(hbm_budget)), int(max_active),
+                                       int(chunk_steps), C.byref(h))
+        if rc != capi.LBM_OK:
+            raise LBMError(rc, "lbm_server_create")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.lbm_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, req: lbm_request) -> int:
+        i = C.c_int64(0)
+        rc = self._L.lbm_server_submit(self._h, C.byref(req), C.byref(i))
+        if rc != capi.LBM_OK:
+            raise LBMError(rc, "lbm_server_submit")
+        return int(i.value)
+
+    def result(self, rid: int) -> lbm_result:
+        r = lbm_result()
+        rc = self._L.lbm_server_result(self._h, C.c_int64(rid), C.byref(r))
+        if rc != capi.LBM_OK:
+            raise LBMError(rc, "lbm_server_result")
+        return r
+
+    def wait(self, rid: int, timeout: float = 600.0) -> lbm_result:
+        rc = self._L.lbm_server_wait(self._h, C.c_int64(rid), C.c_double(timeout))
+        if rc != capi.LBM_OK:
+            raise LBMError(rc, f"lbm_server_wait({rid})")
+        return self.result(rid)
+
+    def stats(self) -> dict:
+        out = (C.c_double * 10)()
+        self._L.lbm_server_stats(self._h, out)
+        keys = ("submitted", "done", "failed", "resident", "queued", "hbm_bytes", "regroupings",
+                "chunks", "advance_s", "uptime_s")
+        return dict(zip(keys, list(out)))
+
+
+def channel_requests(n: int, seed: int = 4004, max_fraction: float = 0.05,
+                     u_rms: float = 0.0) -> list:
+    """n requests of the channel serving workload (walls normal to y)."""
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(n):
+        X = int(rng.integers(8, 25)) * 8
+        Y = int(rng.integers(8, 17)) * 8
+        Z = int(rng.integers(8, 25)) * 8
+        rad = 4.0
+        cap = int(max_fraction * X * Y * Z / (4.0 / 3.0 * math.pi * rad ** 3))
+        npart = min(int(rng.integers(0, 401)), cap)
+        steps = int(rng.integers(200, 2001))
+        reqs.append(request(X, Y, Z, steps, wall_axis=1, npart=npart, rad=rad, rhopart=1.0,
+                            u_rms=u_rms, seed=10_000 + i, mrt_type=1))
+    return reqs
+
+
+def poisson_run(rate: float = 20.0, duration: float = 60.0, hbm_budget: int = 96 << 30,
+                max_active: int = 96, chunk_steps: int = 50, seed: int = 4004,
+                drain: bool = True) -> dict:
+    """Submit requests at Poisson times for `duration` seconds, then (if
+    `drain`) wait for all of them; report solves/s and latency percentiles."""
+    rng = np.random.default_rng(seed + 1)
+    nmax = int(rate * duration * 2 + 50)
+    reqs = channel_requests(nmax, seed)
+    ids = []
+    with LBMServer(hbm_budget, max_active, chunk_steps) as srv:
+        t0 = time.perf_counter()
+        t_next = 0.0
+        k = 0
+        while True:
+            t_next += rng.exponential(1.0 / rate)
+            if t_next > duration or k >= nmax:
+                break
+            delay = t0 + t_next - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            ids.append((srv.submit(reqs[k]), reqs[k]))
+            k += 1
+        submitted_in = time.perf_counter() - t0
+        done_in_window = srv.stats()["done"]
+        if drain:
+            for rid, _ in ids:
+                srv.wait(rid, timeout=3600.0)
+        wall = time.perf_counter() - t0
+        res = [(srv.result(rid), rq) for rid, rq in ids]
+        st = srv.stats()
+    ok = [(r, q) for r, q in res if r.state == REQ_DONE]
+    errors = {}
+    for r, _ in res:
+        if r.state == REQ_FAILED:
+            errors[int(r.error)] = errors.get(int(r.error), 0) + 1
+    lat = np.array([r.t_done - r.t_submit for r, _ in ok])
+    wait = np.array([r.t_start - r.t_submit for r, _ in ok])
+    lups = sum(float(q.nx) * q.ny * q.nz * q.nsteps for _, q in ok)
+    return {
+        "arrival_rate_per_s": rate, "window_s": duration, "submitted": len(ids),
+        "done": len(ok), "failed": len(res) - len(ok), "failures_by_code": errors,
+        "done_within_window": int(done_in_window),
+        "solves_per_s": len(ok) / wall if wall > 0 else 0.0,
+        "solves_per_s_window": done_in_window / submitted_in if submitted_in > 0 else 0.0,
+        "latency_p50_s": float(np.percentile(lat, 50)) if lat.size else None,
+        "latency_p99_s": float(np.percentile(lat, 99)) if lat.size else None,
+        "queue_wait_p50_s": float(np.percentile(wait, 50)) if wait.size else None,
+        "queue_wait_p99_s": float(np.percentile(wait, 99)) if wait.size else None,
+        "mlups": lups / wall / 1e6 if wall > 0 else 0.0,
+        "batched_fraction": float(np.mean([r.batched for r, _ in ok])) if ok else 0.0,
+        "wall_s": wall, "server": st,
+    }

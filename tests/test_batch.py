@@ -148,3 +148,13 @@ def test_batch_forcing_state_follows_the_steps(require_gpu):
     r8.step(8)
     s8 = r8.get_forcing_state()
     assert s_in[0] == s8[0] and s_in[1] == s8[1] and np.array_equal(s_in[2], s8[2])
+
+
+def test_batch_led_by_a_box_without_particles(require_gpu):
+    """Boxes with and without spheres share the flag-buffer parity."""
+    specs = [SPECS[2], SPECS[0], SPECS[1]]       # first box has no particles
+    together = run_batch(specs, 9, graph=True)
+    for spec, (f, p) in zip(specs, together):
+        alone = run_batch([spec], 9, graph=False)[0]
+        assert np.array_equal(alone[0], f)
+        assert np.array_equal(alone[1]["fHIp"], p["fHIp"])
