@@ -281,19 +281,6 @@ def workload(name: str):
                       name=name, ny=ny, nz=nz)
 
 
-def dist_setup(args):
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    pg = None
-    if world > 1:
-        import torch.distributed as dist
-        backend = "nccl" if args.impl == "ours" else "gloo"
-        dist.init_process_group(backend)
-        pg = dist
-    return world, rank, local, pg
-
-
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -322,7 +309,9 @@ def main():
     if args.warmup < 3:
         args.warmup = 3
 
-    world, rank, local, dist = dist_setup(args)
+    from multiphase_flow_codes_gb300.replicas import Replicas
+    rep = Replicas("nccl" if args.impl == "ours" else "gloo")
+    world, rank, local = rep.world, rep.rank, rep.local
     wl = workload(args.workload)
     c = wl.cfg
     N = c.nx * c.ny * c.nz
@@ -364,20 +353,16 @@ def main():
     u, y = make_inputs(wl)
 
     sampler = ClockSampler(local)
-    if dist:
-        dist.barrier()
+    rep.barrier()
     torch.cuda.synchronize()
     sampler.start()
     fixed = tuple(int(v) for v in args.variant.split(",")) if args.variant else None
     ms, launches, phases, f64, p64, variant = run_device(wl, u, y, args.steps, args.warmup, local,
                                                          want_f=not args.no_fp32, variant=fixed)
     clocks = sampler.stop()
-    t_ms = ms
-    if dist:
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_ms = float(t.item())
-    value = N * args.steps * world / (t_ms / 1e3) / 1e6
+    rate, t_s = rep.rate(N * args.steps, ms / 1e3)
+    t_ms = t_s * 1e3
+    value = rate / 1e6
 
     peaks = measured_peaks()
     hbm = float(peaks.get("hbm_gbs", HBM_FALLBACK))
@@ -471,12 +456,8 @@ def main():
         f0_fortran = np.asfortranarray(np.transpose(f0, (0, 3, 2, 1)))
         del f0
         e_ms, h2d, d2h = run_e2e(wl, f0_fortran, y, args.steps, local, variant)
-        e_t = e_ms
-        if dist:
-            t = torch.tensor([e_ms], device=f"cuda:{local}")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e_t = float(t.item())
-        line["e2e"] = {"value": N * args.steps * world / (e_t / 1e3) / 1e6, "unit": "MLUPS",
+        e_rate, _ = rep.rate(N * args.steps, e_ms / 1e3)
+        line["e2e"] = {"value": e_rate / 1e6, "unit": "MLUPS",
                        "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                        "how": "C ABI: lbm_upload_f (Fortran layout, pinned host) + particles, "
                               f"{args.steps} x (lbm_step + particle read-back), lbm_download_f"}
@@ -488,12 +469,10 @@ def main():
                                 "kind": "port",
                                 "sample": f"{args.cpu_steps} full steps of {wl.name} on the CPU "
                                           "restatement (OpenMP)"}
-    if dist:
-        dist.barrier()
-    if rank == 0:
+    rep.barrier()
+    if rep.leader:
         print(json.dumps(line), flush=True)
-    if dist:
-        dist.destroy_process_group()
+    rep.close()
 
 
 if __name__ == "__main__":
