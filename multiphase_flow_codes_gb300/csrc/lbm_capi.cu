@@ -1538,6 +1538,14 @@ struct lbm_batch {
   cudaGraphExec_t graph = nullptr;
   int graph_key[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
   std::vector<cudaEvent_t> ev_side;
+  // particle step and FORCING of all boxes, one launch per kernel
+  BoxParticles* d_parts[2] = {nullptr, nullptr};  // per buffer parity
+  BoxForcing* d_forcing = nullptr;
+  int max_npart = 0, max_nz = 0;
+  long long max_reset = 0, max_rows = 0;
+  bool stochastic = false;
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_side_all = nullptr;
   int64_t graph_kernels = 0;
   std::string err;
 };
@@ -1595,16 +1603,30 @@ std::string batch_step_eager(lbm_batch* b) {
     return "";
   };
   std::string err;
-  if (!(err = chk(cudaEventRecord(b->ev_fork, b->main), "fork", 0)).empty()) return err;
+  // this step's FORCING: run during the previous step (joined since), or
+  // constant, or (first step of a batch) now on each box's stream
+  bool any_pending = false;
+  std::vector<char> pending(b->ctx.size(), 0);
   for (size_t i = 0; i < b->ctx.size(); ++i) {
     lbm_ctx* c = b->ctx[i];
-    if (!(err = chk(cudaStreamWaitEvent(c->stream, b->ev_fork, 0), "box wait", i)).empty()) return err;
-    if (c->batch_ready) {  // ran during the previous step, joined since
+    if (c->batch_ready) {
       c->latest = {FM_TABLE, c->batch_slot};
       c->batch_ready = false;
+    } else if (c->cfg.forcing == LBM_FORCING_STOCHASTIC) {
+      pending[i] = 1;
+      any_pending = true;
     } else {
-      do_forcing(c);
+      do_forcing(c);  // constant or none: no launch
     }
+  }
+  if (any_pending &&
+      !(err = chk(cudaEventRecord(b->ev_fork, b->main), "fork", 0)).empty())
+    return err;
+  for (size_t i = 0; i < b->ctx.size() && any_pending; ++i) {
+    lbm_ctx* c = b->ctx[i];
+    if (!pending[i]) continue;
+    if (!(err = chk(cudaStreamWaitEvent(c->stream, b->ev_fork, 0), "box wait", i)).empty()) return err;
+    do_forcing(c);
     if (!(err = chk(cudaGetLastError(), "forcing", i)).empty()) return err;
     if (!(err = chk(cudaEventRecord(b->ev_join[i], c->stream), "join record", i)).empty()) return err;
     if (!(err = chk(cudaStreamWaitEvent(b->main, b->ev_join[i], 0), "join wait", i)).empty()) return err;
@@ -1616,29 +1638,34 @@ std::string batch_step_eager(lbm_batch* b) {
                      b->main);
   if (!(err = chk(cudaGetLastError(), "batch kernel", 0)).empty()) return err;
   if (!(err = chk(cudaEventRecord(b->ev_fork, b->main), "fork 2", 0)).empty()) return err;
-  for (size_t i = 0; i < b->ctx.size(); ++i) {
-    lbm_ctx* c = b->ctx[i];
-    if (!(err = chk(cudaStreamWaitEvent(c->stream, b->ev_fork, 0), "box wait 2", i)).empty()) return err;
-    if (c->cfg.forcing == LBM_FORCING_STOCHASTIC) {
-      // the next step's FORCING on the side stream, beside the particles;
-      // the state before it is kept so that leaving the batch can undo it
-      int slot = 0;
-      for (int q = 0; q < 3; ++q)
-        if (q != c->latest.slot) { slot = q; break; }
-      if (!(err = chk(cudaStreamWaitEvent(c->side, b->ev_fork, 0), "side wait", i)).empty()) return err;
-      cudaMemcpyAsync(c->d_forcing_backup, c->d_forcing, sizeof(ForcingDev),
-                      cudaMemcpyDeviceToDevice, c->side);
-      launch_forcing_into(c, slot, c->side);
-      if (!(err = chk(cudaGetLastError(), "next forcing", i)).empty()) return err;
-      if (!(err = chk(cudaEventRecord(b->ev_side[i], c->side), "side record", i)).empty()) return err;
-      if (!(err = chk(cudaStreamWaitEvent(b->main, b->ev_side[i], 0), "side join", i)).empty()) return err;
+  const int par = c0->cur;  // buffer parity of this step (every box: cur == fcur)
+  if (b->stochastic) {
+    // the next step's FORCING of every box, one launch per kernel, on the
+    // batch's side stream beside the particle step
+    int slot = 0;
+    for (int q = 0; q < 3; ++q)
+      if (q != c0->latest.slot) { slot = q; break; }
+    if (!(err = chk(cudaStreamWaitEvent(b->side, b->ev_fork, 0), "side wait", 0)).empty()) return err;
+    launch_forcing_multi(b->d_forcing, (int)b->ctx.size(), b->max_nz, b->max_rows, slot, b->side);
+    if (!(err = chk(cudaGetLastError(), "forcing", 0)).empty()) return err;
+    if (!(err = chk(cudaEventRecord(b->ev_side_all, b->side), "side record", 0)).empty()) return err;
+    for (lbm_ctx* c : b->ctx) {
       c->batch_ready = true;
       c->batch_slot = slot;
     }
-    step_post_t<float>(c);
-    if (!(err = chk(cudaGetLastError(), "particles", i)).empty()) return err;
-    if (!(err = chk(cudaEventRecord(b->ev_join[i], c->stream), "join record 2", i)).empty()) return err;
-    if (!(err = chk(cudaStreamWaitEvent(b->main, b->ev_join[i], 0), "join wait 2", i)).empty()) return err;
+  }
+  launch_particle_step_multi(b->d_parts[par], (int)b->ctx.size(), b->max_npart, b->max_reset,
+                             b->main);
+  if (!(err = chk(cudaGetLastError(), "particles", 0)).empty()) return err;
+  if (b->stochastic &&
+      !(err = chk(cudaStreamWaitEvent(b->main, b->ev_side_all, 0), "side join", 0)).empty())
+    return err;
+  for (lbm_ctx* c : b->ctx) {  // host side of the step (step_post_t without launches)
+    c->fcur = 1 - c->fcur;
+    c->cur = 1 - c->cur;
+    c->fmacro = c->latest;
+    c->macro_pending = true;
+    c->macro_derived = true;
   }
   return "";
 }
@@ -1692,13 +1719,54 @@ int lbm_batch_create(lbm_ctx** ctxs, int n, lbm_batch** out) {
     b->nodes += c->g.N;
   }
   b->ntasks = (int)tasks.size();
+  // per-box views of the particle step (both buffer parities) and FORCING
+  std::vector<BoxParticles> parts(2 * (size_t)n);
+  std::vector<BoxForcing> forc(n);
+  b->stochastic = c0->cfg.forcing == LBM_FORCING_STOCHASTIC;
+  for (int i = 0; i < n; ++i) {
+    lbm_ctx* c = b->ctx[i];
+    for (int par = 0; par < 2; ++par) {
+      BoxParticles& x = parts[(size_t)par * n + i];
+      x.g = c->g;
+      x.pv = pview(c);
+      if (!c->particles_on) x.pv.npart = 0;
+      x.pp = c->pp;
+      x.ms = mstate(c);
+      x.ls = c->links;
+      x.fl = c->fill;
+      x.f = static_cast<float*>(c->f[1 - par]);
+      x.flags_cur = c->flags[par];
+      x.flags_next = c->flags[1 - par];
+      x.st = c->status;
+    }
+    if (c->particles_on) {
+      b->max_npart = std::max(b->max_npart, c->npart);
+      b->max_reset = std::max(b->max_reset,
+                              (long long)c->g.N + (long long)c->g.ny * c->g.nz * c->g.sw);
+    }
+    BoxForcing& fb = forc[i];
+    fb.g = c->g;
+    fb.st = c->d_forcing;
+    fb.backup = c->d_forcing_backup;
+    fb.var = c->var; fb.tf = c->tf; fb.pi2 = c->pi2;
+    fb.kxr6 = c->d_kxr6; fb.kyr5 = c->d_kyr5; fb.kzr5 = c->d_kzr5;
+    fb.ytw = c->ytw; fb.ztw = c->ztw; fb.ztab = c->ztab;
+    for (int q = 0; q < 3; ++q) fb.rowtab[q] = static_cast<float*>(c->rowtab[q]);
+    b->max_nz = std::max(b->max_nz, c->g.nz);
+    b->max_rows = std::max(b->max_rows, (long long)c->g.ny * c->g.nz);
+  }
   int rc = 0;
   if (cudaStreamCreateWithFlags(&b->main, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaMalloc((void**)&b->d_boxes, boxes.size() * sizeof(BatchBox)) != cudaSuccess ||
       cudaMalloc((void**)&b->d_tasks, tasks.size() * sizeof(BatchTask)) != cudaSuccess ||
-      cudaMalloc((void**)&b->status, sizeof(DevStatus)) != cudaSuccess)
+      cudaMalloc((void**)&b->status, sizeof(DevStatus)) != cudaSuccess ||
+      cudaMalloc((void**)&b->d_parts[0], parts.size() * sizeof(BoxParticles)) != cudaSuccess ||
+      cudaMalloc((void**)&b->d_forcing, forc.size() * sizeof(BoxForcing)) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->ev_side_all, cudaEventDisableTiming) != cudaSuccess)
     rc = LBM_ERR_CUDA;
+  if (!rc) b->d_parts[1] = b->d_parts[0] + n;
   b->own_main = true;
   b->ev_join.resize(n, nullptr);
   b->ev_side.resize(n, nullptr);
@@ -1710,6 +1778,10 @@ int lbm_batch_create(lbm_ctx** ctxs, int n, lbm_batch** out) {
     cudaMemcpyAsync(b->d_boxes, boxes.data(), boxes.size() * sizeof(BatchBox),
                     cudaMemcpyHostToDevice, b->main);
     cudaMemcpyAsync(b->d_tasks, tasks.data(), tasks.size() * sizeof(BatchTask),
+                    cudaMemcpyHostToDevice, b->main);
+    cudaMemcpyAsync(b->d_parts[0], parts.data(), parts.size() * sizeof(BoxParticles),
+                    cudaMemcpyHostToDevice, b->main);
+    cudaMemcpyAsync(b->d_forcing, forc.data(), forc.size() * sizeof(BoxForcing),
                     cudaMemcpyHostToDevice, b->main);
     cudaMemsetAsync(b->status, 0, sizeof(DevStatus), b->main);
     if (!plan_batch(b->channel, 4, 2, 0, b->ntasks, &b->plan) &&
@@ -1729,6 +1801,7 @@ int lbm_batch_create(lbm_ctx** ctxs, int n, lbm_batch** out) {
 int lbm_batch_destroy(lbm_batch* b) {
   if (!b) return LBM_OK;
   if (b->main) cudaStreamSynchronize(b->main);
+  if (b->side) cudaStreamSynchronize(b->side);
   for (lbm_ctx* c : b->ctx) {
     if (c->side) cudaStreamSynchronize(c->side);
     if (c->stream) cudaStreamSynchronize(c->stream);
@@ -1748,6 +1821,10 @@ int lbm_batch_destroy(lbm_batch* b) {
   cudaFree(b->d_boxes);
   cudaFree(b->d_tasks);
   cudaFree(b->status);
+  cudaFree(b->d_parts[0]);
+  cudaFree(b->d_forcing);
+  if (b->ev_side_all) cudaEventDestroy(b->ev_side_all);
+  if (b->side) cudaStreamDestroy(b->side);
   if (b->own_main && b->main) cudaStreamDestroy(b->main);
   delete b;
   return LBM_OK;

@@ -433,9 +433,9 @@ __global__ void k_mass_momentum(Geometry g, const T* __restrict__ f, double* par
 // exp(+2 pi i kz z / nz); stage 2 (rowtab): B(c, kx, z, y) = sum_jy A
 // exp(+2 pi i ky y / ny).  Together with the per-x twiddles they evaluate
 // the inverse transform of gaussian.f90:557-601 at any node.
-__global__ void k_force_ztab(Geometry g, const ForcingDev* st, const double* __restrict__ ztw,
+__device__ __forceinline__ void k_force_ztab_body(int bx, int gx, Geometry g, const ForcingDev* st, const double* __restrict__ ztw,
                              double* ztab) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;  // over (c, kx, jy, z)
+  int t = bx * blockDim.x + threadIdx.x;  // over (c, kx, jy, z)
   int total = 3 * 3 * 5 * g.nz;
   if (t >= total) return;
   int z = t % g.nz;
@@ -455,14 +455,18 @@ __global__ void k_force_ztab(Geometry g, const ForcingDev* st, const double* __r
   ztab[2 * t] = sr;
   ztab[2 * t + 1] = si;
 }
+__global__ void k_force_ztab(Geometry g, const ForcingDev* st, const double* __restrict__ ztw,
+                             double* ztab) {
+  k_force_ztab_body(blockIdx.x, gridDim.x, g, st, ztw, ztab);
+}
 
 // Row coefficients of the force series (kRowCoef layout) from the (kx, z)
 // table: one thread per (row, component, kx).  The kx = 1, 2 terms of the
 // real inverse transform enter twice (kx and -kx), hence the factor 2.
 template <typename T>
-__global__ void k_force_rowtab(Geometry g, const double* __restrict__ ztab,
+__device__ __forceinline__ void k_force_rowtab_body(int bx, int gx, Geometry g, const double* __restrict__ ztab,
                                const double* __restrict__ ytw, T* __restrict__ rowtab) {
-  long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;  // over (c,kx,z,y)
+  long long t = bx * (long long)blockDim.x + threadIdx.x;  // over (c,kx,z,y)
   long long total = 9LL * g.nz * g.ny;
   if (t >= total) return;
   int y = (int)(t % g.ny);
@@ -487,6 +491,11 @@ __global__ void k_force_rowtab(Geometry g, const double* __restrict__ ztab,
     k[2 * kx - 1] = T(2.0) * sr;
     k[2 * kx] = T(-2.0) * si;
   }
+}
+template <typename T>
+__global__ void k_force_rowtab(Geometry g, const double* __restrict__ ztab,
+                               const double* __restrict__ ytw, T* __restrict__ rowtab) {
+  k_force_rowtab_body<T>(blockIdx.x, gridDim.x, g, ztab, ytw, rowtab);
 }
 
 inline dim3 row_grid(const Geometry& g, int bx) { return dim3((g.nx + bx - 1) / bx, g.ny, g.nz); }
@@ -567,6 +576,33 @@ template <typename T>
 void launch_mass_momentum(const Geometry& g, const T* f, double* partial, int nblocks,
                           cudaStream_t s) {
   { k_mass_momentum<T><<<nblocks, 256, 0, s>>>(g, f, partial); count_launch(); }
+}
+
+namespace {
+__global__ void k_force_ztab_multi(const BoxForcing* boxes) {
+  const BoxForcing& B = boxes[blockIdx.y];
+  const int nblk = (45 * B.g.nz + 127) / 128;
+  if ((int)blockIdx.x >= nblk) return;
+  k_force_ztab_body(blockIdx.x, nblk, B.g, B.st, B.ztw, B.ztab);
+}
+__global__ void k_force_rowtab_multi(const BoxForcing* boxes, int slot) {
+  const BoxForcing& B = boxes[blockIdx.y];
+  const long long nblk = (9LL * B.g.nz * B.g.ny + 255) / 256;
+  if ((long long)blockIdx.x >= nblk) return;
+  k_force_rowtab_body<float>(blockIdx.x, (int)nblk, B.g, B.ztab, B.ytw, B.rowtab[slot]);
+}
+}  // namespace
+
+void launch_forcing_update_multi(const BoxForcing* boxes, int nb, cudaStream_t s);
+
+void launch_forcing_multi(const BoxForcing* boxes, int nb, int max_nz, long long max_rows,
+                          int slot, cudaStream_t s) {
+  if (nb <= 0) return;
+  launch_forcing_update_multi(boxes, nb, s);
+  k_force_ztab_multi<<<dim3((45 * max_nz + 127) / 128, nb), 128, 0, s>>>(boxes);
+  count_launch();
+  k_force_rowtab_multi<<<dim3((unsigned)((9 * max_rows + 255) / 256), nb), 256, 0, s>>>(boxes, slot);
+  count_launch();
 }
 
 template <typename T>

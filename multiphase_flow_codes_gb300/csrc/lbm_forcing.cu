@@ -45,7 +45,7 @@ __device__ __forceinline__ int m655(int i, int j, int k) { return (i - 1) + 6 * 
 // One block: thread 0 draws the 450 uniform numbers in the reference's
 // order (mc, k, j, i = 1,3,5; cont1 then rph), then the magnitudes,
 // phases, Ornstein-Uhlenbeck update and projection run one mode per thread.
-__global__ void __launch_bounds__(256) k_forcing_update(ForcingDev* st, double var, double tf,
+__device__ __forceinline__ void k_forcing_update_body(int bx, int gx, ForcingDev* st, double var, double tf,
                                                         double pi2, const double* kxr6,
                                                         const double* kyr5, const double* kzr5) {
   __shared__ double u[450];
@@ -146,8 +146,32 @@ __global__ void __launch_bounds__(256) k_forcing_update(ForcingDev* st, double v
     }
   }
 }
+__global__ void __launch_bounds__(256) k_forcing_update(ForcingDev* st, double var, double tf,
+                                                        double pi2, const double* kxr6,
+                                                        const double* kyr5, const double* kzr5) {
+  k_forcing_update_body(blockIdx.x, gridDim.x, st, var, tf, pi2, kxr6, kyr5, kzr5);
+}
 
 }  // namespace
+
+namespace {
+// one block per box: keep the state, then the update
+__global__ void __launch_bounds__(256) k_forcing_update_multi(const BoxForcing* boxes) {
+  const BoxForcing& B = boxes[blockIdx.y];
+  const int n = (int)(sizeof(ForcingDev) / sizeof(int32_t));
+  const int32_t* src = reinterpret_cast<const int32_t*>(B.st);
+  int32_t* dst = reinterpret_cast<int32_t*>(B.backup);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+  __syncthreads();
+  k_forcing_update_body(0, 1, B.st, B.var, B.tf, B.pi2, B.kxr6, B.kyr5, B.kzr5);
+}
+}  // namespace
+
+void launch_forcing_update_multi(const BoxForcing* boxes, int nb, cudaStream_t s) {
+  if (nb <= 0) return;
+  k_forcing_update_multi<<<dim3(1, nb), 256, 0, s>>>(boxes);
+  count_launch();
+}
 
 void launch_forcing_update(ForcingDev* st, double var, double tf, double pi2,
                            const double* kxr6, const double* kyr5, const double* kzr5,

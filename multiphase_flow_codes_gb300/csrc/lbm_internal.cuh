@@ -293,6 +293,40 @@ struct FillList {
   int32_t* count;
   int cap;
 };
+// ---- particle step of many boxes per launch (lbm_batch) ---------------
+// Everything one box's particle subroutines need for one buffer parity; the
+// multi-box kernels take an array of these, blockIdx.y selecting the box.
+struct BoxParticles {
+  Geometry g;
+  ParticleView pv;
+  PartParams pp;
+  MoveState ms;
+  LinkSlab ls;
+  FillList fl;
+  float* f;               // populations after this step's stream + collide (pushed)
+  int32_t* flags_cur;     // flags of this step
+  int32_t* flags_next;    // flags the step builds
+  DevStatus* st;
+};
+// one launch per kernel of the particle step (bounce-back through refill)
+// for nb boxes of the array
+void launch_particle_step_multi(const BoxParticles* boxes, int nb, int max_npart,
+                                long long max_reset, cudaStream_t s);
+// FORCING of many boxes into table slot `slot`, keeping each box's state
+// before the update in `backup`
+struct BoxForcing {
+  Geometry g;
+  ForcingDev* st;
+  ForcingDev* backup;
+  double var, tf, pi2;
+  const double* kxr6; const double* kyr5; const double* kzr5;
+  const double* ytw; const double* ztw;
+  double* ztab;
+  float* rowtab[3];
+};
+void launch_forcing_multi(const BoxForcing* boxes, int nb, int max_nz, long long max_rows,
+                          int slot, cudaStream_t s);
+
 template <typename T>
 void launch_filling(const Geometry& g, const ParticleView& pv, const PartParams& pp,
                     const double* ypglbp, const double* wpp, const double* omgpp,

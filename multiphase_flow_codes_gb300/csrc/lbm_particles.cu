@@ -162,8 +162,8 @@ constexpr float kDecide = 4e-3f;
 // from the second sweep on unless the centre lies within an ulp of
 // n/2 - 1/2, which sweep_ok reports.  FP64 and serial by nature; run for all
 // particles at once rather than inside each link block.
-__global__ void k_link_sweeps(Geometry g, ParticleView pv, LinkSlab ls) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void k_link_sweeps_body(int bx, int gx, Geometry g, ParticleView pv, LinkSlab ls) {
+  const int t = bx * blockDim.x + threadIdx.x;
   if (t >= 3 * pv.npart) return;
   const int p = t / 3, axis = t - 3 * p;
   SweepEv* out = reinterpret_cast<SweepEv*>(static_cast<char*>(ls.sweeps) + (size_t)p * kSweepBytes);
@@ -193,8 +193,11 @@ __global__ void k_link_sweeps(Geometry g, ParticleView pv, LinkSlab ls) {
   }
   ls.sweep_ok[3 * p + axis] = ok;
 }
+__global__ void k_link_sweeps(Geometry g, ParticleView pv, LinkSlab ls) {
+  k_link_sweeps_body(blockIdx.x, gridDim.x, g, pv, ls);
+}
 
-__global__ void __launch_bounds__(PB) k_links(Geometry g, ParticleView pv, int32_t* isnodes,
+__device__ __forceinline__ void k_links_body(int bx, int gx, Geometry g, ParticleView pv, int32_t* isnodes,
                                               LinkSlab ls, DevStatus* st, int alpha_fp32) {
   using Scan = cub::BlockScan<int, PB>;
   __shared__ typename Scan::TempStorage scan_tmp;
@@ -213,7 +216,7 @@ __global__ void __launch_bounds__(PB) k_links(Geometry g, ParticleView pv, int32
   __shared__ int near_rc[MAXNEAR];  // fluid nodes within reach: row << 8 | candidate
   __shared__ int nnear;
 
-  const int p = blockIdx.x;
+  const int p = bx;
   if (p >= pv.npart) return;
   const double rad = pv.rad;
   const double radp2 = rad * 1.0 + 2.0;
@@ -527,6 +530,10 @@ __global__ void __launch_bounds__(PB) k_links(Geometry g, ParticleView pv, int32
     if (!fixed_ok) raise_error(st, LBM_ERR_STATE, p);
   }
 }
+__global__ void __launch_bounds__(PB) k_links(Geometry g, ParticleView pv, int32_t* isnodes,
+                                              LinkSlab ls, DevStatus* st, int alpha_fp32) {
+  k_links_body(blockIdx.x, gridDim.x, g, pv, isnodes, ls, st, alpha_fp32);
+}
 
 // running sum: plain FP64, or FP32 with Kahan compensation (FP32 path)
 template <typename T>
@@ -567,12 +574,12 @@ __device__ __forceinline__ T read_post(const Geometry& g, const T* f, int pushed
 // beads_collision for one particle per block: every link computes the
 // bounced population f9 (stored per link) and its momentum exchange.
 template <typename T>
-__global__ void __launch_bounds__(PB) k_bounce(Geometry g, ParticleView pv, const T* f, int pushed,
+__device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, ParticleView pv, const T* f, int pushed,
                                                const int32_t* __restrict__ isnodes, LinkSlab ls,
                                                double* fHIp, double* torqp) {
   using Red = cub::BlockReduce<double, PB>;
   __shared__ typename Red::TempStorage red_tmp;
-  const int p = blockIdx.x;
+  const int p = bx;
   if (p >= pv.npart) return;
   const int cnt = ls.count[p];
   const int32_t* code = ls.code + (long long)p * ls.cap;
@@ -717,14 +724,20 @@ __global__ void __launch_bounds__(PB) k_bounce(Geometry g, ParticleView pv, cons
     }
   }
 }
+template <typename T>
+__global__ void __launch_bounds__(PB) k_bounce(Geometry g, ParticleView pv, const T* f, int pushed,
+                                               const int32_t* __restrict__ isnodes, LinkSlab ls,
+                                               double* fHIp, double* torqp) {
+  k_bounce_body<T>(blockIdx.x, gridDim.x, g, pv, f, pushed, isnodes, ls, fHIp, torqp);
+}
 
 // the bounce-back stores of beads_collision: f(ipp, x + c) = f9
 // (B/partlib.f90:1605-1621).  In the pushed layout that pre-streaming slot
 // already sits at its streaming target, the fluid node x itself.
 template <typename T>
-__global__ void __launch_bounds__(PB) k_bounce_store(Geometry g, ParticleView pv, T* f, int pushed,
+__device__ __forceinline__ void k_bounce_store_body(int bx, int gx, Geometry g, ParticleView pv, T* f, int pushed,
                                                      LinkSlab ls) {
-  const int p = blockIdx.x;
+  const int p = bx;
   if (p >= pv.npart) return;
   const int cnt = ls.count[p];
   const int32_t* code = ls.code + (long long)p * ls.cap;
@@ -750,6 +763,11 @@ __global__ void __launch_bounds__(PB) k_bounce_store(Geometry g, ParticleView pv
     }
   }
 }
+template <typename T>
+__global__ void __launch_bounds__(PB) k_bounce_store(Geometry g, ParticleView pv, T* f, int pushed,
+                                                     LinkSlab ls) {
+  k_bounce_store_body<T>(blockIdx.x, gridDim.x, g, pv, f, pushed, ls);
+}
 
 // beads_lubforce, one warp per particle.  Contributions to particle p are
 // accumulated in ascending partner id, the order in which the reference's
@@ -768,8 +786,8 @@ __device__ __forceinline__ bool near_pair(const Geometry& g, const double* y, in
   return dx <= lim && dy <= lim && dz <= lim && dx * dx + dy * dy + dz * dz <= lim * lim;
 }
 
-__global__ void k_lubforce(Geometry g, int npart, PartParams pp, MoveState ms) {
-  const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+__device__ __forceinline__ void k_lubforce_body(int bx, int gx, Geometry g, int npart, PartParams pp, MoveState ms) {
+  const int p = (bx * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (p >= npart) return;
   const bool channel = g.channel != 0;
@@ -835,11 +853,14 @@ __global__ void k_lubforce(Geometry g, int npart, PartParams pp, MoveState ms) {
   ms.flubp[3 * p + 1] = acc[1];
   ms.flubp[3 * p + 2] = acc[2];
 }
+__global__ void k_lubforce(Geometry g, int npart, PartParams pp, MoveState ms) {
+  k_lubforce_body(blockIdx.x, gridDim.x, g, npart, pp, ms);
+}
 
 // beads_move, B/partlib.f90:2305-2370, one thread per particle.  Also saves
 // the pre-move centre (ypglbp, used by beads_filling).
-__global__ void k_move(int npart, PartParams pp, MoveState ms) {
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void k_move_body(int bx, int gx, int npart, PartParams pp, MoveState ms) {
+  int p = bx * blockDim.x + threadIdx.x;
   if (p >= npart) return;
   const bool first = *ms.first_move != 0;
   const double dt = 1.0;
@@ -881,12 +902,15 @@ __global__ void k_move(int npart, PartParams pp, MoveState ms) {
     ms.torqpp[3 * p + c] = ms.torqp[3 * p + c];
   }
 }
+__global__ void k_move(int npart, PartParams pp, MoveState ms) {
+  k_move_body(blockIdx.x, gridDim.x, npart, pp, ms);
+}
 
 __global__ void k_clear_first(int* first_move) { *first_move = 0; }
 
 // beads_redistribute's periodic wrap, B/partlib.f90:2600-2613
-__global__ void k_wrap(Geometry g, int npart, MoveState ms) {
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void k_wrap_body(int bx, int gx, Geometry g, int npart, MoveState ms) {
+  int p = bx * blockDim.x + threadIdx.x;
   if (p >= npart) return;
   double* y = ms.ypglb + 3 * p;
   double xc = y[0], yc = y[1], zc = y[2];
@@ -899,12 +923,15 @@ __global__ void k_wrap(Geometry g, int npart, MoveState ms) {
   if (zc >= (double)g.nz) y[2] = y[2] - (double)g.nz;
   if (zc < 0.0) y[2] = y[2] + (double)g.nz;
 }
+__global__ void k_wrap(Geometry g, int npart, MoveState ms) {
+  k_wrap_body(blockIdx.x, gridDim.x, g, npart, ms);
+}
 
 // ovlpchk after a move (hgap = dist - 2 rad < 0 aborts the reference,
 // B/partlib.f90:2630-2646); here it raises LBM_ERR_OVERLAP.  One warp per
 // particle, partners with a larger id.
-__global__ void k_overlap(Geometry g, int npart, PartParams pp, MoveState ms, DevStatus* st) {
-  const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+__device__ __forceinline__ void k_overlap_body(int bx, int gx, Geometry g, int npart, PartParams pp, MoveState ms, DevStatus* st) {
+  const int p = (bx * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (p >= npart) return;
   const bool channel = g.channel != 0;
@@ -922,6 +949,9 @@ __global__ void k_overlap(Geometry g, int npart, PartParams pp, MoveState ms, De
     if (hgap < 0.0) raise_error(st, LBM_ERR_OVERLAP, p);
   }
 }
+__global__ void k_overlap(Geometry g, int npart, PartParams pp, MoveState ms, DevStatus* st) {
+  k_overlap_body(blockIdx.x, gridDim.x, g, npart, pp, ms, st);
+}
 
 // beads_filling (B/partlib.f90:2846-3094), in two kernels.
 // k_fill_detect: one block per particle scans the particle's previous
@@ -930,12 +960,12 @@ __global__ void k_overlap(Geometry g, int npart, PartParams pp, MoveState ms, De
 // k_fill_events: one warp per event refills the node.  A refill reads only
 // nodes that are fluid in both steps and writes only its own node, so the
 // events are independent and their order does not matter.
-__global__ void __launch_bounds__(PB) k_fill_detect(Geometry g, ParticleView pv, PartParams pp,
+__device__ __forceinline__ void k_fill_detect_body(int bx, int gx, Geometry g, ParticleView pv, PartParams pp,
                                                     const double* __restrict__ ypglbp,
                                                     const int32_t* __restrict__ isnodes,
                                                     const int32_t* __restrict__ isnodes0,
                                                     FillList fl, DevStatus* st) {
-  const int id = blockIdx.x;
+  const int id = bx;
   if (id >= pv.npart) return;
   const bool channel = g.channel != 0;
   const double cx0 = ypglbp[3 * id], cy0 = ypglbp[3 * id + 1], cz0 = ypglbp[3 * id + 2];
@@ -970,6 +1000,13 @@ __global__ void __launch_bounds__(PB) k_fill_detect(Geometry g, ParticleView pv,
     }
   }
 }
+__global__ void __launch_bounds__(PB) k_fill_detect(Geometry g, ParticleView pv, PartParams pp,
+                                                    const double* __restrict__ ypglbp,
+                                                    const int32_t* __restrict__ isnodes,
+                                                    const int32_t* __restrict__ isnodes0,
+                                                    FillList fl, DevStatus* st) {
+  k_fill_detect_body(blockIdx.x, gridDim.x, g, pv, pp, ypglbp, isnodes, isnodes0, fl, st);
+}
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -998,7 +1035,7 @@ __device__ __forceinline__ R feq_q(int q, R u9, R v9, R w9, R rho9) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(128) k_fill_events(Geometry g, ParticleView pv, PartParams pp,
+__device__ __forceinline__ void k_fill_events_body(int bx, int gx, Geometry g, ParticleView pv, PartParams pp,
                                                      const double* __restrict__ ypglbp,
                                                      const double* __restrict__ wpp,
                                                      const double* __restrict__ omgpp,
@@ -1007,8 +1044,8 @@ __global__ void __launch_bounds__(128) k_fill_events(Geometry g, ParticleView pv
                                                      FillList fl) {
   using R = T;  // refill arithmetic in the population precision
   const int lane = threadIdx.x & 31;
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int warp = (bx * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gx * blockDim.x) >> 5;
   const int nev = min(*fl.count, fl.cap);
   const bool channel = g.channel != 0;
   const double rad = pp.rad;
@@ -1112,6 +1149,16 @@ __global__ void __launch_bounds__(128) k_fill_events(Geometry g, ParticleView pv
     if (lane < NPOP) f[(size_t)q * g.N + n] = T(fnew + feq_q<R>(q, u9, v9, w9, rho9));
   }
 }
+template <typename T>
+__global__ void __launch_bounds__(128) k_fill_events(Geometry g, ParticleView pv, PartParams pp,
+                                                     const double* __restrict__ ypglbp,
+                                                     const double* __restrict__ wpp,
+                                                     const double* __restrict__ omgpp,
+                                                     const int32_t* __restrict__ isnodes,
+                                                     const int32_t* __restrict__ isnodes0, T* f,
+                                                     FillList fl) {
+  k_fill_events_body<T>(blockIdx.x, gridDim.x, g, pv, pp, ypglbp, wpp, omgpp, isnodes, isnodes0, f, fl);
+}
 
 }  // namespace
 
@@ -1166,6 +1213,98 @@ void launch_filling(const Geometry& g, const ParticleView& pv, const PartParams&
   cudaMemsetAsync(fl.count, 0, sizeof(int), s);
   { k_fill_detect<<<pv.npart, PB, 0, s>>>(g, pv, pp, ypglbp, isnodes, isnodes0, fl, st); count_launch(); }
   { k_fill_events<T><<<4 * 152, 128, 0, s>>>(g, pv, pp, ypglbp, wpp, omgpp, isnodes, isnodes0, f, fl); count_launch(); }
+}
+
+// ---- many boxes per launch ------------------------------------------------
+namespace {
+
+#define BOX_OR_RETURN(nblocks_expr)                  \
+  const BoxParticles& B = boxes[blockIdx.y];         \
+  const int nblk = (nblocks_expr);                   \
+  if ((int)blockIdx.x >= nblk) return;
+
+__global__ void __launch_bounds__(PB) k_bounce_multi(const BoxParticles* boxes) {
+  BOX_OR_RETURN(B.pv.npart)
+  k_bounce_body<float>(blockIdx.x, nblk, B.g, B.pv, B.f, 1, B.flags_cur, B.ls, B.ms.fHIp, B.ms.torqp);
+}
+__global__ void __launch_bounds__(PB) k_bounce_store_multi(const BoxParticles* boxes) {
+  BOX_OR_RETURN(B.pv.npart)
+  k_bounce_store_body<float>(blockIdx.x, nblk, B.g, B.pv, B.f, 1, B.ls);
+}
+__global__ void k_lubforce_multi(const BoxParticles* boxes) {
+  BOX_OR_RETURN((B.pv.npart * 32 + 127) / 128)
+  k_lubforce_body(blockIdx.x, nblk, B.g, B.pv.npart, B.pp, B.ms);
+}
+__global__ void k_move_multi(const BoxParticles* boxes) {
+  BOX_OR_RETURN((B.pv.npart + 127) / 128)
+  k_move_body(blockIdx.x, nblk, B.pv.npart, B.pp, B.ms);
+}
+__global__ void k_clear_first_multi(const BoxParticles* boxes) {
+  const BoxParticles& B = boxes[blockIdx.y];
+  if (B.pv.npart > 0 && threadIdx.x == 0) *B.ms.first_move = 0;
+}
+__global__ void k_wrap_multi(const BoxParticles* boxes) {
+  BOX_OR_RETURN((B.pv.npart + 127) / 128)
+  k_wrap_body(blockIdx.x, nblk, B.g, B.pv.npart, B.ms);
+}
+__global__ void k_overlap_multi(const BoxParticles* boxes) {
+  BOX_OR_RETURN((B.pv.npart * 32 + 127) / 128)
+  k_overlap_body(blockIdx.x, nblk, B.g, B.pv.npart, B.pp, B.ms, B.st);
+}
+// the new step's flags: every id -1, the solid mask clear; the refill list empty
+__global__ void k_reset_multi(const BoxParticles* boxes) {
+  const BoxParticles& B = boxes[blockIdx.y];
+  if (B.pv.npart <= 0) return;
+  const long long N = B.g.N;
+  const long long words = (long long)B.g.ny * B.g.nz * B.g.sw;
+  uint32_t* mask = reinterpret_cast<uint32_t*>(B.flags_next + N);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < N + words; t += stride) {
+    if (t < N) B.flags_next[t] = -1;
+    else mask[t - N] = 0u;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) *B.fl.count = 0;
+}
+__global__ void k_link_sweeps_multi(const BoxParticles* boxes) {
+  BOX_OR_RETURN((3 * B.pv.npart + 127) / 128)
+  k_link_sweeps_body(blockIdx.x, nblk, B.g, B.pv, B.ls);
+}
+__global__ void __launch_bounds__(PB) k_links_multi(const BoxParticles* boxes) {
+  BOX_OR_RETURN(B.pv.npart)
+  k_links_body(blockIdx.x, nblk, B.g, B.pv, B.flags_next, B.ls, B.st, 1);
+}
+__global__ void __launch_bounds__(PB) k_fill_detect_multi(const BoxParticles* boxes) {
+  BOX_OR_RETURN(B.pv.npart)
+  k_fill_detect_body(blockIdx.x, nblk, B.g, B.pv, B.pp, B.ms.ypglbp, B.flags_next, B.flags_cur, B.fl,
+                     B.st);
+}
+constexpr int kFillBlocks = 8;
+__global__ void __launch_bounds__(128) k_fill_events_multi(const BoxParticles* boxes) {
+  BOX_OR_RETURN(B.pv.npart > 0 ? kFillBlocks : 0)
+  k_fill_events_body<float>(blockIdx.x, nblk, B.g, B.pv, B.pp, B.ms.ypglbp, B.ms.wpp, B.ms.omgpp,
+                            B.flags_next, B.flags_cur, B.f, B.fl);
+}
+#undef BOX_OR_RETURN
+
+}  // namespace
+
+void launch_particle_step_multi(const BoxParticles* boxes, int nb, int max_npart,
+                                long long max_reset, cudaStream_t s) {
+  if (nb <= 0 || max_npart <= 0) return;
+  auto grid = [&](long long blocks) { return dim3((unsigned)(blocks > 0 ? blocks : 1), nb); };
+  k_bounce_multi<<<grid(max_npart), PB, 0, s>>>(boxes); count_launch();
+  k_bounce_store_multi<<<grid(max_npart), PB, 0, s>>>(boxes); count_launch();
+  k_lubforce_multi<<<grid((max_npart * 32 + 127) / 128), 128, 0, s>>>(boxes); count_launch();
+  k_move_multi<<<grid((max_npart + 127) / 128), 128, 0, s>>>(boxes); count_launch();
+  k_clear_first_multi<<<grid(1), 32, 0, s>>>(boxes); count_launch();
+  k_wrap_multi<<<grid((max_npart + 127) / 128), 128, 0, s>>>(boxes); count_launch();
+  k_overlap_multi<<<grid((max_npart * 32 + 127) / 128), 128, 0, s>>>(boxes); count_launch();
+  const long long rb = (max_reset + 256 * 8 - 1) / (256 * 8);
+  k_reset_multi<<<grid(rb < 1024 ? rb : 1024), 256, 0, s>>>(boxes); count_launch();
+  k_link_sweeps_multi<<<grid((3 * max_npart + 127) / 128), 128, 0, s>>>(boxes); count_launch();
+  k_links_multi<<<grid(max_npart), PB, 0, s>>>(boxes); count_launch();
+  k_fill_detect_multi<<<grid(max_npart), PB, 0, s>>>(boxes); count_launch();
+  k_fill_events_multi<<<grid(kFillBlocks), 128, 0, s>>>(boxes); count_launch();
 }
 
 template void launch_bounce_back<double>(const Geometry&, const ParticleView&, const double*,
