@@ -151,11 +151,14 @@ def initial_f(u):
     return f
 
 
-def run_device(wl, u, y, steps, warmup, device, want_f=False, variant=None):
+def run_device(wl, u, y, steps, warmup, device, want_f=False, variant=None, sums=None):
     """Device-resident timing of `steps` C-ABI step calls."""
     import torch
+    from multiphase_flow_codes_gb300 import _capi as capi
     from multiphase_flow_codes_gb300.engine import LBMBox
     box = LBMBox(wl.cfg)
+    if sums is not None and wl.cfg.precision == capi.LBM_PREC_F64:
+        box.set_sums(sums)
     stream = torch.cuda.Stream(device=device)
     box.set_stream(stream.cuda_stream)
     box.initpop(*u)
@@ -201,11 +204,14 @@ def kernel_name(variant):
     return "k_fused (stream + MRT collide + forcing; direct)"
 
 
-def run_e2e(wl, f0_fortran, y, steps, device, variant=None):
+def run_e2e(wl, f0_fortran, y, steps, device, variant=None, sums=None):
     """End to end through the C ABI with host buffers (see module doc)."""
     import torch
+    from multiphase_flow_codes_gb300 import _capi as capi
     from multiphase_flow_codes_gb300.engine import LBMBox
     box = LBMBox(wl.cfg)
+    if sums is not None and wl.cfg.precision == capi.LBM_PREC_F64:
+        box.set_sums(sums)
     if variant is not None:
         box.set_variant(*variant)
     npart = y.shape[0]
@@ -300,6 +306,9 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=20.0,
                     help="window of the Poisson serving run (0: skip it)")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="requests per second")
+    ap.add_argument("--sums", choices=["fixed", "float"], default="fixed",
+                    help="FP64 collision arithmetic: integer-coefficient moment sums exact in "
+                         "64-bit fixed point (default) or all in FP64")
     ap.add_argument("--variant", default=None,
                     help="stream+collide kernel as 'variant,stages,groups,ctas_per_sm' "
                          "(default: autotuned on the workload)")
@@ -322,6 +331,9 @@ def main():
                 "forcing": "stochastic low-k (|k| < sqrt 8)", "mrt_type": c.mrt_type,
                 "l2": "inputs larger than L2 (populations %.2f GB)" % (2 * 19 * N * (8 if dtype == "f64" else 4) / 1e9),
                 "parallelism": f"replicas x{world}"}
+    if dtype == "f64":
+        cfg_desc["collision_sums"] = ("integer-coefficient moment sums exact in 64-bit fixed point, "
+                                      "products FP64" if args.sums == "fixed" else "all FP64")
 
     if args.impl == "reference":
         if rank != 0:
@@ -357,8 +369,10 @@ def main():
     torch.cuda.synchronize()
     sampler.start()
     fixed = tuple(int(v) for v in args.variant.split(",")) if args.variant else None
+    sums = capi.LBM_SUMS_FIXED if args.sums == "fixed" else capi.LBM_SUMS_FLOAT
     ms, launches, phases, f64, p64, variant = run_device(wl, u, y, args.steps, args.warmup, local,
-                                                         want_f=not args.no_fp32, variant=fixed)
+                                                         want_f=not args.no_fp32, variant=fixed,
+                                                         sums=sums)
     clocks = sampler.stop()
     rate, t_s = rep.rate(N * args.steps, ms / 1e3)
     t_ms = t_s * 1e3
@@ -372,7 +386,7 @@ def main():
     alg_bytes = 2 * 19 * esz * N
     achieved = alg_bytes / (sc_ms / sc_n / 1e3) / 1e9 if sc_n else None
     figs = profile_figures()
-    key = f"fused_{dtype}_{c.nx}"
+    key = f"fused_{dtype}_{c.nx}" + ("_fx" if dtype == "f64" and args.sums == "fixed" else "")
     traffic = None
     if key in figs and figs[key].get("dram_bytes_per_node"):
         traffic = figs[key]["dram_bytes_per_node"] * N
@@ -455,7 +469,7 @@ def main():
         f0 = initial_f(u)
         f0_fortran = np.asfortranarray(np.transpose(f0, (0, 3, 2, 1)))
         del f0
-        e_ms, h2d, d2h = run_e2e(wl, f0_fortran, y, args.steps, local, variant)
+        e_ms, h2d, d2h = run_e2e(wl, f0_fortran, y, args.steps, local, variant, sums)
         e_rate, _ = rep.rate(N * args.steps, e_ms / 1e3)
         line["e2e"] = {"value": e_rate / 1e6, "unit": "MLUPS",
                        "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,

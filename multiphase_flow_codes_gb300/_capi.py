@@ -31,6 +31,7 @@ LBM_BC_PERIODIC, LBM_BC_XWALLS = 0, 1
 LBM_FORCING_NONE, LBM_FORCING_STOCHASTIC, LBM_FORCING_CONSTANT = 0, 1, 2
 LBM_PRESET_BOX, LBM_PRESET_CHANNEL = 0, 1
 LBM_VARIANT_DIRECT, LBM_VARIANT_STAGED, LBM_VARIANT_STAGED_X2 = 1, 2, 3
+LBM_SUMS_FLOAT, LBM_SUMS_FIXED = 0, 1
 
 
 class lbm_config(C.Structure):
@@ -106,6 +107,8 @@ SIGNATURES = {
     "lbm_mass_momentum_noalloc": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, _P]),
     "lbm_fma_throughput": (C.c_int, [C.c_int, _D]),
     "lbm_set_variant": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "lbm_set_sums": (C.c_int, [_P, C.c_int]),
+    "lbm_get_sums": (C.c_int, [_P, C.POINTER(C.c_int)]),
     "lbm_get_variant": (C.c_int, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                   C.POINTER(C.c_int)]),
     "lbm_autotune": (C.c_int, [_P, C.c_int, _D]),

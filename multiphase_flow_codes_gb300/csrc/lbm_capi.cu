@@ -67,6 +67,8 @@ struct lbm_ctx {
   // stream + collide kernel (lbm_set_variant / lbm_autotune)
   int variant = LBM_VARIANT_DIRECT;
   StagedPlan staged;
+  // arithmetic of the FP64 collision (lbm_set_sums)
+  int sums = LBM_SUMS_FLOAT;
 
   // forcing
   ForcingDev* d_forcing = nullptr;
@@ -405,7 +407,7 @@ void launch_stream_collide(lbm_ctx* c, const T* fin, T* fout) {
                            fview<T>(c, c->latest), c->staged, c->status, c->stream);
   else
     launch_fused_step<T>(c->g, c->r, fin, fout, c->flags[c->fcur], fview<T>(c, c->fmacro),
-                         fview<T>(c, c->latest), c->stream);
+                         fview<T>(c, c->latest), c->sums == LBM_SUMS_FIXED, c->stream);
 }
 
 // plan a staged variant with `stages` stages (0: the default, four where two
@@ -414,18 +416,19 @@ void launch_stream_collide(lbm_ctx* c, const T* fin, T* fout) {
 bool plan_staged(lbm_ctx* c, int variant, int stages, int ctas_per_sm, StagedPlan* p,
                  int groups = 1) {
   const bool packed = variant == LBM_VARIANT_STAGED_X2;
+  const bool fx = !c->f32 && c->sums == LBM_SUMS_FIXED;
   if (variant != LBM_VARIANT_STAGED && !packed) return false;
   if (stages == 0) {
     for (int S = 4; S >= 2 && stages == 0; --S) {
       StagedPlan t;
       const bool ok = c->f32 ? plan_fused_staged<float>(c->g, S, 0, packed, groups, &t)
-                             : plan_fused_staged<double>(c->g, S, 0, packed, groups, &t);
+                             : plan_fused_staged<double>(c->g, S, 0, packed, groups, &t, fx);
       if (ok && (t.ctas_per_sm >= 2 || S == 2)) stages = S;
     }
     if (stages == 0) return false;
   }
   return c->f32 ? plan_fused_staged<float>(c->g, stages, ctas_per_sm, packed, groups, p)
-                : plan_fused_staged<double>(c->g, stages, ctas_per_sm, packed, groups, p);
+                : plan_fused_staged<double>(c->g, stages, ctas_per_sm, packed, groups, p, fx);
 }
 
 // the part of a fused step after stream + collide: bounce-back, the
@@ -696,6 +699,7 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
   g.channel = cfg->boundary == LBM_BC_XWALLS;
   g.sw = 4 * ((g.nx + 127) / 128);
   ctx->f32 = cfg->precision == LBM_PREC_F32;
+  ctx->sums = ctx->f32 ? LBM_SUMS_FLOAT : LBM_SUMS_FIXED;
   ctx->esz = ctx->f32 ? 4 : 8;
   // MRT rates, B/para.f90:91-135
   const double tau = 3.0 * cfg->visc + 0.5;
@@ -1400,6 +1404,34 @@ int lbm_set_variant(lbm_ctx* ctx, int variant, int stages, int groups, int ctas_
   }
   ctx->variant = variant;
   ctx->staged = p;
+  return LBM_OK;
+}
+
+int lbm_set_sums(lbm_ctx* ctx, int mode) {
+  if (!ctx) return LBM_ERR_ARG;
+  if (mode != LBM_SUMS_FLOAT && mode != LBM_SUMS_FIXED)
+    return fail(ctx, LBM_ERR_ARG, "unknown collision arithmetic");
+  if (ctx->f32 && mode != LBM_SUMS_FLOAT)
+    return fail(ctx, LBM_ERR_ARG, "fixed-point sums apply to FP64 contexts only");
+  const int keep = ctx->sums;
+  ctx->sums = mode;
+  if (ctx->variant != LBM_VARIANT_DIRECT) {
+    // the staged kernel differs: re-plan the same schedule for it
+    StagedPlan p;
+    if (!plan_staged(ctx, ctx->variant, ctx->staged.S, ctx->staged.ctas_per_sm, &p,
+                     ctx->staged.groups)) {
+      cudaGetLastError();
+      ctx->sums = keep;
+      return fail(ctx, LBM_ERR_ARG, "the current stream+collide schedule does not apply");
+    }
+    ctx->staged = p;
+  }
+  return LBM_OK;
+}
+
+int lbm_get_sums(lbm_ctx* ctx, int* mode) {
+  if (!ctx || !mode) return LBM_ERR_ARG;
+  *mode = ctx->sums;
   return LBM_OK;
 }
 

@@ -69,7 +69,7 @@ RatesT<T> rates_t(const Rates& r) {
 //   fp*     body force of the previous step (macrovar's u = j + Fp/2)
 //   f*      body force of this step
 template <typename T>
-__device__ __forceinline__ void collide_fast(T (&f)[NPOP], T fpx, T fpy, T fpz, T fx, T fy,
+__host__ __device__ __forceinline__ void collide_fast(T (&f)[NPOP], T fpx, T fpy, T fpz, T fx, T fy,
                                              T fz, const RatesT<T>& r) {
   const T a1 = f[1] + f[2], d1 = f[1] - f[2];
   const T a3 = f[3] + f[4], d3 = f[3] - f[4];
@@ -193,6 +193,220 @@ __device__ __forceinline__ void collide_fast(T (&f)[NPOP], T fpx, T fpy, T fpz, 
     f[17] = base + m - tl17 + r2;
     f[18] = base - p + tl17 - r1;
   }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 collision with error-free integer sums.
+//
+// GB300 issues FP64 at about 2 lanes per clock per SM and 32-bit integer work
+// at 64, so the FP64 kernel is bound by its FP64 instruction count.  Two
+// thirds of those instructions are the sums with small integer coefficients
+// of the forward and inverse moment transforms.  collide_fx computes those
+// sums exactly in 64-bit fixed point (integer adds, no rounding) and keeps
+// every product with a non-integer factor (rates, equilibrium, forcing) in
+// FP64.  Conversions between FP64 and fixed point are integer bit operations
+// (the hardware conversions run at the FP64 rate):
+//   inputs and forward sums  v * 2^-58, inputs |f| < 2^-3, sums |.| < 2^5
+//   scaled moments, outputs  v * 2^-61, moments |M| < 2^-5, sums |.| < 2^2
+// Input rounding is at most 2^-59 and moment rounding 2^-62 in absolute
+// terms, the size of the FP64 rounding of the same sums at the populations'
+// magnitudes (~1e-2), so results agree with collide_fast to rounding.  A
+// node whose inputs or moments leave these ranges (or are not finite), or
+// whose populations are all below 2^-12 in magnitude (where the fixed
+// point's absolute resolution would cost relative precision), is reported
+// by a false return with f untouched; the caller then collides it with
+// collide_fast.
+
+constexpr int kFxIn = 58, kFxInMax = -3;    // inputs, forward transform
+constexpr int kFxOut = 61, kFxOutMax = -5;  // scaled moments, inverse transform
+// a node whose largest |f| is below 2^kFxMinExp keeps FP64's relative
+// precision through the FP64 path (fixed point resolves 2^-61 absolute)
+constexpr int kFxMinExp = -12;
+
+template <int K, int MAXEXP>
+__host__ __device__ __forceinline__ long long fx_from(double x, unsigned& bad, unsigned& big) {
+  static_assert(64 - K - MAXEXP >= 2, "fixed-point range");
+  unsigned long long b;
+  memcpy(&b, &x, 8);
+  const int e = (int)((b >> 52) & 0x7ff);
+  bad |= (unsigned)(e >= 1023 + MAXEXP);  // |x| >= 2^MAXEXP, inf, nan
+  big |= (unsigned)(e >= 1023 + kFxMinExp);
+  // magnitude with the hidden bit at bit 63: |x| = m * 2^(e - 1086)
+  const unsigned long long m = (b << 11) | 0x8000000000000000ULL;
+  // |x| * 2^K = m * 2^-(1086 - K - e); round half up on the magnitude
+  const int r = 1086 - K - e;  // >= 2 under the range test; zero/subnormal: > 64
+  const int rr = (r < 64 ? r : 64) - 1;
+  unsigned long long v = ((m >> rr) + 1) >> 1;
+  if (r > 64 || bad) v = 0;
+  return (b >> 63) ? -(long long)v : (long long)v;
+}
+
+template <int K>
+__host__ __device__ __forceinline__ double fx_to(long long v) {
+  if (v == 0) return 0.0;
+  const unsigned long long s = v < 0 ? 1ULL : 0ULL;
+  unsigned long long a = s ? 0ULL - (unsigned long long)v : (unsigned long long)v;
+#ifdef __CUDA_ARCH__
+  const int lz = __clzll((long long)a);
+#else
+  const int lz = __builtin_clzll(a);
+#endif
+  a <<= lz;  // leading one at bit 63
+  unsigned long long mant = a >> 11;  // 53 bits with the hidden one
+  const unsigned rem = (unsigned)(a & 0x7ff);
+  mant += (unsigned long long)((rem > 0x400u) | ((rem == 0x400u) & (unsigned)(mant & 1)));
+  // value in [2^(63-lz-K), 2^(64-lz-K)); a mantissa carry to 2^53 adds one
+  // to the exponent field through the sum below
+  const unsigned long long E = (unsigned long long)(63 - lz - K + 1023);
+  const unsigned long long bits = (s << 63) | (((E - 1) << 52) + mant);
+  double d;
+  memcpy(&d, &bits, 8);
+  return d;
+}
+
+
+// Same arithmetic as collide_fast (same operands, same FP64 products); only
+// the integer-coefficient sums are exact.  Returns false, leaving f as it
+// was, when a value is out of the fixed-point ranges.
+__host__ __device__ __forceinline__ bool collide_fx(double (&f)[NPOP], double fpx, double fpy,
+                                                    double fpz, double fx, double fy, double fz,
+                                                    const RatesT<double>& r) {
+  typedef long long I;
+  unsigned bad = 0, big = 0;
+  I g[NPOP];
+#pragma unroll
+  for (int q = 0; q < NPOP; ++q) g[q] = fx_from<kFxIn, kFxInMax>(f[q], bad, big);
+  if (bad || !big) return false;
+  // forward transform, exact (collision.f90:101-118; grouping as collide_fast)
+  const I a1 = g[1] + g[2], d1 = g[1] - g[2];
+  const I a3 = g[3] + g[4], d3 = g[3] - g[4];
+  const I a5 = g[5] + g[6], d5 = g[5] - g[6];
+  const I s78 = g[7] + g[8], d78 = g[7] - g[8], s910 = g[9] + g[10], d910 = g[9] - g[10];
+  const I s1112 = g[11] + g[12], d1112 = g[11] - g[12];
+  const I s1314 = g[13] + g[14], d1314 = g[13] - g[14];
+  const I s1516 = g[15] + g[16], d1516 = g[15] - g[16];
+  const I s1718 = g[17] + g[18], d1718 = g[17] - g[18];
+  const I sum1 = a1 + a3 + a5;
+  const I Sxy = s78 + s910, Sxz = s1112 + s1314, Syz = s1516 + s1718;
+  const I sum2 = Sxy + Sxz + Syz;
+  const I D1 = d78 + d910, D2 = d1112 + d1314;
+  const I sum3 = D1 + D2;
+  const I A = s78 - s910, Bv = d1516 + d1718;
+  const I sum4 = A + Bv;
+  const I C = s1112 - s1314, Dd = s1516 - s1718;
+  const I sum5 = C + Dd;
+  const I sum7 = a3 + a5, sum8 = Sxy + Sxz, sum10 = a3 - a5, sum11 = Sxy - Sxz;
+  const double rho = fx_to<kFxIn>(g[0] + sum1 + sum2);
+  const double jx = fx_to<kFxIn>(d1 + sum3), jy = fx_to<kFxIn>(d3 + sum4),
+               jz = fx_to<kFxIn>(d5 + sum5);
+  const double ev1 = fx_to<kFxIn>(-30 * g[0] - 11 * sum1 + 8 * sum2);
+  const double ev2 = fx_to<kFxIn>(12 * g[0] - 4 * sum1 + sum2);
+  const double ev3 = fx_to<kFxIn>(-4 * d1 + sum3);
+  const double ev4 = fx_to<kFxIn>(-4 * d3 + sum4);
+  const double ev5 = fx_to<kFxIn>(-4 * d5 + sum5);
+  const double ev6 = fx_to<kFxIn>(2 * (a1 - Syz) - sum7 + sum8);
+  const double ev7 = fx_to<kFxIn>(-4 * a1 + 2 * (sum7 - Syz) + sum8);
+  const double ev8 = fx_to<kFxIn>(sum10 + sum11);
+  const double ev9 = fx_to<kFxIn>(-2 * sum10 + sum11);
+  const double ev10 = fx_to<kFxIn>(d78 - d910);
+  const double ev11 = fx_to<kFxIn>(d1516 - d1718);
+  const double ev12 = fx_to<kFxIn>(d1112 - d1314);
+  const double ev13 = fx_to<kFxIn>(D1 - D2);
+  const double ev14 = fx_to<kFxIn>(Bv - A);
+  const double ev15 = fx_to<kFxIn>(C - Dd);
+  // macrovar: u = sum c f + F_prev / 2
+  const double ux = jx + 0.5 * fpx, uy = jy + 0.5 * fpy, uz = jz + 0.5 * fpz;
+
+  // equilibrium and forcing moments, FP64 (collision.f90:66-81)
+  const double uxs = ux * ux, uys = uy * uy, uzs = uz * uz;
+  const double t1 = uxs + uys + uzs;
+  const double eq6 = 2.0 * uxs - uys - uzs;
+  const double eq8 = uys - uzs;
+  const double fa = fx * ux, fb = fy * uy, fc = fz * uz;
+  const double G3 = fa + fb + fc;
+  const double e6 = 2.0 * fa - fb - fc;
+  const double e8 = fb - fc;
+
+  // scaled post-collision moments (collision.f90:138-157), then fixed point
+  I M[16];
+  M[1] = fx_from<kFxOut, kFxOutMax>(r.A[1] * ev1 + r.B1r * rho + r.B1t * t1 + r.H1 * G3, bad, big);
+  M[2] = fx_from<kFxOut, kFxOutMax>(r.A[2] * ev2 + r.B2r * rho + r.B2t * t1 + r.H2 * G3, bad, big);
+  M[3] = fx_from<kFxOut, kFxOutMax>(r.A[3] * ev3 + r.B3 * ux + r.H3 * fx, bad, big);
+  M[4] = fx_from<kFxOut, kFxOutMax>(r.A[4] * ev4 + r.B3 * uy + r.H3 * fy, bad, big);
+  M[5] = fx_from<kFxOut, kFxOutMax>(r.A[5] * ev5 + r.B3 * uz + r.H3 * fz, bad, big);
+  M[6] = fx_from<kFxOut, kFxOutMax>(r.A[6] * ev6 + r.B6 * eq6 + r.H6 * e6, bad, big);
+  M[7] = fx_from<kFxOut, kFxOutMax>(r.A[7] * ev7 + r.B7 * eq6 + r.H7 * e6, bad, big);
+  M[8] = fx_from<kFxOut, kFxOutMax>(r.A[8] * ev8 + r.B8 * eq8 + r.H8 * e8, bad, big);
+  M[9] = fx_from<kFxOut, kFxOutMax>(r.A[9] * ev9 + r.B9 * eq8 + r.H9 * e8, bad, big);
+  M[10] = fx_from<kFxOut, kFxOutMax>(
+      r.A[10] * ev10 + uy * (r.B10 * ux + r.H10 * fx) + r.H10 * fy * ux, bad, big);
+  M[11] = fx_from<kFxOut, kFxOutMax>(
+      r.A[11] * ev11 + uz * (r.B10 * uy + r.H10 * fy) + r.H10 * fz * uy, bad, big);
+  M[12] = fx_from<kFxOut, kFxOutMax>(
+      r.A[12] * ev12 + uz * (r.B10 * ux + r.H10 * fx) + r.H10 * fz * ux, bad, big);
+  M[13] = fx_from<kFxOut, kFxOutMax>(r.A[13] * ev13, bad, big);
+  M[14] = fx_from<kFxOut, kFxOutMax>(r.A[14] * ev14, bad, big);
+  M[15] = fx_from<kFxOut, kFxOutMax>(r.A[15] * ev15, bad, big);
+  const I tl1 = fx_from<kFxOut, kFxOutMax>((1.0 / 19.0) * rho, bad, big);
+  const I tl6 = fx_from<kFxOut, kFxOutMax>(0.1 * ux + 0.05 * fx, bad, big);
+  const I tl8 = fx_from<kFxOut, kFxOutMax>(0.1 * uy + 0.05 * fy, bad, big);
+  const I tl10 = fx_from<kFxOut, kFxOutMax>(0.1 * uz + 0.05 * fz, bad, big);
+  if (bad) return false;
+
+  // inverse transform, exact (collision.f90:160-200)
+  I h[NPOP];
+  h[0] = tl1 - 30 * M[1] + 12 * M[2];
+  const I suma = tl1 - 11 * M[1] - 4 * M[2];
+  const I sumb = tl1 + 8 * M[1] + M[2];
+  const I sumc = tl6 - 4 * M[3];
+  const I sumd = 2 * M[6] - 4 * M[7];
+  const I sume = tl8 - 4 * M[4];
+  const I q67 = 2 * M[7] - M[6], r89 = M[8] - 2 * M[9];
+  const I sumf = q67 + r89;
+  const I sumg = tl10 - 4 * M[5];
+  const I sumh = q67 - r89;
+  const I p67 = M[6] + M[7], p89 = M[8] + M[9];
+  const I sumi = p67 + p89;
+  const I sumk = p67 - p89;
+  const I sump = -2 * p67;
+  const I sum67 = tl6 + M[3], sum89 = tl8 + M[4], sum1011 = tl10 + M[5];
+  const I ad = suma + sumd, af = suma + sumf, ah = suma + sumh;
+  h[1] = ad + sumc;
+  h[2] = ad - sumc;
+  h[3] = af + sume;
+  h[4] = af - sume;
+  h[5] = ah + sumg;
+  h[6] = ah - sumg;
+  {  // x-y diagonals 7..10
+    const I base = sumb + sumi, p = sum67 + sum89, m = sum67 - sum89;
+    const I bp = base + M[10], bm = base - M[10];
+    const I P = p + (M[13] - M[14]), Q = m + (M[13] + M[14]);
+    h[7] = bp + P;
+    h[10] = bp - P;
+    h[8] = bm - Q;
+    h[9] = bm + Q;
+  }
+  {  // x-z diagonals 11..14
+    const I base = sumb + sumk, p = sum67 + sum1011, m = sum67 - sum1011;
+    const I bp = base + M[12], bm = base - M[12];
+    const I P = p + (M[15] - M[13]), Q = m - (M[13] + M[15]);
+    h[11] = bp + P;
+    h[14] = bp - P;
+    h[12] = bm - Q;
+    h[13] = bm + Q;
+  }
+  {  // y-z diagonals 15..18
+    const I base = sumb + sump, p = sum89 + sum1011, m = sum89 - sum1011;
+    const I bp = base + M[11], bm = base - M[11];
+    const I P = p + (M[14] - M[15]), Q = m + (M[14] + M[15]);
+    h[15] = bp + P;
+    h[18] = bp - P;
+    h[16] = bm - Q;
+    h[17] = bm + Q;
+  }
+#pragma unroll
+  for (int q = 0; q < NPOP; ++q) f[q] = fx_to<kFxOut>(h[q]);
+  return true;
 }
 
 // Body force of two fields (previous and current step) at one node, sharing

@@ -206,7 +206,9 @@ __device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >
 // fused stream + collide (push).  One thread per node, a block covers part
 // of an x-row; grid (ceil(nx/B), ny, nz).  Node indices fit in 32 bits
 // (N < 2^26 is enforced at context creation).
-template <typename T, bool CHANNEL>
+// FX (FP64 only): collide with exact fixed-point moment sums (collide_fx),
+// falling back to collide_fast for the nodes it declines.
+template <typename T, bool CHANNEL, bool FX = false>
 __global__ void __launch_bounds__(128) k_fused(Geometry g, RatesT<T> r, const T* __restrict__ fin,
                                                T* __restrict__ fout,
                                                const int32_t* __restrict__ isnodes,
@@ -222,7 +224,17 @@ __global__ void __launch_bounds__(128) k_fused(Geometry g, RatesT<T> r, const T*
   if (!is_solid(solid_mask(isnodes, g), g, z * g.ny + y, x)) {
     T fp[3], fc[3];
     body_force2(fprev, fnew, x, z * g.ny + y, fp, fc);
-    collide_fast(f, fp[0], fp[1], fp[2], fc[0], fc[1], fc[2], r);
+    bool done = false;
+    if constexpr (FX) {
+      done = collide_fx(f, fp[0], fp[1], fp[2], fc[0], fc[1], fc[2], r);
+      if (!done) {
+        // reloaded rather than kept, so the inputs need no registers
+        // during the fixed-point collision
+#pragma unroll
+        for (int q = 0; q < NPOP; ++q) f[q] = fin[(size_t)q * N + n];
+      }
+    }
+    if (!done) collide_fast(f, fp[0], fp[1], fp[2], fc[0], fc[1], fc[2], r);
   }
   // push: neighbour offsets with periodic wrap
   const int oxp = (x == nx - 1) ? 1 - nx : 1, oxm = (x == 0) ? nx - 1 : -1;
@@ -507,9 +519,19 @@ inline unsigned blocks_for(long long n, int b) { return (unsigned)((n + b - 1) /
 template <typename T>
 void launch_fused_step(const Geometry& g, const Rates& r, const T* fin, T* fout,
                        const int32_t* isnodes, const ForceView<T>& fprev,
-                       const ForceView<T>& fnew, cudaStream_t s) {
+                       const ForceView<T>& fnew, bool fx, cudaStream_t s) {
   const int B = 128;
   const RatesT<T> rt = rates_t<T>(r);
+  if constexpr (sizeof(T) == 8) {
+    if (fx) {
+      if (g.channel)
+        k_fused<T, true, true><<<row_grid(g, B), B, 0, s>>>(g, rt, fin, fout, isnodes, fprev, fnew);
+      else
+        k_fused<T, false, true><<<row_grid(g, B), B, 0, s>>>(g, rt, fin, fout, isnodes, fprev, fnew);
+      count_launch();
+      return;
+    }
+  }
   if (g.channel)
     { k_fused<T, true><<<row_grid(g, B), B, 0, s>>>(g, rt, fin, fout, isnodes, fprev, fnew); count_launch(); }
   else
@@ -617,7 +639,7 @@ void launch_forcing_tables(const Geometry& g, const ForcingDev* st, const double
 #define LBM_INSTANTIATE(T)                                                                   \
   template void launch_fused_step<T>(const Geometry&, const Rates&, const T*, T*,           \
                                      const int32_t*, const ForceView<T>&,                   \
-                                     const ForceView<T>&, cudaStream_t);                    \
+                                     const ForceView<T>&, bool, cudaStream_t);              \
   template void launch_macrovar<T>(const Geometry&, const T*, const int32_t*,               \
                                    const ForceView<T>&, const ParticleView&, T*, T*, T*, T*, \
                                    cudaStream_t);                                           \

@@ -20,6 +20,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cstring>
 #include <cuda_runtime.h>
 
 #include "../../include/lbm.h"
@@ -136,13 +137,14 @@ void count_launch();
 template <typename T>
 void launch_fused_step(const Geometry& g, const Rates& r, const T* fin, T* fout,
                        const int32_t* isnodes, const ForceView<T>& fprev,
-                       const ForceView<T>& fnew, cudaStream_t s);
+                       const ForceView<T>& fnew, bool fx, cudaStream_t s);
 // the same step with its rows staged through shared memory by bulk copies
 // (lbm_staged.cu); periodic boxes with nx a multiple of 4
 struct StagedPlan {
   int S = 0;            // input stages (rows in flight + 1)
   bool packed = false;  // FP32 pair kernel on f32x2 arithmetic
   int groups = 1;       // packed: consumer warp groups (rows in the collision at once)
+  bool fx = false;      // FP64: exact fixed-point moment sums (collide_fx)
   int ctas_per_sm = 0;
   int grid = 0, threads = 0;
   size_t smem = 0;
@@ -153,7 +155,7 @@ template <typename T>
 int staged_max_stages(const Geometry& g);
 template <typename T>
 bool plan_fused_staged(const Geometry& g, int S, int ctas_per_sm, bool packed, int groups,
-                       StagedPlan* plan);
+                       StagedPlan* plan, bool fx = false);
 template <typename T>
 void launch_fused_staged(const Geometry& g, const Rates& r, const T* fin, T* fout,
                          const int32_t* isnodes, const ForceView<T>& fprev,

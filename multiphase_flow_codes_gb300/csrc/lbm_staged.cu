@@ -116,7 +116,9 @@ __device__ __forceinline__ void row_force(const ForceView<T>& v, const T* k, T c
 
 // Scalar consumers: one node per thread.  One producer warp (warp 0) and
 // W = blockDim/32 - 1 consumer warps.
-template <typename T, bool CHANNEL>
+// FX (FP64 only): collide with exact fixed-point moment sums (collide_fx),
+// falling back to collide_fast for the nodes it declines.
+template <typename T, bool CHANNEL, bool FX = false>
 __global__ void __launch_bounds__(288) k_fused_staged(Geometry g, RatesT<T> r,
                                                       const T* __restrict__ fin,
                                                       T* __restrict__ fout,
@@ -188,7 +190,15 @@ __global__ void __launch_bounds__(288) k_fused_staged(Geometry g, RatesT<T> r,
         T fp[3], fc[3];
         row_force(fprev, ka, c1, s1, c2, s2, fp);
         row_force(fnew, kb, c1, s1, c2, s2, fc);
-        collide_fast(f, fp[0], fp[1], fp[2], fc[0], fc[1], fc[2], r);
+        bool done = false;
+        if constexpr (FX) {
+          done = collide_fx(f, fp[0], fp[1], fp[2], fc[0], fc[1], fc[2], r);
+          if (!done) {
+#pragma unroll
+            for (int q = 0; q < NPOP; ++q) f[q] = in[q * nx + x];
+          }
+        }
+        if (!done) collide_fast(f, fp[0], fp[1], fp[2], fc[0], fc[1], fc[2], r);
       }
       // 32-bit element indices: 19 N < 2^31 (N < 2^26 is enforced)
       const int n = n0 + x;
@@ -381,11 +391,14 @@ int staged_max_stages(const Geometry& g) {
 }
 
 template <typename T>
-static void* staged_kernel(bool channel, bool packed) {
+static void* staged_kernel(bool channel, bool packed, bool fx) {
   if (packed) {
     if constexpr (sizeof(T) == 4)
       return channel ? (void*)k_fused_staged_x2<true> : (void*)k_fused_staged_x2<false>;
     return nullptr;
+  }
+  if constexpr (sizeof(T) == 8) {
+    if (fx) return channel ? (void*)k_fused_staged<T, true, true> : (void*)k_fused_staged<T, false, true>;
   }
   return channel ? (void*)k_fused_staged<T, true> : (void*)k_fused_staged<T, false>;
 }
@@ -395,12 +408,13 @@ static void* staged_kernel(bool channel, bool packed) {
 // false when the plan does not apply.
 template <typename T>
 bool plan_fused_staged(const Geometry& g, int S, int ctas_per_sm, bool packed, int groups,
-                       StagedPlan* plan) {
+                       StagedPlan* plan, bool fx) {
+  fx = fx && sizeof(T) == 8 && !packed;
   if (!staged_eligible<T>(g, S, packed)) return false;
   const StagedLayout<T> L{g.nx, S, g.sw};
   int dev = 0, sms = 0, fit = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return false;
-  const void* kern = staged_kernel<T>(g.channel != 0, packed);
+  const void* kern = staged_kernel<T>(g.channel != 0, packed, fx);
   if (!kern) return false;
   // the largest plan any caller may launch, so plans can alternate freely
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024) !=
@@ -431,6 +445,7 @@ bool plan_fused_staged(const Geometry& g, int S, int ctas_per_sm, bool packed, i
   plan->S = S;
   plan->packed = packed;
   plan->groups = groups;
+  plan->fx = fx;
   plan->ctas_per_sm = per_sm;
   plan->grid = nrows < sms * per_sm ? nrows : sms * per_sm;
   return true;
@@ -454,6 +469,18 @@ void launch_fused_staged(const Geometry& g, const Rates& r, const T* fin, T* fou
       return;
     }
   }
+  if constexpr (sizeof(T) == 8) {
+    if (p.fx) {
+      if (g.channel)
+        k_fused_staged<T, true, true><<<p.grid, p.threads, p.smem, s>>>(
+            g, rates_t<T>(r), fin, fout, isnodes, fprev, fnew, p.S, st);
+      else
+        k_fused_staged<T, false, true><<<p.grid, p.threads, p.smem, s>>>(
+            g, rates_t<T>(r), fin, fout, isnodes, fprev, fnew, p.S, st);
+      count_launch();
+      return;
+    }
+  }
   if (g.channel)
     k_fused_staged<T, true><<<p.grid, p.threads, p.smem, s>>>(g, rates_t<T>(r), fin, fout, isnodes,
                                                               fprev, fnew, p.S, st);
@@ -466,7 +493,7 @@ void launch_fused_staged(const Geometry& g, const Rates& r, const T* fin, T* fou
 #define LBM_STAGED_INSTANTIATE(T)                                                            \
   template bool staged_eligible<T>(const Geometry&, int, bool);                              \
   template int staged_max_stages<T>(const Geometry&);                                        \
-  template bool plan_fused_staged<T>(const Geometry&, int, int, bool, int, StagedPlan*);     \
+  template bool plan_fused_staged<T>(const Geometry&, int, int, bool, int, StagedPlan*, bool); \
   template void launch_fused_staged<T>(const Geometry&, const Rates&, const T*, T*,          \
                                        const int32_t*, const ForceView<T>&,                  \
                                        const ForceView<T>&, const StagedPlan&, DevStatus*,   \

@@ -285,6 +285,16 @@ class LBMBox:
                  "get_variant")
         return v.value, s.value, g.value, c.value
 
+    def set_sums(self, mode: int):
+        """Arithmetic of the collision (capi.LBM_SUMS_*): FIXED (FP64 default)
+        computes the integer-coefficient moment sums exactly in fixed point."""
+        self._ck(self._L.lbm_set_sums(self._h, int(mode)), "set_sums")
+
+    def sums(self) -> int:
+        m = C.c_int(0)
+        self._ck(self._L.lbm_get_sums(self._h, C.byref(m)), "get_sums")
+        return m.value
+
     def autotune(self, reps: int = 5) -> float:
         """Time every applicable stream+collide variant on the current state
         (without advancing it), keep the fastest; returns its ms per launch."""
