@@ -75,8 +75,8 @@ struct lbm_ctx {
   double* d_kxr6 = nullptr;
   double* d_kyr5 = nullptr;
   double* d_kzr5 = nullptr;
-  double* ztab = nullptr;
-  double* ytw = nullptr;  // (cos, sin) of 2 pi ky y / ny, [5][ny]
+  void* ztab = nullptr;  // (kx, z) partial sums of the force series, population precision
+  void* ytw = nullptr;   // (cos, sin) of 2 pi ky y / ny, [5][ny], population precision
   double* ztw = nullptr;  // (cos, sin) of 2 pi kz z / nz, [5][nz]
   void* rowtab[3] = {nullptr, nullptr, nullptr};
   void* xtw = nullptr;
@@ -313,11 +313,13 @@ int pick_slot(lbm_ctx* c) {
 void launch_forcing_into(lbm_ctx* c, int slot, cudaStream_t st) {
   launch_forcing_update(c->d_forcing, c->var, c->tf, c->pi2, c->d_kxr6, c->d_kyr5, c->d_kzr5, st);
   if (c->f32)
-    launch_forcing_tables<float>(c->g, c->d_forcing, c->ytw, c->ztw,
-                                 static_cast<float*>(c->rowtab[slot]), c->ztab, st);
+    launch_forcing_tables<float>(c->g, c->d_forcing, static_cast<const float*>(c->ytw), c->ztw,
+                                 static_cast<float*>(c->rowtab[slot]),
+                                 static_cast<float*>(c->ztab), st);
   else
-    launch_forcing_tables<double>(c->g, c->d_forcing, c->ytw, c->ztw,
-                                  static_cast<double*>(c->rowtab[slot]), c->ztab, st);
+    launch_forcing_tables<double>(c->g, c->d_forcing, static_cast<const double*>(c->ytw),
+                                  c->ztw, static_cast<double*>(c->rowtab[slot]),
+                                  static_cast<double*>(c->ztab), st);
 }
 
 // FORCING: advance the stochastic state and tabulate the new field.  If the
@@ -766,8 +768,8 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
     al((void**)&ctx->d_kxr6, 16 * sizeof(double));
     al((void**)&ctx->d_kyr5, 8 * sizeof(double));
     al((void**)&ctx->d_kzr5, 8 * sizeof(double));
-    al((void**)&ctx->ztab, 45LL * g.nz * 2 * sizeof(double));
-    al((void**)&ctx->ytw, 5LL * g.ny * 2 * sizeof(double));
+    al(&ctx->ztab, 45LL * g.nz * 2 * sizeof(double));
+    al(&ctx->ytw, 5LL * g.ny * 2 * sizeof(double));
     al((void**)&ctx->ztw, 5LL * g.nz * 2 * sizeof(double));
     for (int s = 0; s < 3; ++s) al(&ctx->rowtab[s], (long long)kRowCoef * g.ny * g.nz * ctx->esz);
   }
@@ -841,7 +843,7 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
     cudaMemcpy(ctx->d_kxr6, kx6, sizeof kx6, cudaMemcpyHostToDevice);
     cudaMemcpy(ctx->d_kyr5, ky5, sizeof ky5, cudaMemcpyHostToDevice);
     cudaMemcpy(ctx->d_kzr5, kz5, sizeof kz5, cudaMemcpyHostToDevice);
-    auto twid = [&](const double* k5, int n, double* dst) {
+    auto twid = [&](const double* k5, int n, void* dst, bool f32) {
       std::vector<double> t(10 * (size_t)n);
       for (int j = 0; j < 5; ++j)
         for (int x = 0; x < n; ++x) {
@@ -851,10 +853,15 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
           t[2 * ((size_t)j * n + x)] = std::cos(ang);
           t[2 * ((size_t)j * n + x) + 1] = std::sin(ang);
         }
-      cudaMemcpy(dst, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice);
+      if (f32) {
+        std::vector<float> tf(t.begin(), t.end());
+        cudaMemcpy(dst, tf.data(), tf.size() * sizeof(float), cudaMemcpyHostToDevice);
+      } else {
+        cudaMemcpy(dst, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice);
+      }
     };
-    twid(ky5, g.ny, ctx->ytw);
-    twid(kz5, g.nz, ctx->ztw);
+    twid(ky5, g.ny, ctx->ytw, ctx->f32);
+    twid(kz5, g.nz, ctx->ztw, false);
     ForcingDev st;
     std::memset(&st, 0, sizeof st);
     st.iseedf = -cfg->iseedf;
@@ -1782,7 +1789,8 @@ int lbm_batch_create(lbm_ctx** ctxs, int n, lbm_batch** out) {
     fb.backup = c->d_forcing_backup;
     fb.var = c->var; fb.tf = c->tf; fb.pi2 = c->pi2;
     fb.kxr6 = c->d_kxr6; fb.kyr5 = c->d_kyr5; fb.kzr5 = c->d_kzr5;
-    fb.ytw = c->ytw; fb.ztw = c->ztw; fb.ztab = c->ztab;
+    fb.ytw = static_cast<const float*>(c->ytw); fb.ztw = c->ztw;
+    fb.ztab = static_cast<float*>(c->ztab);
     for (int q = 0; q < 3; ++q) fb.rowtab[q] = static_cast<float*>(c->rowtab[q]);
     b->max_nz = std::max(b->max_nz, c->g.nz);
     b->max_rows = std::max(b->max_rows, (long long)c->g.ny * c->g.nz);

@@ -445,8 +445,9 @@ __global__ void k_mass_momentum(Geometry g, const T* __restrict__ f, double* par
 // exp(+2 pi i kz z / nz); stage 2 (rowtab): B(c, kx, z, y) = sum_jy A
 // exp(+2 pi i ky y / ny).  Together with the per-x twiddles they evaluate
 // the inverse transform of gaussian.f90:557-601 at any node.
+template <typename ZT>
 __device__ __forceinline__ void k_force_ztab_body(int bx, int gx, Geometry g, const ForcingDev* st, const double* __restrict__ ztw,
-                             double* ztab) {
+                             ZT* ztab) {
   int t = bx * blockDim.x + threadIdx.x;  // over (c, kx, jy, z)
   int total = 3 * 3 * 5 * g.nz;
   if (t >= total) return;
@@ -464,20 +465,22 @@ __device__ __forceinline__ void k_force_ztab_body(int bx, int gx, Geometry g, co
     sr += cr * cs - ci * sn;
     si += cr * sn + ci * cs;
   }
-  ztab[2 * t] = sr;
-  ztab[2 * t + 1] = si;
+  // stored in the table's precision (the row sums read it without conversion)
+  ztab[2 * t] = ZT(sr);
+  ztab[2 * t + 1] = ZT(si);
 }
+template <typename ZT>
 __global__ void k_force_ztab(Geometry g, const ForcingDev* st, const double* __restrict__ ztw,
-                             double* ztab) {
-  k_force_ztab_body(blockIdx.x, gridDim.x, g, st, ztw, ztab);
+                             ZT* ztab) {
+  k_force_ztab_body<ZT>(blockIdx.x, gridDim.x, g, st, ztw, ztab);
 }
 
 // Row coefficients of the force series (kRowCoef layout) from the (kx, z)
 // table: one thread per (row, component, kx).  The kx = 1, 2 terms of the
 // real inverse transform enter twice (kx and -kx), hence the factor 2.
 template <typename T>
-__device__ __forceinline__ void k_force_rowtab_body(int bx, int gx, Geometry g, const double* __restrict__ ztab,
-                               const double* __restrict__ ytw, T* __restrict__ rowtab) {
+__device__ __forceinline__ void k_force_rowtab_body(int bx, int gx, Geometry g, const T* __restrict__ ztab,
+                               const T* __restrict__ ytw, T* __restrict__ rowtab) {
   long long t = bx * (long long)blockDim.x + threadIdx.x;  // over (c,kx,z,y)
   long long total = 9LL * g.nz * g.ny;
   if (t >= total) return;
@@ -489,8 +492,8 @@ __device__ __forceinline__ void k_force_rowtab_body(int bx, int gx, Geometry g, 
 #pragma unroll
   for (int jy = 0; jy < 5; ++jy) {
     long long ai = ((long long)(ckx * 5 + jy)) * g.nz + z;
-    T ar = T(ztab[2 * ai]), aim = T(ztab[2 * ai + 1]);
-    T cs = T(ytw[2 * (jy * g.ny + y)]), sn = T(ytw[2 * (jy * g.ny + y) + 1]);
+    T ar = ztab[2 * ai], aim = ztab[2 * ai + 1];
+    T cs = ytw[2 * (jy * g.ny + y)], sn = ytw[2 * (jy * g.ny + y) + 1];
     sr += ar * cs - aim * sn;
     si += ar * sn + aim * cs;
   }
@@ -505,8 +508,8 @@ __device__ __forceinline__ void k_force_rowtab_body(int bx, int gx, Geometry g, 
   }
 }
 template <typename T>
-__global__ void k_force_rowtab(Geometry g, const double* __restrict__ ztab,
-                               const double* __restrict__ ytw, T* __restrict__ rowtab) {
+__global__ void k_force_rowtab(Geometry g, const T* __restrict__ ztab,
+                               const T* __restrict__ ytw, T* __restrict__ rowtab) {
   k_force_rowtab_body<T>(blockIdx.x, gridDim.x, g, ztab, ytw, rowtab);
 }
 
@@ -605,7 +608,7 @@ __global__ void k_force_ztab_multi(const BoxForcing* boxes) {
   const BoxForcing& B = boxes[blockIdx.y];
   const int nblk = (45 * B.g.nz + 127) / 128;
   if ((int)blockIdx.x >= nblk) return;
-  k_force_ztab_body(blockIdx.x, nblk, B.g, B.st, B.ztw, B.ztab);
+  k_force_ztab_body<float>(blockIdx.x, nblk, B.g, B.st, B.ztw, B.ztab);
 }
 __global__ void k_force_rowtab_multi(const BoxForcing* boxes, int slot) {
   const BoxForcing& B = boxes[blockIdx.y];
@@ -628,10 +631,10 @@ void launch_forcing_multi(const BoxForcing* boxes, int nb, int max_nz, long long
 }
 
 template <typename T>
-void launch_forcing_tables(const Geometry& g, const ForcingDev* st, const double* ytw,
-                           const double* ztw, T* rowtab, double* ztab, cudaStream_t s) {
+void launch_forcing_tables(const Geometry& g, const ForcingDev* st, const T* ytw,
+                           const double* ztw, T* rowtab, T* ztab, cudaStream_t s) {
   int nz_t = 45 * g.nz;
-  { k_force_ztab<<<blocks_for(nz_t, 128), 128, 0, s>>>(g, st, ztw, ztab); count_launch(); }
+  { k_force_ztab<T><<<blocks_for(nz_t, 128), 128, 0, s>>>(g, st, ztw, ztab); count_launch(); }
   long long nr = 9LL * g.nz * g.ny;
   { k_force_rowtab<T><<<blocks_for(nr, 256), 256, 0, s>>>(g, ztab, ytw, rowtab); count_launch(); }
 }
@@ -660,8 +663,8 @@ void launch_forcing_tables(const Geometry& g, const ForcingDev* st, const double
                                       double*, double*, cudaStream_t);                      \
   template void launch_mass_momentum<T>(const Geometry&, const T*, double*, int,            \
                                         cudaStream_t);                                      \
-  template void launch_forcing_tables<T>(const Geometry&, const ForcingDev*, const double*, \
-                                         const double*, T*, double*, cudaStream_t);
+  template void launch_forcing_tables<T>(const Geometry&, const ForcingDev*, const T*, \
+                                         const double*, T*, T*, cudaStream_t);
 
 LBM_INSTANTIATE(double)
 LBM_INSTANTIATE(float)

@@ -42,27 +42,83 @@ __device__ double ran1_dev(int32_t* idum, int32_t* iy, int32_t* iv) {
 
 __device__ __forceinline__ int m655(int i, int j, int k) { return (i - 1) + 6 * (j - 1) + 30 * (k - 1); }
 
-// One block: thread 0 draws the 450 uniform numbers in the reference's
-// order (mc, k, j, i = 1,3,5; cont1 then rph), then the magnitudes,
-// phases, Ornstein-Uhlenbeck update and projection run one mode per thread.
+// a * b mod (2^31 - 1) for a, b in [1, 2^31 - 2], exact (2^31 = 1 mod m)
+__device__ __forceinline__ int32_t mulmod_m31(int32_t a, int32_t b) {
+  const unsigned long long p = (unsigned long long)(uint32_t)a * (uint32_t)b;
+  unsigned long long r = (p & 0x7fffffffULL) + (p >> 31);
+  r = (r & 0x7fffffffULL) + (r >> 31);
+  if (r >= 0x7fffffffULL) r -= 0x7fffffffULL;
+  return (int32_t)r;
+}
+
+// 16807^n mod (2^31 - 1): n steps of the generator's multiplier at once
+__device__ __forceinline__ int32_t lcg_jump(int n) {
+  int32_t r = 1, b = 16807;
+  while (n) {
+    if (n & 1) r = mulmod_m31(r, b);
+    b = mulmod_m31(b, b);
+    n >>= 1;
+  }
+  return r;
+}
+
+// One block.  The 450 uniform numbers come in the reference's order (mc, k,
+// j, i = 1,3,5; cont1 then rph).  Their multiplicative congruential part is
+// computed for all draws at once by jumping ahead (Schrage's form in ran1 is
+// the exact product 16807 idum mod 2^31-1, so the jump gives the same
+// integers); only the shuffle table's chain (iy selects the slot that the
+// next idum replaces) runs in one thread, on shared memory.  The first call
+// of a generator (idum <= 0: table initialisation) runs ran1 itself.  Then
+// the magnitudes, phases, Ornstein-Uhlenbeck update and projection run one
+// mode per thread on shared copies of the state.
 __device__ __forceinline__ void k_forcing_update_body(int bx, int gx, ForcingDev* st, double var, double tf,
                                                         double pi2, const double* kxr6,
                                                         const double* kyr5, const double* kzr5) {
   __shared__ double u[450];
   __shared__ double fr[450];
+  __shared__ double sb[450];
+  __shared__ double sa[450];
+  __shared__ int32_t lcg[450];
+  __shared__ int32_t iys[450];
+  __shared__ int32_t siv[32];
+  __shared__ int32_t sstate[2];
   const int tid = threadIdx.x;
   const double smallx = 1.0e-18;
   const double xkf = sqrt(8.0);
   const double dt = 1.0;
+  const double AM = 1.0 / 2147483647.0, RNMX = 1.0 - 1.2e-7;
+  const int32_t idum0 = st->iseedf, iy0 = st->iyf;
+  const bool init = idum0 <= 0 || iy0 == 0;  // the same in every thread
+  if (tid < 32) siv[tid] = st->ivf[tid];
+  for (int m = tid; m < 450; m += blockDim.x) sb[m] = st->b[m];
+  if (!init)
+    for (int n = tid; n < 450; n += blockDim.x) lcg[n] = mulmod_m31(idum0, lcg_jump(n + 1));
+  __syncthreads();
   if (tid == 0) {
-    int32_t idum = st->iseedf, iy = st->iyf;
-    int32_t iv[32];
-    for (int i = 0; i < 32; ++i) iv[i] = st->ivf[i];
-    for (int d = 0; d < 450; ++d) u[d] = ran1_dev(&idum, &iy, iv);
-    st->iseedf = idum;
-    st->iyf = iy;
-    for (int i = 0; i < 32; ++i) st->ivf[i] = iv[i];
+    if (init) {
+      int32_t idum = idum0, iy = iy0;
+      int32_t iv[32];
+      for (int i = 0; i < 32; ++i) iv[i] = siv[i];
+      for (int d = 0; d < 450; ++d) u[d] = ran1_dev(&idum, &iy, iv);
+      for (int i = 0; i < 32; ++i) siv[i] = iv[i];
+      sstate[0] = idum;
+      sstate[1] = iy;
+    } else {
+      // ran1's shuffle: j = iy / NDIV with NDIV = 2^26 and iy >= 1
+      int32_t iy = iy0;
+      for (int d = 0; d < 450; ++d) {
+        const int jj = iy >> 26;
+        iy = siv[jj];
+        siv[jj] = lcg[d];
+        iys[d] = iy;
+      }
+      sstate[0] = lcg[449];
+      sstate[1] = iy;
+    }
   }
+  __syncthreads();
+  if (!init)
+    for (int d = tid; d < 450; d += blockDim.x) u[d] = fmin(AM * (double)iys[d], RNMX);
   __syncthreads();
   // white noise, gaussian.f90:201-215; draw pair d <-> (mc, k, j, i)
   for (int d = tid; d < 225; d += blockDim.x) {
@@ -99,12 +155,12 @@ __device__ __forceinline__ void k_forcing_update_body(int bx, int gx, ForcingDev
     q[m655(2, 1, 1)] = 0.0;
   }
   __syncthreads();
-  double* b1 = st->b;
-  double* b2 = st->b + 150;
-  double* b3 = st->b + 300;
-  double* a1 = st->a;
-  double* a2 = st->a + 150;
-  double* a3 = st->a + 300;
+  double* b1 = sb;
+  double* b2 = sb + 150;
+  double* b3 = sb + 300;
+  double* a1 = sa;
+  double* a2 = sa + 150;
+  double* a3 = sa + 300;
   // OU update and solenoidal projection, gaussian.f90:243-274
   for (int m = tid; m < 150; m += blockDim.x) {
     int i = 1 + m % 6, j = 1 + (m / 6) % 5, k = 1 + m / 30;
@@ -128,7 +184,7 @@ __device__ __forceinline__ void k_forcing_update_body(int bx, int gx, ForcingDev
   __syncthreads();
   // gaussian.f90:277-307
   if (tid < 3) {
-    double* a = st->a + 150 * tid;
+    double* a = sa + 150 * tid;
     a[m655(1, 1, 1)] = 0.0;
     a[m655(2, 1, 1)] = 0.0;
     for (int k = 1; k <= 5; ++k) {
@@ -144,6 +200,16 @@ __device__ __forceinline__ void k_forcing_update_body(int bx, int gx, ForcingDev
       a[m655(1, 1, kk)] = a[m655(1, 1, k)];
       a[m655(2, 1, kk)] = -a[m655(2, 1, k)];
     }
+  }
+  __syncthreads();
+  for (int m = tid; m < 450; m += blockDim.x) {
+    st->b[m] = sb[m];
+    st->a[m] = sa[m];
+  }
+  if (tid < 32) st->ivf[tid] = siv[tid];
+  if (tid == 0) {
+    st->iseedf = sstate[0];
+    st->iyf = sstate[1];
   }
 }
 __global__ void __launch_bounds__(256) k_forcing_update(ForcingDev* st, double var, double tf,

@@ -225,9 +225,10 @@ void launch_forcing_update(ForcingDev* st, double var, double tf, double pi2,
                            cudaStream_t s);
 template <typename T>
 // ytw[jy][y], ztw[kz][z]: (cos, sin) of 2 pi k n / N for the five low
-// wavenumbers of each axis, tabulated once per box
-void launch_forcing_tables(const Geometry& g, const ForcingDev* st, const double* ytw,
-                           const double* ztw, T* rowtab, double* ztab, cudaStream_t s);
+// wavenumbers of each axis, tabulated once per box (ytw in the populations'
+// precision, ztw in FP64); ztab: the (kx, z) partial sums, T
+void launch_forcing_tables(const Geometry& g, const ForcingDev* st, const T* ytw,
+                           const double* ztw, T* rowtab, T* ztab, cudaStream_t s);
 
 // statistics (lbm_stats.cu): spectrum, dissipation and derivative moments
 // of statistc; per-particle slip velocity
@@ -322,8 +323,8 @@ struct BoxForcing {
   ForcingDev* backup;
   double var, tf, pi2;
   const double* kxr6; const double* kyr5; const double* kzr5;
-  const double* ytw; const double* ztw;
-  double* ztab;
+  const float* ytw; const double* ztw;
+  float* ztab;
   float* rowtab[3];
 };
 void launch_forcing_multi(const BoxForcing* boxes, int nb, int max_nz, long long max_rows,

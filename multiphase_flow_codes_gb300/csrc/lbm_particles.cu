@@ -24,6 +24,7 @@ namespace lbm {
 namespace {
 
 constexpr int PB = 256;  // threads per particle block
+constexpr int kBounceSpan = 64;  // coordinates per axis tabulated by beads_collision
 
 __device__ __forceinline__ double near_img(double c, double p, int n, int nh) {
   if ((c - p) > (double)nh) c = c - (double)n;
@@ -597,6 +598,40 @@ __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, Partic
   const R xc0 = R(pv.ypglb[3 * p]), yc0 = R(pv.ypglb[3 * p + 1]), zc0 = R(pv.ypglb[3 * p + 2]);
   const bool channel = g.channel != 0;
   const uint32_t* mask = solid_mask(isnodes, g);
+  // Per axis, the link point coordinate pnt = i + 1/2 and the image of the
+  // centre nearest to it depend on the node's coordinate i alone: tabulate
+  // them once per particle for the kBounceSpan coordinates around the
+  // centre (same operations as per link, so the same values); links outside
+  // the table compute them directly.
+  __shared__ R tpnt[3][kBounceSpan], tcen[3][kBounceSpan];
+  int lo[3];
+  {
+    const R cen[3] = {xc0, yc0, zc0};
+    const int nn[3] = {g.nx, g.ny, g.nz}, nh[3] = {g.nxh, g.nyh, g.nzh};
+    for (int a = 0; a < 3; ++a)
+      lo[a] = (int)floor((double)pv.ypglb[3 * p + a]) - (kBounceSpan / 2);
+    for (int t = threadIdx.x; t < 3 * kBounceSpan; t += PB) {
+      const int a = t / kBounceSpan, d = t - a * kBounceSpan;
+      const bool periodic = !(channel && a == 0);
+      int i = lo[a] + d;
+      if (periodic) i = ((i % nn[a]) + nn[a]) % nn[a];
+      const R pnt = R(i + 1) - R(0.5);
+      tpnt[a][d] = pnt;
+      tcen[a][d] = periodic ? near_img_t<R>(cen[a], pnt, nn[a], nh[a]) : cen[a];
+    }
+    __syncthreads();
+  }
+  auto coord = [&](int a, int i, R cen, int n, int nhalf, bool periodic, R& pnt, R& c) {
+    int d = i - lo[a];
+    if (periodic) d = d < 0 ? d + n : (d >= n ? d - n : d);
+    if (d >= 0 && d < kBounceSpan) {
+      pnt = tpnt[a][d];
+      c = tcen[a][d];
+    } else {
+      pnt = R(i + 1) - R(0.5);
+      c = periodic ? near_img_t<R>(cen, pnt, n, nhalf) : cen;
+    }
+  };
   for (int l = threadIdx.x; l < cnt; l += PB) {
     // 32-bit decode: node < 2^26
     const int cd = code[l];
@@ -607,11 +642,10 @@ __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, Partic
     const int k = r / g.ny, j = r - k * g.ny;
     R alpha = alph[l];
     int ipp = ipopp(ipop);
-    R xpnt = R(i + 1) - R(0.5), ypnt = R(j + 1) - R(0.5), zpnt = R(k + 1) - R(0.5);
-    R xc = xc0, yc = yc0, zc = zc0;
-    if (!channel) xc = near_img_t<R>(xc, xpnt, g.nx, g.nxh);
-    yc = near_img_t<R>(yc, ypnt, g.ny, g.nyh);
-    zc = near_img_t<R>(zc, zpnt, g.nz, g.nzh);
+    R xpnt, ypnt, zpnt, xc, yc, zc;
+    coord(0, i, xc0, g.nx, g.nxh, !channel, xpnt, xc);
+    coord(1, j, yc0, g.ny, g.nyh, true, ypnt, yc);
+    coord(2, k, zc0, g.nz, g.nzh, true, zpnt, zc);
     int ix = cix(ipop), iy = ciy(ipop), iz = ciz(ipop);
     int im1 = i - ix, im2 = i - 2 * ix;
     int jm1 = wrapi(j - iy, g.ny), km1 = wrapi(k - iz, g.nz);
@@ -624,14 +658,16 @@ __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, Partic
       im1 = wrapi(im1, g.nx);
       im2 = wrapi(im2, g.nx);
     }
-    R xx0 = xpnt + R(ix) * alpha - xc;
-    R yy0 = ypnt + R(iy) * alpha - yc;
-    R zz0 = zpnt + R(iz) * alpha - zc;
+    // c_a alpha with c_a in {-1, 0, 1}: exact, so selected rather than multiplied
+    auto sel = [](int c, R v) { return c == 0 ? R(0) : (c > 0 ? v : -v); };
+    R xx0 = xpnt + sel(ix, alpha) - xc;
+    R yy0 = ypnt + sel(iy, alpha) - yc;
+    R zz0 = zpnt + sel(iz, alpha) - zc;
     R ff1 = R(read_post(g, f, pushed, ipop, i, j, k));
     R uwx = w1 + omg2 * zz0 - omg3 * yy0;
     R uwy = w2 + omg3 * xx0 - omg1 * zz0;
     R uwz = w3 + omg1 * yy0 - omg2 * xx0;
-    R uwpro = uwx * R(ix) + uwy * R(iy) + uwz * R(iz);
+    R uwpro = sel(ix, uwx) + sel(iy, uwy) + sel(iz, uwz);
     const R wwp = ipop <= 6 ? R(1.0 / 18.0) : R(1.0 / 36.0);
     R f9;
     if (alpha <= 0.5) {
@@ -671,15 +707,17 @@ __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, Partic
         R c2 = R(1.0) - c1;
         f9 = c1 * ff1 + c2 * ff2 - R(6.0) * wwp * c1 * uwpro;
       } else {
-        R c1 = R(1.0) / alpha / (R(2.0) * alpha + R(1.0));
-        R c2 = (R(2.0) * alpha - R(1.0)) / alpha;
+        // 1 / alpha / (2 alpha + 1) and (2 alpha - 1) / alpha with one division
+        const R inv = R(1.0) / (alpha * (R(2.0) * alpha + R(1.0)));
+        R c1 = inv;
+        R c2 = (R(2.0) * alpha - R(1.0)) * (R(2.0) * alpha + R(1.0)) * inv;
         R c3 = R(1.0) - c1 - c2;
         f9 = c1 * ff1 + c2 * ff2 + c3 * ff3 - R(6.0) * wwp * c1 * uwpro;
       }
     }
     f9s[l] = f9;
     R dff = ff1 + f9;
-    R dxmom = dff * R(ix), dymom = dff * R(iy), dzmom = dff * R(iz);
+    R dxmom = sel(ix, dff), dymom = sel(iy, dff), dzmom = sel(iz, dff);
     acc6[0].add(dxmom);
     acc6[1].add(dymom);
     acc6[2].add(dzmom);
