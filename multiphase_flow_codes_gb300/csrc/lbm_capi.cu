@@ -69,6 +69,14 @@ struct lbm_ctx {
   StagedPlan staged;
   // arithmetic of the FP64 collision (lbm_set_sums)
   int sums = LBM_SUMS_FLOAT;
+  // FP64 fixed-point direct kernel: this step's body force per node (3 x N),
+  // kept for the next step's macroscopic velocity.  It holds the field of
+  // table slot fcache_slot as that slot stood at version fcache_version;
+  // every (re)write of a slot bumps its version.
+  double* fcache = nullptr;
+  int fcache_slot = -1;
+  unsigned long long fcache_version = 0;
+  unsigned long long slot_version[3] = {0, 0, 0};
 
   // forcing
   ForcingDev* d_forcing = nullptr;
@@ -311,6 +319,7 @@ int pick_slot(lbm_ctx* c) {
 }
 
 void launch_forcing_into(lbm_ctx* c, int slot, cudaStream_t st) {
+  ++c->slot_version[slot];
   launch_forcing_update(c->d_forcing, c->var, c->tf, c->pi2, c->d_kxr6, c->d_kyr5, c->d_kzr5, st);
   if (c->f32)
     launch_forcing_tables<float>(c->g, c->d_forcing, static_cast<const float*>(c->ytw), c->ztw,
@@ -401,15 +410,31 @@ void particle_phase(lbm_ctx* c, T* f_plain) {
   c->fcur = nf;
 }
 
-// the fused stream + collide of the selected variant, fin -> fout
+// the fused stream + collide of the selected variant, fin -> fout.
+// use_cache: a step (not a timing run) that may read and must then refresh
+// the per-node force cache of the FP64 fixed-point direct kernel.
 template <typename T>
-void launch_stream_collide(lbm_ctx* c, const T* fin, T* fout) {
-  if (c->variant == LBM_VARIANT_STAGED || c->variant == LBM_VARIANT_STAGED_X2)
+void launch_stream_collide(lbm_ctx* c, const T* fin, T* fout, bool use_cache = false) {
+  if (c->variant == LBM_VARIANT_STAGED || c->variant == LBM_VARIANT_STAGED_X2) {
     launch_fused_staged<T>(c->g, c->r, fin, fout, c->flags[c->fcur], fview<T>(c, c->fmacro),
                            fview<T>(c, c->latest), c->staged, c->status, c->stream);
-  else
-    launch_fused_step<T>(c->g, c->r, fin, fout, c->flags[c->fcur], fview<T>(c, c->fmacro),
-                         fview<T>(c, c->latest), c->sums == LBM_SUMS_FIXED, c->stream);
+    if (use_cache) c->fcache_slot = -1;
+    return;
+  }
+  int mode = 0;
+  const bool fx = !c->f32 && c->sums == LBM_SUMS_FIXED;
+  if (use_cache && fx && c->fcache && c->latest.mode == FM_TABLE) {
+    const bool hit = c->fmacro.mode == FM_TABLE && c->fmacro.slot == c->fcache_slot &&
+                     c->slot_version[c->fcache_slot] == c->fcache_version;
+    mode = hit ? 2 : 1;
+  }
+  launch_fused_step<T>(c->g, c->r, fin, fout, c->flags[c->fcur], fview<T>(c, c->fmacro),
+                       fview<T>(c, c->latest), fx, reinterpret_cast<T*>(c->fcache), mode,
+                       c->stream);
+  if (use_cache) {
+    c->fcache_slot = mode ? c->latest.slot : -1;
+    c->fcache_version = mode ? c->slot_version[c->latest.slot] : 0;
+  }
 }
 
 // plan a staged variant with `stages` stages (0: the default, four where two
@@ -462,7 +487,7 @@ void fused_step_t(lbm_ctx* c) {
   T* fin = fbuf<T>(c, c->cur);
   T* fout = fbuf<T>(c, 1 - c->cur);
   prof_begin(c);
-  launch_stream_collide<T>(c, fin, fout);
+  launch_stream_collide<T>(c, fin, fout, true);
   prof_end(c, LBM_PHASE_STREAM_COLLIDE);
   prefetch_forcing(c);
   if (c->particles_on) {
@@ -529,6 +554,7 @@ uint64_t footprint(const lbm_config& c, int64_t* cap_out) {
   if (c.forcing == LBM_FORCING_STOCHASTIC) {
     b += 3ull * kRowCoef * c.ny * c.nz * es + 45ull * c.nz * 2 * 8;  // row tables, z table
     b += 10ull * (c.ny + c.nz) * 8 + 2 * sizeof(ForcingDev) + 32 * 8;
+    if (c.precision != LBM_PREC_F32) b += 3 * N * 8;  // per-node force cache
   }
   b += 4ull * c.nx * es;
   uint64_t stage = std::min<uint64_t>(19 * N, kStagingDoubles) * 8;
@@ -772,6 +798,7 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
     al(&ctx->ytw, 5LL * g.ny * 2 * sizeof(double));
     al((void**)&ctx->ztw, 5LL * g.nz * 2 * sizeof(double));
     for (int s = 0; s < 3; ++s) al(&ctx->rowtab[s], (long long)kRowCoef * g.ny * g.nz * ctx->esz);
+    if (!ctx->f32) al((void**)&ctx->fcache, 3 * (size_t)g.N * sizeof(double));
   }
   ctx->npmax = cfg->npart_max > 0 ? cfg->npart_max : 0;
   if (ctx->npmax > 0) {
@@ -908,7 +935,7 @@ int lbm_destroy(lbm_ctx* ctx) {
                   ctx->rowtab[2], ctx->pbuf, ctx->first_move, ctx->links.code,
                   ctx->links.alpha, ctx->links.f9, ctx->links.count, ctx->links.sweeps,
                   ctx->links.sweep_ok, ctx->fill.node,
-                  ctx->fill.part, ctx->fill.count};
+                  ctx->fill.part, ctx->fill.count, ctx->fcache};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
@@ -1737,6 +1764,7 @@ int lbm_batch_create(lbm_ctx** ctxs, int n, lbm_batch** out) {
     cancel_prefetch(c);
     cudaStreamSynchronize(c->stream);
     c->in_batch = true;
+    c->fcache_slot = -1;
   }
   // boxes and tasks
   std::vector<BatchBox> boxes(n);
@@ -1851,6 +1879,7 @@ int lbm_batch_destroy(lbm_batch* b) {
       c->batch_ready = false;
     }
     c->in_batch = false;
+    c->fcache_slot = -1;
   }
   if (b->graph) cudaGraphExecDestroy(b->graph);
   for (cudaEvent_t e : b->ev_join)

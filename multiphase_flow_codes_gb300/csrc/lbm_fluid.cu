@@ -208,21 +208,55 @@ __device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >
 // (N < 2^26 is enforced at context creation).
 // FX (FP64 only): collide with exact fixed-point moment sums (collide_fx),
 // falling back to collide_fast for the nodes it declines.
+// fcache (FX only; fcache_mode 0: unused): the body force per node, three
+// component planes of N.  Mode 1 evaluates both fields from their tables;
+// mode 2 reads the previous step's field from the cache, which the previous
+// launch of this kernel wrote from the same table.  Modes 1 and 2 store this
+// step's field at every node (solid ones too: a node that becomes fluid
+// reads it next step).
 template <typename T, bool CHANNEL, bool FX = false>
-__global__ void __launch_bounds__(128) k_fused(Geometry g, RatesT<T> r, const T* __restrict__ fin,
+__global__ void __launch_bounds__(128, FX ? 4 : 1) k_fused(Geometry g, RatesT<T> r, const T* __restrict__ fin,
                                                T* __restrict__ fout,
                                                const int32_t* __restrict__ isnodes,
-                                               ForceView<T> fprev, ForceView<T> fnew) {
+                                               ForceView<T> fprev, ForceView<T> fnew,
+                                               T* fcache, int fcache_mode) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y, z = blockIdx.z;
   if (x >= g.nx) return;
   const int nx = g.nx, nxy = g.nx * g.ny, N = (int)g.N;
   const int n = x + nx * y + nxy * z;
   T f[NPOP];
+  T fp[3];
+  // the cached force is loaded with the populations (same latency)
+  if constexpr (FX) {
+    if (fcache_mode == 2) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) fp[c] = fcache[(size_t)c * N + n];
+    }
+  }
 #pragma unroll
   for (int q = 0; q < NPOP; ++q) f[q] = fin[(size_t)q * N + n];
-  if (!is_solid(solid_mask(isnodes, g), g, z * g.ny + y, x)) {
-    T fp[3], fc[3];
+  const bool solid = is_solid(solid_mask(isnodes, g), g, z * g.ny + y, x);
+  bool cached = false;
+  if constexpr (FX) {
+   if (fcache_mode != 0) {
+    cached = true;
+    T fc[3];
+    body_force(fnew, g, x, y, z, fc[0], fc[1], fc[2]);
+    if (!solid && fcache_mode != 2) body_force(fprev, g, x, y, z, fp[0], fp[1], fp[2]);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) fcache[(size_t)c * N + n] = fc[c];
+    if (!solid) {
+      if (!collide_fx(f, fp[0], fp[1], fp[2], fc[0], fc[1], fc[2], r)) {
+#pragma unroll
+        for (int q = 0; q < NPOP; ++q) f[q] = fin[(size_t)q * N + n];
+        collide_fast(f, fp[0], fp[1], fp[2], fc[0], fc[1], fc[2], r);
+      }
+    }
+   }
+  }
+  if (!cached && !solid) {
+    T fc[3];
     body_force2(fprev, fnew, x, z * g.ny + y, fp, fc);
     bool done = false;
     if constexpr (FX) {
@@ -522,23 +556,27 @@ inline unsigned blocks_for(long long n, int b) { return (unsigned)((n + b - 1) /
 template <typename T>
 void launch_fused_step(const Geometry& g, const Rates& r, const T* fin, T* fout,
                        const int32_t* isnodes, const ForceView<T>& fprev,
-                       const ForceView<T>& fnew, bool fx, cudaStream_t s) {
+                       const ForceView<T>& fnew, bool fx, T* fcache, int fcache_mode,
+                       cudaStream_t s) {
   const int B = 128;
   const RatesT<T> rt = rates_t<T>(r);
   if constexpr (sizeof(T) == 8) {
     if (fx) {
+      if (!fcache || fnew.mode != FM_TABLE) fcache_mode = 0;
       if (g.channel)
-        k_fused<T, true, true><<<row_grid(g, B), B, 0, s>>>(g, rt, fin, fout, isnodes, fprev, fnew);
+        k_fused<T, true, true><<<row_grid(g, B), B, 0, s>>>(g, rt, fin, fout, isnodes, fprev, fnew,
+                                                            fcache, fcache_mode);
       else
-        k_fused<T, false, true><<<row_grid(g, B), B, 0, s>>>(g, rt, fin, fout, isnodes, fprev, fnew);
+        k_fused<T, false, true><<<row_grid(g, B), B, 0, s>>>(g, rt, fin, fout, isnodes, fprev, fnew,
+                                                             fcache, fcache_mode);
       count_launch();
       return;
     }
   }
   if (g.channel)
-    { k_fused<T, true><<<row_grid(g, B), B, 0, s>>>(g, rt, fin, fout, isnodes, fprev, fnew); count_launch(); }
+    { k_fused<T, true><<<row_grid(g, B), B, 0, s>>>(g, rt, fin, fout, isnodes, fprev, fnew, nullptr, 0); count_launch(); }
   else
-    { k_fused<T, false><<<row_grid(g, B), B, 0, s>>>(g, rt, fin, fout, isnodes, fprev, fnew); count_launch(); }
+    { k_fused<T, false><<<row_grid(g, B), B, 0, s>>>(g, rt, fin, fout, isnodes, fprev, fnew, nullptr, 0); count_launch(); }
 }
 
 template <typename T>
@@ -642,7 +680,7 @@ void launch_forcing_tables(const Geometry& g, const ForcingDev* st, const T* ytw
 #define LBM_INSTANTIATE(T)                                                                   \
   template void launch_fused_step<T>(const Geometry&, const Rates&, const T*, T*,           \
                                      const int32_t*, const ForceView<T>&,                   \
-                                     const ForceView<T>&, bool, cudaStream_t);              \
+                                     const ForceView<T>&, bool, T*, int, cudaStream_t);     \
   template void launch_macrovar<T>(const Geometry&, const T*, const int32_t*,               \
                                    const ForceView<T>&, const ParticleView&, T*, T*, T*, T*, \
                                    cudaStream_t);                                           \

@@ -135,9 +135,12 @@ void count_launch();
 
 // fluid
 template <typename T>
+// fx: FP64 fixed-point moment sums; fcache/fcache_mode: the per-node force
+// cache of the FP64 fixed-point kernel (k_fused in lbm_fluid.cu), mode 0 off
 void launch_fused_step(const Geometry& g, const Rates& r, const T* fin, T* fout,
                        const int32_t* isnodes, const ForceView<T>& fprev,
-                       const ForceView<T>& fnew, bool fx, cudaStream_t s);
+                       const ForceView<T>& fnew, bool fx, T* fcache, int fcache_mode,
+                       cudaStream_t s);
 // the same step with its rows staged through shared memory by bulk copies
 // (lbm_staged.cu); periodic boxes with nx a multiple of 4
 struct StagedPlan {
