@@ -400,12 +400,19 @@ def main():
         peak = C.c_double(0.0)
         rc = capi.lib().lbm_fma_throughput(capi.LBM_PREC_F64, C.byref(peak))
         fp64_peak = peak.value if rc == 0 and peak.value > 0 else None
-        tf = figs[key]["fp64_flop_per_node"] * N / (sc_ms / sc_n / 1e3) / 1e12
+        per_s = N / (sc_ms / sc_n / 1e3)
+        tf = figs[key]["fp64_flop_per_node"] * per_s / 1e12
+        # the FMA probe issues one FP64 instruction per two flops
+        ti = figs[key].get("fp64_inst_per_node", 0.0) * per_s / 1e12
         fp64 = {"achieved_tflops": tf, "peak_tflops": fp64_peak,
                 "frac": tf / fp64_peak if fp64_peak else None, "unit": "TFLOP/s",
                 "flop_per_node": figs[key]["fp64_flop_per_node"],
+                "fp64_inst_per_node": figs[key].get("fp64_inst_per_node"),
+                "issue_frac": (2 * ti / fp64_peak) if (fp64_peak and ti) else None,
                 "note": "FP64 FMA peak measured live on this GPU (lbm_fma_throughput); FP64 flops "
-                        "per node from the ncu instruction counters; the FP64 kernel is FP64-issue bound"}
+                        "and instructions per node from the ncu counters; issue_frac = FP64 "
+                        "instructions per second over the probe's FMA instructions per second. "
+                        "The FP64 kernel is bound by its FP64 and integer instruction issue"}
 
     line = {"metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms / args.steps,

@@ -99,3 +99,16 @@ def run(steps: int = 500, warmup: int = 6, nboxes: int = 48, tune_reps: int = 3)
         batch.close()
         for b in boxes:
             b.close()
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser(description="time the batched ensemble")
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=6)
+    ap.add_argument("--boxes", type=int, default=48)
+    ap.add_argument("--tune-reps", type=int, default=3)
+    a = ap.parse_args()
+    print(json.dumps(run(a.steps, a.warmup, a.boxes, a.tune_reps)))

@@ -102,3 +102,29 @@ def test_fixed_sums_hand_back_out_of_range_nodes(require_gpu, oracle_mod, varian
     a, b = fxd[:, far], fld[:, far]
     assert np.abs(b).max() > 0
     assert relerr(a, b) <= 1e-13
+
+
+def test_force_cache_across_mixed_steps(require_gpu, oracle_mod):
+    """The FP64 direct kernel keeps each step's body force per node for the
+    next step's velocity.  Steps through other paths in between (the unfused
+    subroutines, the staged kernel, a timing run of the autotuner) must leave
+    no stale field behind: the run stays on the oracle's trajectory."""
+    o, box = make_pair(oracle_mod, shape=(40, 32, 36), npart=2, rad=4.0, rhopart=2.5)
+    box.set_variant(capi.LBM_VARIANT_DIRECT)
+    plan = ["fused", "fused", "unfused", "fused", "fused", "staged", "fused", "tune", "fused",
+            "fused"]
+    for what in plan:
+        if what == "unfused":
+            box.step_unfused(1)
+        elif what == "staged":
+            box.set_variant(capi.LBM_VARIANT_STAGED)
+            box.step(1)
+            box.set_variant(capi.LBM_VARIANT_DIRECT)
+        elif what == "tune":
+            box.autotune(1)
+            box.set_variant(capi.LBM_VARIANT_DIRECT)
+            box.step(1)
+        else:
+            box.step(1)
+        o.step(1)
+    assert relerr(box.get_f(), o.f) <= TOL64
