@@ -167,6 +167,13 @@ int lbm_beads_links(lbm_ctx* ctx);        /* partlib.f90:934   beads_links    */
 int lbm_beads_filling(lbm_ctx* ctx);      /* partlib.f90:2793  beads_filling  */
 int lbm_macrovar(lbm_ctx* ctx);           /* collision.f90:232 macrovar       */
 int lbm_rhoupdat(lbm_ctx* ctx);           /* collision.f90:213 rhoupdat       */
+/* The density pre-relaxation of a new run (B/main.f90:86-108, C/main.f90:
+ * 71-95): repeat collision_MRT, streaming, rhoupdat with the velocity held
+ * fixed until max|rho - rho_previous| <= eps or the iteration counter passes
+ * max_iter (the reference: rhoepsl = 1e-5, 15000).  iters: the counter at
+ * exit (the reference's printed istep); err: the last max difference.  One
+ * 8-byte read-back per iteration. */
+int lbm_prerelax(lbm_ctx* ctx, double eps, int max_iter, int* iters, double* err);
 
 /* The whole time step of main.f90:172-188, `nsteps` times, fused into a
  * short chain of kernels per step.  Leaves the same state as calling the

@@ -1391,6 +1391,36 @@ int lbm_rhoupdat(lbm_ctx* ctx) {
   return LBM_OK;
 }
 
+int lbm_prerelax(lbm_ctx* ctx, double eps, int max_iter, int* iters, double* err) {
+  if (!ctx || !(eps >= 0.0) || max_iter < 0) return LBM_ERR_ARG;
+  if (ctx->in_batch) return fail(ctx, LBM_ERR_STATE, "a batched context steps only through its batch");
+  materialize_macro(ctx);
+  unsigned long long* maxbits = reinterpret_cast<unsigned long long*>(ctx->partial);
+  int istep = 0;
+  double e = 0.0;
+  for (;;) {
+    if (int rc = lbm_collision_mrt(ctx)) return rc;
+    if (int rc = lbm_streaming(ctx)) return rc;
+    if (ctx->f32)
+      launch_rhoupdat_maxdiff<float>(ctx->g, fbuf<float>(ctx, ctx->cur), mbuf<float>(ctx, 0),
+                                     maxbits, ctx->stream);
+    else
+      launch_rhoupdat_maxdiff<double>(ctx->g, fbuf<double>(ctx, ctx->cur), mbuf<double>(ctx, 0),
+                                      maxbits, ctx->stream);
+    unsigned long long bits = 0;
+    CK(cudaMemcpyAsync(&bits, maxbits, sizeof bits, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    std::memcpy(&e, &bits, sizeof e);
+    if (!std::isfinite(e)) return fail(ctx, LBM_ERR_NONFINITE, "pre-relaxation: density not finite");
+    if (e <= eps || istep > max_iter) break;
+    ++istep;
+  }
+  ctx->macro_derived = false;
+  if (iters) *iters = istep;
+  if (err) *err = e;
+  return LBM_OK;
+}
+
 // Report a device error raised by an earlier lbm_step without blocking:
 // the status word is copied back asynchronously at the end of each call.
 static int poll_status(lbm_ctx* ctx) {

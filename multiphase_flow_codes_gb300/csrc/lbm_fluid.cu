@@ -386,6 +386,35 @@ __global__ void k_rhoupdat(Geometry g, const T* __restrict__ f, T* __restrict__ 
   rho[n] = r;
 }
 
+// rhoupdat that also reports max |rho_new - rho_old| (the pre-relaxation
+// test of B/main.f90:91-93) through an atomic max on the bits of the
+// non-negative FP64 difference (ordered like the values)
+template <typename T>
+__global__ void __launch_bounds__(256) k_rhoupdat_maxdiff(Geometry g, const T* __restrict__ f,
+                                                          T* __restrict__ rho,
+                                                          unsigned long long* maxbits) {
+  long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  double d = 0.0;
+  if (n < g.N) {
+    T r = f[n];
+#pragma unroll
+    for (int q = 1; q < NPOP; ++q) r = r + f[q * g.N + n];
+    d = fabs((double)r - (double)rho[n]);
+    if (!(d == d)) d = __longlong_as_double(0x7ff0000000000000LL);  // NaN -> +inf
+    rho[n] = r;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) d = fmax(d, __shfl_xor_sync(0xffffffffu, d, o));
+  __shared__ double wm[8];
+  if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = d;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = wm[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, wm[w]);
+    atomicMax(maxbits, (unsigned long long)__double_as_longlong(m));
+  }
+}
+
 // initpop, B/initial.f90:14-26 (rho' = 0)
 template <typename T>
 __global__ void k_initpop(Geometry g, const double* __restrict__ ux, const double* __restrict__ uy,
@@ -602,6 +631,13 @@ void launch_streaming(const Geometry& g, const T* fin, T* fout, cudaStream_t s) 
 }
 
 template <typename T>
+void launch_rhoupdat_maxdiff(const Geometry& g, const T* f, T* rho, unsigned long long* maxbits,
+                             cudaStream_t s) {
+  cudaMemsetAsync(maxbits, 0, sizeof(unsigned long long), s);
+  { k_rhoupdat_maxdiff<T><<<blocks_for(g.N, 256), 256, 0, s>>>(g, f, rho, maxbits); count_launch(); }
+}
+
+template <typename T>
 void launch_rhoupdat(const Geometry& g, const T* f, T* rho, cudaStream_t s) {
   { k_rhoupdat<T><<<blocks_for(g.N, 256), 256, 0, s>>>(g, f, rho); count_launch(); }
 }
@@ -689,6 +725,8 @@ void launch_forcing_tables(const Geometry& g, const ForcingDev* st, const T* ytw
                                     const T*, cudaStream_t);                                \
   template void launch_streaming<T>(const Geometry&, const T*, T*, cudaStream_t);           \
   template void launch_rhoupdat<T>(const Geometry&, const T*, T*, cudaStream_t);            \
+  template void launch_rhoupdat_maxdiff<T>(const Geometry&, const T*, T*, unsigned long long*, \
+                                           cudaStream_t);                                      \
   template void launch_initpop<T>(const Geometry&, const double*, const double*,            \
                                   const double*, T*, T*, cudaStream_t);                     \
   template void launch_aos_to_soa<T>(const Geometry&, const double*, T*, long long,         \

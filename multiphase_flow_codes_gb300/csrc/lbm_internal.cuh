@@ -195,6 +195,9 @@ void launch_collision(const Geometry& g, const Rates& r, T* f, const int32_t* is
 template <typename T>
 void launch_streaming(const Geometry& g, const T* fin, T* fout, cudaStream_t s);
 template <typename T>
+void launch_rhoupdat_maxdiff(const Geometry& g, const T* f, T* rho, unsigned long long* maxbits,
+                             cudaStream_t s);
+template <typename T>
 void launch_rhoupdat(const Geometry& g, const T* f, T* rho, cudaStream_t s);
 template <typename T>
 void launch_initpop(const Geometry& g, const double* ux, const double* uy,

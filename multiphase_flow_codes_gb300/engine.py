@@ -268,6 +268,14 @@ class LBMBox:
     def rhoupdat(self):
         self._ck(self._L.lbm_rhoupdat(self._h), "rhoupdat")
 
+    def prerelax(self, eps: float = 1e-5, max_iter: int = 15000) -> tuple:
+        """Density pre-relaxation of a new run (main.f90:86-108); returns
+        (iterations counter at exit, last max |rho - rho_previous|)."""
+        it, err = C.c_int(0), C.c_double(0.0)
+        self._ck(self._L.lbm_prerelax(self._h, float(eps), int(max_iter), C.byref(it),
+                                      C.byref(err)), "prerelax")
+        return it.value, err.value
+
     def step(self, nsteps: int = 1):
         """The time step of main.f90:172-188, ``nsteps`` times (fused path)."""
         self._ck(self._L.lbm_step(self._h, int(nsteps)), "step")
