@@ -138,6 +138,15 @@ int lbm_upload_particles(lbm_ctx* ctx, int npart, const double* ypglb,
 /* any pointer may be NULL; each is a (3, npart) array */
 int lbm_download_particles(lbm_ctx* ctx, double* ypglb, double* wp, double* omgp,
                            double* fHIp, double* flubp, double* torqp);
+/* The whole particle state, for checkpoints: dir 0 gets, dir 1 sets.
+ * `state` holds 15 (3, npart) Fortran arrays back to back, in var_inc's
+ * names (B/var_inc.f90:95-103): ypglb, ypglbp, wp, wpp, omgp, omgpp, dwdt,
+ * domgdt, forcep, forcepp, torqp, torqpp, thetap, fHIp, flubp.  first_move
+ * (may be NULL; 0 when NULL on set) is 1 when the next beads_move is the
+ * first after release (partlib.f90:2310).  Setting rebuilds the solid flags
+ * and links from ypglb (beads_links), as the reference's restart does after
+ * loadcntdpart (main.f90:129-132).  npart must equal the context's on get. */
+int lbm_particle_state(lbm_ctx* ctx, int dir, int npart, double* state, int32_t* first_move);
 /* ibnodes (1 solid, -1 fluid) and isnodes (particle id, -1 fluid); each
  * lx*ly*lz int32 in Fortran order; either may be NULL */
 int lbm_download_flags(lbm_ctx* ctx, int32_t* ibnodes, int32_t* isnodes);

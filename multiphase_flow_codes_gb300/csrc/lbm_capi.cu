@@ -1168,6 +1168,49 @@ int lbm_upload_particles(lbm_ctx* ctx, int npart, const double* ypglb, const dou
   return check_status(ctx);
 }
 
+int lbm_particle_state(lbm_ctx* ctx, int dir, int npart, double* state, int32_t* first_move) {
+  if (!ctx || (dir != 0 && dir != 1) || npart < 0 || (npart > 0 && !state)) return LBM_ERR_ARG;
+  if (ctx->in_batch && dir != 0)
+    return fail(ctx, LBM_ERR_STATE, "the particle state of a batched context is read-only");
+  double* vecs[15] = {ctx->ypglb, ctx->ypglbp, ctx->wp, ctx->wpp, ctx->omgp,
+                      ctx->omgpp, ctx->dwdt, ctx->domgdt, ctx->forcep, ctx->forcepp,
+                      ctx->torqp, ctx->torqpp, ctx->thetap, ctx->fHIp, ctx->flubp};
+  const size_t b = 3 * (size_t)npart * sizeof(double);
+  if (dir == 0) {
+    if (npart != ctx->npart) return fail(ctx, LBM_ERR_ARG, "npart differs from the context's");
+    for (int i = 0; i < 15 && npart > 0; ++i)
+      CK(cudaMemcpyAsync(state + (size_t)i * 3 * npart, vecs[i], b, cudaMemcpyDeviceToHost,
+                         ctx->stream));
+    int fm = 0;
+    if (ctx->first_move)
+      CK(cudaMemcpyAsync(&fm, ctx->first_move, sizeof fm, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (first_move) *first_move = fm;
+    return LBM_OK;
+  }
+  if (npart > ctx->npmax) return fail(ctx, LBM_ERR_ARG, "npart above the context's capacity");
+  materialize_macro(ctx);
+  if (ctx->npmax > 0)
+    CK(cudaMemsetAsync(ctx->pbuf, 0, 15 * 3 * (size_t)ctx->npmax * sizeof(double), ctx->stream));
+  for (int i = 0; i < 15 && npart > 0; ++i)
+    CK(cudaMemcpyAsync(vecs[i], state + (size_t)i * 3 * npart, b, cudaMemcpyHostToDevice,
+                       ctx->stream));
+  if (ctx->first_move) {
+    const int fm = first_move ? *first_move : 0;
+    CK(cudaMemcpyAsync(ctx->first_move, &fm, sizeof fm, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));  // fm lives on this stack frame
+  }
+  ctx->npart = npart;
+  CK(reset_flags(ctx, 0));
+  CK(reset_flags(ctx, 1));
+  ctx->particles_on = npart > 0;
+  if (npart > 0)
+    launch_links(ctx->g, pview(ctx), ctx->flags[ctx->fcur], ctx->links, ctx->status, ctx->f32,
+                 ctx->stream);
+  CK(cudaGetLastError());
+  return check_status(ctx);
+}
+
 int lbm_download_particles(lbm_ctx* ctx, double* ypglb, double* wp, double* omgp, double* fHIp,
                            double* flubp, double* torqp) {
   if (!ctx) return LBM_ERR_ARG;

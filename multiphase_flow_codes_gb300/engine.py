@@ -196,6 +196,35 @@ class LBMBox:
                 "download_particles")
         return arrs
 
+    # the 15 (3, npart) vectors of var_inc, in lbm_particle_state's order
+    PARTICLE_VECTORS = ("ypglb", "ypglbp", "wp", "wpp", "omgp", "omgpp", "dwdt", "domgdt",
+                        "forcep", "forcepp", "torqp", "torqpp", "thetap", "fHIp", "flubp")
+
+    def get_particle_state(self) -> dict:
+        """Every particle vector, (npart, 3) each, and 'first_move'."""
+        n = max(self.npart, 0)
+        buf = np.zeros((15, n, 3))
+        fm = C.c_int32(0)
+        self._ck(self._L.lbm_particle_state(self._h, 0, n, dptr(buf), C.byref(fm)),
+                 "particle_state")
+        out = {k: buf[i].copy() for i, k in enumerate(self.PARTICLE_VECTORS)}
+        out["first_move"] = int(fm.value)
+        return out
+
+    def set_particle_state(self, state: dict, first_move: int = 0):
+        """Set the particle vectors given in `state` (others zero) and rebuild
+        the flags and links from ypglb."""
+        y = np.asarray(state["ypglb"], dtype=np.float64).reshape(-1, 3)
+        n = y.shape[0]
+        buf = np.zeros((15, n, 3))
+        for i, k in enumerate(self.PARTICLE_VECTORS):
+            if k in state:
+                buf[i] = np.asarray(state[k], dtype=np.float64).reshape(n, 3)
+        fm = C.c_int32(int(first_move))
+        self._ck(self._L.lbm_particle_state(self._h, 1, n, dptr(buf), C.byref(fm)),
+                 "particle_state")
+        self.npart = n
+
     def get_flags(self):
         ib = np.empty((self.nz, self.ny, self.nx), dtype=np.int32)
         isn = np.empty((self.nz, self.ny, self.nx), dtype=np.int32)

@@ -56,6 +56,8 @@ def lib() -> C.CDLL:
         L.orc_initpartpos.argtypes = [P, C.c_int]
         L.orc_release.argtypes = [P, C.c_int]
         L.orc_release.restype = None
+        L.orc_restore.argtypes = [P, C.c_int]
+        L.orc_restore.restype = None
         L.orc_step.argtypes = [P, C.c_int]
         L.orc_ran1_sequence.argtypes = [C.c_int32, C.c_int, C.POINTER(C.c_double)]
         L.orc_ran1_sequence.restype = None
@@ -165,6 +167,24 @@ class OracleBox:
         self.wp[:n] = 0.0 if wp is None else wp
         self.omgp[:n] = 0.0 if omgp is None else omgp
         self._L.orc_release(self._h, n)
+
+    def restore_particles(self, state: dict):
+        """Restart: set every (3, npart) particle vector (names as var_inc),
+        then rebuild the flags and links (B/main.f90:129-132)."""
+        n = int(np.asarray(state["ypglb"]).reshape(-1, 3).shape[0])
+        for k in self.PART:
+            if k in state:
+                getattr(self, k)[:n] = np.asarray(state[k]).reshape(n, 3)
+        self._L.orc_restore(self._h, n)
+
+    def set_forcing_state(self, iseedf: int, iyf: int, ivf, b):
+        self._view("iseedf", np.int32, (1,))[0] = iseedf
+        self._view("iyf", np.int32, (1,))[0] = iyf
+        self.ivf[:] = np.asarray(ivf, dtype=np.int32)
+        b = np.asarray(b, dtype=np.float64).reshape(450)
+        self.b1r[:] = b[:150]
+        self.b2r[:] = b[150:300]
+        self.b3r[:] = b[300:]
 
     def step(self, nsteps: int = 1) -> int:
         return self._L.orc_step(self._h, nsteps)

@@ -643,6 +643,16 @@ struct Oracle {
     beads_links();
   }
 
+  // restart with particles (B/main.f90:129-132): the state vectors were set
+  // from a checkpoint; rebuild the flags and links, the next move is not the
+  // first after release
+  void restore(int np) {
+    npart = np;
+    particles_on = np > 0;
+    first_move = false;
+    if (np > 0) beads_links();
+  }
+
   // beads_links, B/partlib.f90:934-1058 (channel: C/partlib.f90:939-1058)
   void beads_links() {
     std::fill(ilink.begin(), ilink.end(), -1);
@@ -1117,6 +1127,7 @@ void orc_initpop(void* h) { static_cast<Oracle*>(h)->initpop(); }
 int orc_initpartpos(void* h, int np) { return static_cast<Oracle*>(h)->initpartpos(np); }
 // positions already in ypglb (set through orc_field), velocities in wp/omgp
 void orc_release(void* h, int np) { static_cast<Oracle*>(h)->release(np); }
+void orc_restore(void* h, int np) { static_cast<Oracle*>(h)->restore(np); }
 int orc_step(void* h, int nsteps) {
   Oracle* o = static_cast<Oracle*>(h);
   for (int s = 0; s < nsteps; ++s) {
