@@ -227,6 +227,19 @@ int lbm_statistics(lbm_ctx* ctx, int nek, double* ek, double* dk, double* out);
  * rigid-body velocity once macrovar fills the solid nodes, so the slip is
  * taken on a fluid shell instead.)  No counterpart in the reference. */
 int lbm_particle_slip(lbm_ctx* ctx, double r_in, double r_out, double* slip);
+/* rmsstat (B/saveload.f90:1530-1730): the columns of rms.dat after the time,
+ * out[36] = nf, nf/nx^3, mean u (3), rms u (3), velfrms, velfmn, mean wp (3),
+ * rms wp (3), velprms, velpmn, mean vorticity (3), rms vorticity (3),
+ * omgfrms/2, omgfmn, mean omgp (3), rms omgp (3), omgprms, omgpmn,
+ * omgfrms^2, velfrms^2.  Fluid statistics over the nodes with isnodes < 0;
+ * the vorticity is vortcalc's spectral curl with integer wavenumbers (the
+ * Nyquist modes dropped); particle columns are 0 before release; omgpmn
+ * takes the x mean twice as the reference does. */
+int lbm_rmsstat(lbm_ctx* ctx, double* out);
+/* diag (B/saveload.f90:1342-1400) without the time: out[5] = max |u| over
+ * fluid nodes, idwp (1-based, first of equal maxima; 0 without particles),
+ * max |wp|, idomgp, max |omgp|. */
+int lbm_diag(lbm_ctx* ctx, double* out);
 
 /* ---- kernel selection (no counterpart in the reference) ------------------ */
 /* Variants of the fused stream + collide kernel of lbm_step.  Both compute

@@ -99,6 +99,8 @@ SIGNATURES = {
     "lbm_beads_filling": (C.c_int, [_P]),
     "lbm_macrovar": (C.c_int, [_P]),
     "lbm_rhoupdat": (C.c_int, [_P]),
+    "lbm_rmsstat": (C.c_int, [_P, _D]),
+    "lbm_diag": (C.c_int, [_P, _D]),
     "lbm_particle_state": (C.c_int, [_P, C.c_int, C.c_int, _D, C.POINTER(C.c_int32)]),
     "lbm_prerelax": (C.c_int, [_P, C.c_double, C.c_int, C.POINTER(C.c_int), _D]),
     "lbm_step": (C.c_int, [_P, C.c_int]),

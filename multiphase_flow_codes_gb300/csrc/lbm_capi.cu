@@ -1104,6 +1104,107 @@ int lbm_statistics(lbm_ctx* ctx, int nek, double* ek, double* dk, double* out) {
   return LBM_OK;
 }
 
+// mean and rms of one component of (3, n) particle vectors, summed in index
+// order as the reference's sum() over a vector
+static void part_mean_rms(const std::vector<double>& v, int n, int c, double* mn, double* rms) {
+  double s = 0.0;
+  for (int p = 0; p < n; ++p) s += v[3 * p + c];
+  *mn = s / (double)n;
+  double q = 0.0;
+  for (int p = 0; p < n; ++p) q += (v[3 * p + c] - *mn) * (v[3 * p + c] - *mn);
+  *rms = std::sqrt(q / (double)n);
+}
+
+int lbm_rmsstat(lbm_ctx* ctx, double* out) {
+  if (!ctx || !out) return LBM_ERR_ARG;
+  if (int rc = poll_status(ctx)) return rc;
+  materialize_macro(ctx);
+  double fl[13];
+  int rc = ctx->f32 ? fluid_rms_stats<float>(ctx->g, ctx->flags[ctx->fcur], mbuf<float>(ctx, 1),
+                                             mbuf<float>(ctx, 2), mbuf<float>(ctx, 3), &ctx->spec,
+                                             fl, ctx->stream)
+                    : fluid_rms_stats<double>(ctx->g, ctx->flags[ctx->fcur], mbuf<double>(ctx, 1),
+                                              mbuf<double>(ctx, 2), mbuf<double>(ctx, 3),
+                                              &ctx->spec, fl, ctx->stream);
+  if (rc) {
+    cudaGetLastError();
+    return fail(ctx, rc, "rmsstat: FFT or allocation failed");
+  }
+  const double nf = fl[0];
+  const double nx3 = (double)ctx->g.nx * ctx->g.nx * ctx->g.nx;  // real(nx**3), saveload.f90:1712
+  double wmn[3] = {0, 0, 0}, wrms[3] = {0, 0, 0}, omn[3] = {0, 0, 0}, orms[3] = {0, 0, 0};
+  const int np = ctx->particles_on ? ctx->npart : 0;
+  if (np > 0) {
+    std::vector<double> wp(3 * (size_t)np), om(3 * (size_t)np);
+    CK(cudaMemcpyAsync(wp.data(), ctx->wp, wp.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaMemcpyAsync(om.data(), ctx->omgp, om.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (int c = 0; c < 3; ++c) {
+      part_mean_rms(wp, np, c, &wmn[c], &wrms[c]);
+      part_mean_rms(om, np, c, &omn[c], &orms[c]);
+    }
+  }
+  auto norm = [](double a, double b, double c) { return std::sqrt(a * a + b * b + c * c); };
+  const double velfrms = norm(fl[4], fl[5], fl[6]);
+  const double omgfrms = norm(fl[10], fl[11], fl[12]);
+  double o[36] = {nf, nf / nx3,
+                  fl[1], fl[2], fl[3], fl[4], fl[5], fl[6], velfrms, norm(fl[1], fl[2], fl[3]),
+                  wmn[0], wmn[1], wmn[2], wrms[0], wrms[1], wrms[2], norm(wrms[0], wrms[1], wrms[2]),
+                  norm(wmn[0], wmn[1], wmn[2]),
+                  fl[7], fl[8], fl[9], fl[10], fl[11], fl[12], omgfrms / 2.0, norm(fl[7], fl[8], fl[9]),
+                  omn[0], omn[1], omn[2], orms[0], orms[1], orms[2], norm(orms[0], orms[1], orms[2]),
+                  // saveload.f90:1694 takes omgpxmn twice
+                  norm(omn[0], omn[1], omn[0]),
+                  omgfrms * omgfrms, velfrms * velfrms};
+  std::memcpy(out, o, sizeof o);
+  CK(cudaGetLastError());
+  return LBM_OK;
+}
+
+int lbm_diag(lbm_ctx* ctx, double* out) {
+  if (!ctx || !out) return LBM_ERR_ARG;
+  if (int rc = poll_status(ctx)) return rc;
+  materialize_macro(ctx);
+  double vmax = 0.0;
+  int rc = ctx->f32 ? fluid_vmax<float>(ctx->g, ctx->flags[ctx->fcur], mbuf<float>(ctx, 1),
+                                        mbuf<float>(ctx, 2), mbuf<float>(ctx, 3), &ctx->spec,
+                                        &vmax, ctx->stream)
+                    : fluid_vmax<double>(ctx->g, ctx->flags[ctx->fcur], mbuf<double>(ctx, 1),
+                                         mbuf<double>(ctx, 2), mbuf<double>(ctx, 3), &ctx->spec,
+                                         &vmax, ctx->stream);
+  if (rc) {
+    cudaGetLastError();
+    return fail(ctx, rc, "diag: reduction failed");
+  }
+  double o[5] = {vmax, 0.0, 0.0, 0.0, 0.0};
+  const int np = ctx->particles_on ? ctx->npart : 0;
+  if (np > 0) {
+    std::vector<double> wp(3 * (size_t)np), om(3 * (size_t)np);
+    CK(cudaMemcpyAsync(wp.data(), ctx->wp, wp.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaMemcpyAsync(om.data(), ctx->omgp, om.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    // maxval and the first maxloc (1-based) of the magnitudes
+    for (int which = 0; which < 2; ++which) {
+      const std::vector<double>& v = which ? om : wp;
+      double best = -1.0;
+      int at = 0;
+      for (int p = 0; p < np; ++p) {
+        const double m = std::sqrt(v[3 * p] * v[3 * p] + v[3 * p + 1] * v[3 * p + 1] +
+                                   v[3 * p + 2] * v[3 * p + 2]);
+        if (m > best) { best = m; at = p + 1; }
+      }
+      o[1 + 2 * which] = at;
+      o[2 + 2 * which] = best;
+    }
+  }
+  std::memcpy(out, o, sizeof o);
+  return LBM_OK;
+}
+
 int lbm_particle_slip(lbm_ctx* ctx, double r_in, double r_out, double* slip) {
   if (!ctx || !slip || !(r_out > r_in) || r_in < 0.0) return LBM_ERR_ARG;
   if (ctx->npart <= 0) return LBM_OK;

@@ -240,6 +240,16 @@ void launch_forcing_tables(const Geometry& g, const ForcingDev* st, const T* ytw
 // of statistc; per-particle slip velocity
 struct SpectrumWork;
 void spectrum_free(SpectrumWork* w);
+// rmsstat's fluid part (B/saveload.f90:1530-1730): out[0] fluid node count,
+// out[1..3] mean u, out[4..6] rms u, out[7..9] mean vorticity, out[10..12]
+// rms vorticity, all over fluid nodes (isnodes < 0)
+template <typename T>
+int fluid_rms_stats(const Geometry& g, const int32_t* isnodes, const T* ux, const T* uy,
+                    const T* uz, SpectrumWork** pw, double* out, cudaStream_t s);
+// diag's max |u| over fluid nodes (B/saveload.f90:1357-1361)
+template <typename T>
+int fluid_vmax(const Geometry& g, const int32_t* isnodes, const T* ux, const T* uy, const T* uz,
+               SpectrumWork** pw, double* vmax, cudaStream_t s);
 template <typename T>
 int spectrum_stats(const Geometry& g, double visc, const T* ux, const T* uy, const T* uz,
                    SpectrumWork** work, int nek_out, double* ek, double* dk, double* out,

@@ -21,6 +21,7 @@
 #include <cub/cub.cuh>
 #include <cufft.h>
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -338,7 +339,7 @@ struct SpectrumWork {
   int32_t* perm = nullptr;    // modes of shells 1..nek, sorted by shell
   long long nperm = 0;
   int32_t* offsets = nullptr; // nek + 1 segment offsets
-  double* terms = nullptr;    // 3 N scratch (shell terms, moment terms)
+  double* terms = nullptr;    // 4 N scratch (shell, moment and masked terms)
   double* sums = nullptr;     // results
   void* cub_tmp = nullptr;
   size_t cub_bytes = 0;
@@ -401,7 +402,7 @@ static int spectrum_setup(const Geometry& g, SpectrumWork** pw) {
       !al((void**)&w->spec, 3 * nc * sizeof(double2)) ||
       !al((void**)&w->perm, perm.size() * sizeof(int32_t)) ||
       !al((void**)&w->offsets, off.size() * sizeof(int32_t)) ||
-      !al((void**)&w->terms, 3 * N * sizeof(double)) ||
+      !al((void**)&w->terms, 4 * N * sizeof(double)) ||
       !al((void**)&w->sums, (2 * (size_t)w->nek + 8) * sizeof(double)))
     return LBM_ERR_NOMEM;
   cudaMemcpy(w->perm, perm.data(), perm.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
@@ -410,7 +411,9 @@ static int spectrum_setup(const Geometry& g, SpectrumWork** pw) {
   cub::DeviceSegmentedReduce::Sum(nullptr, b1, w->terms, w->sums, w->nek, w->offsets,
                                   w->offsets + 1);
   cub::DeviceReduce::Sum(nullptr, b2, w->terms, w->sums, N);
-  w->cub_bytes = b1 > b2 ? b1 : b2;
+  size_t b3 = 0;
+  cub::DeviceReduce::Max(nullptr, b3, w->terms, w->sums, N);
+  w->cub_bytes = std::max(b1, std::max(b2, b3));
   if (!al(&w->cub_tmp, w->cub_bytes)) return LBM_ERR_NOMEM;
   return cudaGetLastError() == cudaSuccess ? LBM_OK : LBM_ERR_CUDA;
 }
@@ -483,6 +486,149 @@ int spectrum_stats(const Geometry& g, double visc, const T* ux, const T* uy, con
   return LBM_OK;
 }
 
+// ---- rmsstat and diag (B/saveload.f90:1530-1730, 1342-1400) --------------
+
+// fluid-masked terms of three fields: pass 0 the values (and a 1 per fluid
+// node in t[3]), pass 1 the squared deviations from the means
+__global__ void k_masked_terms(long long n, const int32_t* __restrict__ isnodes,
+                               const double* __restrict__ a, const double* __restrict__ b,
+                               const double* __restrict__ c, double ma, double mb, double mc,
+                               int pass, double* __restrict__ t) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const bool fluid = isnodes[i] < 0;
+  if (pass == 0) {
+    t[i] = fluid ? a[i] : 0.0;
+    t[n + i] = fluid ? b[i] : 0.0;
+    t[2 * n + i] = fluid ? c[i] : 0.0;
+    t[3 * n + i] = fluid ? 1.0 : 0.0;
+  } else {
+    const double da = a[i] - ma, db = b[i] - mb, dc = c[i] - mc;
+    t[i] = fluid ? da * da : 0.0;
+    t[n + i] = fluid ? db * db : 0.0;
+    t[2 * n + i] = fluid ? dc * dc : 0.0;
+  }
+}
+
+// vorticity o = curl u from the spectrum: i k x u^ (integer k as vortcalc
+// uses, B/saveload.f90:3411-3450; Nyquist dropped as in k_derivative),
+// normalised by 1/N for the unnormalised inverse
+__global__ void k_curl(int nx, int ny, int nz, double2* vx, double2* vy, double2* vz,
+                       double inv_n) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int nxc = nx / 2 + 1;
+  const long long total = (long long)nxc * ny * nz;
+  if (t >= total) return;
+  const int kxi = (int)(t % nxc);
+  const long long r = t / nxc;
+  const int kyi = signed_k((int)(r % ny), ny), kzi = signed_k((int)(r / ny), nz);
+  const double kx = 2 * kxi == nx ? 0 : kxi, ky = 2 * kyi == ny ? 0 : kyi,
+               kz = 2 * kzi == nz ? 0 : kzi;
+  const double2 a = vx[t], b = vy[t], c = vz[t];
+  // w = k x u (complex), then times i: (re, im) -> (-im, re)
+  const double2 wx = make_double2(ky * c.x - kz * b.x, ky * c.y - kz * b.y);
+  const double2 wy = make_double2(kz * a.x - kx * c.x, kz * a.y - kx * c.y);
+  const double2 wz = make_double2(kx * b.x - ky * a.x, kx * b.y - ky * a.y);
+  vx[t] = make_double2(-wx.y * inv_n, wx.x * inv_n);
+  vy[t] = make_double2(-wy.y * inv_n, wy.x * inv_n);
+  vz[t] = make_double2(-wz.y * inv_n, wz.x * inv_n);
+}
+
+// |u| at fluid nodes, 0 at solid ones (diag's vel)
+template <typename T>
+__global__ void k_speed(long long n, const int32_t* __restrict__ isnodes, const T* __restrict__ ux,
+                        const T* __restrict__ uy, const T* __restrict__ uz, double* __restrict__ v) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double a = ux[i], b = uy[i], c = uz[i];
+  v[i] = isnodes[i] >= 0 ? 0.0 : sqrt(a * a + b * b + c * c);
+}
+
+// masked mean and rms of three double fields into m[3], rms[3]; nf counted
+static int masked_mean_rms(SpectrumWork* w, long long N, const int32_t* isnodes, const double* a,
+                           const double* b, const double* c, double* m, double* rms, long long* nf,
+                           cudaStream_t s) {
+  double h[4];
+  k_masked_terms<<<blocks(N, 256), 256, 0, s>>>(N, isnodes, a, b, c, 0, 0, 0, 0, w->terms);
+  count_launch();
+  for (int k = 0; k < 4; ++k) {
+    size_t bb = w->cub_bytes;
+    cub::DeviceReduce::Sum(w->cub_tmp, bb, w->terms + k * N, w->sums + k, N, s);
+  }
+  if (cudaMemcpyAsync(h, w->sums, sizeof h, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return LBM_ERR_CUDA;
+  const long long n = (long long)h[3];
+  *nf = n;
+  for (int k = 0; k < 3; ++k) m[k] = n > 0 ? h[k] / (double)n : 0.0;
+  k_masked_terms<<<blocks(N, 256), 256, 0, s>>>(N, isnodes, a, b, c, m[0], m[1], m[2], 1, w->terms);
+  count_launch();
+  for (int k = 0; k < 3; ++k) {
+    size_t bb = w->cub_bytes;
+    cub::DeviceReduce::Sum(w->cub_tmp, bb, w->terms + k * N, w->sums + k, N, s);
+  }
+  if (cudaMemcpyAsync(h, w->sums, 3 * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return LBM_ERR_CUDA;
+  for (int k = 0; k < 3; ++k) rms[k] = n > 0 ? sqrt(h[k] / (double)n) : 0.0;
+  return LBM_OK;
+}
+
+template <typename T>
+int fluid_rms_stats(const Geometry& g, const int32_t* isnodes, const T* ux, const T* uy,
+                    const T* uz, SpectrumWork** pw, double* out, cudaStream_t s) {
+  if (int rc = spectrum_setup(g, pw)) return rc;
+  SpectrumWork* w = *pw;
+  const long long N = g.N;
+  const long long nc = (long long)(g.nx / 2 + 1) * g.ny * g.nz;
+  const T* u[3] = {ux, uy, uz};
+  for (int a = 0; a < 3; ++a) {
+    k_to_double<T><<<blocks(N, 256), 256, 0, s>>>(u[a], w->real + a * N, N);
+    count_launch();
+  }
+  long long nf = 0;
+  double um[3], ur[3], om[3], orr[3];
+  if (int rc = masked_mean_rms(w, N, isnodes, w->real, w->real + N, w->real + 2 * N, um, ur, &nf, s))
+    return rc;
+  // vortcalc: the whole velocity field, solid nodes included
+  cufftSetStream(w->fwd, s);
+  cufftSetStream(w->inv, s);
+  for (int a = 0; a < 3; ++a)
+    if (cufftExecD2Z(w->fwd, w->real + a * N, w->spec + a * nc) != CUFFT_SUCCESS) return LBM_ERR_CUDA;
+  k_curl<<<blocks(nc, 256), 256, 0, s>>>(g.nx, g.ny, g.nz, w->spec, w->spec + nc, w->spec + 2 * nc,
+                                         1.0 / (double)N);
+  count_launch();
+  for (int a = 0; a < 3; ++a)
+    if (cufftExecZ2D(w->inv, w->spec + a * nc, w->real + a * N) != CUFFT_SUCCESS) return LBM_ERR_CUDA;
+  long long nf2 = 0;
+  if (int rc = masked_mean_rms(w, N, isnodes, w->real, w->real + N, w->real + 2 * N, om, orr, &nf2, s))
+    return rc;
+  out[0] = (double)nf;
+  for (int k = 0; k < 3; ++k) {
+    out[1 + k] = um[k];
+    out[4 + k] = ur[k];
+    out[7 + k] = om[k];
+    out[10 + k] = orr[k];
+  }
+  return LBM_OK;
+}
+
+template <typename T>
+int fluid_vmax(const Geometry& g, const int32_t* isnodes, const T* ux, const T* uy, const T* uz,
+               SpectrumWork** pw, double* vmax, cudaStream_t s) {
+  if (int rc = spectrum_setup(g, pw)) return rc;
+  SpectrumWork* w = *pw;
+  const long long N = g.N;
+  k_speed<T><<<blocks(N, 256), 256, 0, s>>>(N, isnodes, ux, uy, uz, w->terms);
+  count_launch();
+  size_t bb = w->cub_bytes;
+  cub::DeviceReduce::Max(w->cub_tmp, bb, w->terms, w->sums, N, s);
+  if (cudaMemcpyAsync(vmax, w->sums, sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return LBM_ERR_CUDA;
+  return LBM_OK;
+}
+
 template <typename T>
 void launch_slip(const Geometry& g, const ParticleView& pv, const T* ux, const T* uy, const T* uz,
                  const int32_t* isnodes, double r_in, double r_out, double* slip, cudaStream_t s) {
@@ -494,6 +640,10 @@ void launch_slip(const Geometry& g, const ParticleView& pv, const T* ux, const T
 #define LBM_STATS_INSTANTIATE(T)                                                              \
   template int spectrum_stats<T>(const Geometry&, double, const T*, const T*, const T*,       \
                                  SpectrumWork**, int, double*, double*, double*, cudaStream_t); \
+  template int fluid_rms_stats<T>(const Geometry&, const int32_t*, const T*, const T*,        \
+                                  const T*, SpectrumWork**, double*, cudaStream_t);           \
+  template int fluid_vmax<T>(const Geometry&, const int32_t*, const T*, const T*, const T*,    \
+                             SpectrumWork**, double*, cudaStream_t);                          \
   template void launch_slip<T>(const Geometry&, const ParticleView&, const T*, const T*,      \
                                const T*, const int32_t*, double, double, double*, cudaStream_t); \
   template void launch_summary<T>(const T*, long long, const T*, const T*, const T*, double*,  \

@@ -176,6 +176,25 @@ class LBMBox:
                      "particle_slip")
         return out
 
+    RMS_COLUMNS = ("nf", "portionf", "uxmn", "uymn", "uzmn", "uxrms", "uyrms", "uzrms", "velfrms",
+                   "velfmn", "wpxmn", "wpymn", "wpzmn", "wpxrms", "wpyrms", "wpzrms", "velprms",
+                   "velpmn", "oxmn", "oymn", "ozmn", "oxrms", "oyrms", "ozrms", "omgfrms_half",
+                   "omgfmn", "omgpxmn", "omgpymn", "omgpzmn", "omgpxrms", "omgpyrms", "omgpzrms",
+                   "omgprms", "omgpmn", "omgfrms2", "velfrms2")
+
+    def rmsstat(self) -> dict:
+        """rmsstat's columns (saveload.f90:1530-1730) by name."""
+        out = np.zeros(36)
+        self._ck(self._L.lbm_rmsstat(self._h, dptr(out)), "rmsstat")
+        return dict(zip(self.RMS_COLUMNS, out.tolist()))
+
+    def diag(self) -> dict:
+        """diag's columns (saveload.f90:1342-1400)."""
+        out = np.zeros(5)
+        self._ck(self._L.lbm_diag(self._h, dptr(out)), "diag")
+        return {"vmax": out[0], "idwp": int(out[1]), "wpmax": out[2], "idomgp": int(out[3]),
+                "omgpmax": out[4]}
+
     # ---- particles -------------------------------------------------------
     def release_particles(self, ypglb: np.ndarray, wp: np.ndarray | None = None,
                           omgp: np.ndarray | None = None):

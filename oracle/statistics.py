@@ -78,3 +78,62 @@ def particle_slip(ux, uy, uz, isnodes, ypglb, wp, r_in, r_out, channel=False):
         cnt = max(int(m.sum()), 1)
         out[p] = np.asarray(wp[p]) - np.array([ux[m].sum(), uy[m].sum(), uz[m].sum()]) / cnt
     return out
+
+
+def vorticity(ux, uy, uz):
+    """vortcalc (saveload.f90:3411-3450): the spectral curl with integer
+    wavenumbers, Nyquist modes dropped; fields (nz, ny, nx)."""
+    nz, ny, nx = ux.shape
+    v = [np.fft.rfftn(u, axes=(0, 1, 2)) for u in (ux, uy, uz)]
+    kx = np.arange(nx // 2 + 1)[None, None, :]
+    ky = _signed(ny)[None, :, None]
+    kz = _signed(nz)[:, None, None]
+    kx = np.where(2 * kx == nx, 0, kx)
+    ky = np.where(2 * ky == ny, 0, ky)
+    kz = np.where(2 * kz == nz, 0, kz)
+    wx = 1j * (ky * v[2] - kz * v[1])
+    wy = 1j * (kz * v[0] - kx * v[2])
+    wz = 1j * (kx * v[1] - ky * v[0])
+    return tuple(np.fft.irfftn(w, s=(nz, ny, nx), axes=(0, 1, 2)) for w in (wx, wy, wz))
+
+
+def rmsstat(ux, uy, uz, isnodes, wp=None, omgp=None):
+    """The 36 columns of rms.dat after the time (saveload.f90:1530-1730)."""
+    nz, ny, nx = ux.shape
+    fl = np.asarray(isnodes) < 0
+    nf = int(fl.sum())
+
+    def mean_rms(a, b, c):
+        m = [x[fl].sum() / nf for x in (a, b, c)]
+        r = [np.sqrt(((x - mx) ** 2)[fl].sum() / nf) for x, mx in zip((a, b, c), m)]
+        return m, r
+
+    um, ur = mean_rms(ux, uy, uz)
+    om, orr = mean_rms(*vorticity(ux, uy, uz))
+    norm = lambda a, b, c: np.sqrt(a * a + b * b + c * c)
+    if wp is not None and len(wp):
+        wp = np.asarray(wp).reshape(-1, 3)
+        omgp = np.asarray(omgp).reshape(-1, 3)
+        n = wp.shape[0]
+        wm = [wp[:, c].sum() / n for c in range(3)]
+        wr = [np.sqrt(((wp[:, c] - wm[c]) ** 2).sum() / n) for c in range(3)]
+        pm = [omgp[:, c].sum() / n for c in range(3)]
+        pr = [np.sqrt(((omgp[:, c] - pm[c]) ** 2).sum() / n) for c in range(3)]
+    else:
+        wm = wr = pm = pr = [0.0, 0.0, 0.0]
+    velfrms, omgfrms = norm(*ur), norm(*orr)
+    return np.array([nf, nf / float(nx ** 3), *um, *ur, velfrms, norm(*um), *wm, *wr, norm(*wr),
+                     norm(*wm), *om, *orr, omgfrms / 2.0, norm(*om), *pm, *pr, norm(*pr),
+                     norm(pm[0], pm[1], pm[0]), omgfrms ** 2, velfrms ** 2])
+
+
+def diag(ux, uy, uz, isnodes, wp=None, omgp=None):
+    """diag's columns after the time (saveload.f90:1342-1400)."""
+    vel = np.sqrt(ux * ux + uy * uy + uz * uz)
+    vel = np.where(np.asarray(isnodes) >= 0, 0.0, vel)
+    out = [float(vel.max()), 0, 0.0, 0, 0.0]
+    if wp is not None and len(wp):
+        wm = np.sqrt((np.asarray(wp).reshape(-1, 3) ** 2).sum(axis=1))
+        om = np.sqrt((np.asarray(omgp).reshape(-1, 3) ** 2).sum(axis=1))
+        out[1:] = [int(np.argmax(wm)) + 1, float(wm.max()), int(np.argmax(om)) + 1, float(om.max())]
+    return out
