@@ -240,6 +240,15 @@ int lbm_rmsstat(lbm_ctx* ctx, double* out);
  * fluid nodes, idwp (1-based, first of equal maxima; 0 without particles),
  * max |wp|, idomgp, max |omgp|. */
 int lbm_diag(lbm_ctx* ctx, double* out);
+/* The channel's wall-normal profiles, statistc (fluid_only 0, 13 columns)
+ * and statistc2 (fluid_only 1, 15 columns) of C/saveload.f90:1136-1428: per
+ * x-plane i = 1..nx, out[(i-1)*ncol + c] = x = i - 1/2, y+, mean u, v, w /
+ * ustar, their variances, the stresses uw, uv, vw, mean rho / ustar^2, its
+ * variance, and (statistc2) the fluid and solid area fractions.  statistc
+ * averages over the whole plane, statistc2 over its fluid nodes.  ustar <= 0:
+ * from the channel force, force_y = 2 rho0 ustar^2 / nx (C/para.f90:15-17);
+ * y+ uses ystar = visc / ustar. */
+int lbm_channel_profiles(lbm_ctx* ctx, int fluid_only, double ustar, double* out);
 
 /* ---- kernel selection (no counterpart in the reference) ------------------ */
 /* Variants of the fused stream + collide kernel of lbm_step.  Both compute

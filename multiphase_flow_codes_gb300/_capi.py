@@ -101,6 +101,7 @@ SIGNATURES = {
     "lbm_rhoupdat": (C.c_int, [_P]),
     "lbm_rmsstat": (C.c_int, [_P, _D]),
     "lbm_diag": (C.c_int, [_P, _D]),
+    "lbm_channel_profiles": (C.c_int, [_P, C.c_int, C.c_double, _D]),
     "lbm_particle_state": (C.c_int, [_P, C.c_int, C.c_int, _D, C.POINTER(C.c_int32)]),
     "lbm_prerelax": (C.c_int, [_P, C.c_double, C.c_int, C.POINTER(C.c_int), _D]),
     "lbm_step": (C.c_int, [_P, C.c_int]),

@@ -1163,6 +1163,60 @@ int lbm_rmsstat(lbm_ctx* ctx, double* out) {
   return LBM_OK;
 }
 
+int lbm_channel_profiles(lbm_ctx* ctx, int fluid_only, double ustar, double* out) {
+  if (!ctx || !out) return LBM_ERR_ARG;
+  if (int rc = poll_status(ctx)) return rc;
+  if (!(ustar > 0.0)) {
+    // force_in_y = 2 rho0 ustar^2 / nx (C/para.f90:15-17)
+    const double fy = ctx->cfg.force_y;
+    if (!(fy > 0.0)) return fail(ctx, LBM_ERR_ARG, "profiles: ustar not given and no channel force");
+    ustar = std::sqrt(fy * ctx->g.nx / (2.0 * ctx->cfg.rho0));
+  }
+  materialize_macro(ctx);
+  const int nx = ctx->g.nx;
+  std::vector<double> sm((size_t)nx * 12);
+  int rc = ctx->f32 ? plane_sums<float>(ctx->g, ctx->flags[ctx->fcur], fluid_only ? 1 : 0,
+                                        mbuf<float>(ctx, 0), mbuf<float>(ctx, 1), mbuf<float>(ctx, 2),
+                                        mbuf<float>(ctx, 3), sm.data(), ctx->stream)
+                    : plane_sums<double>(ctx->g, ctx->flags[ctx->fcur], fluid_only ? 1 : 0,
+                                         mbuf<double>(ctx, 0), mbuf<double>(ctx, 1),
+                                         mbuf<double>(ctx, 2), mbuf<double>(ctx, 3), sm.data(),
+                                         ctx->stream);
+  if (rc) {
+    cudaGetLastError();
+    return fail(ctx, rc, "profiles: reduction failed");
+  }
+  const double ystar = ctx->cfg.visc / ustar;  // C/para.f90:18
+  const int lxh = nx / 2;
+  const double nyz = (double)ctx->g.ny * ctx->g.nz;
+  const int ncol = fluid_only ? 15 : 13;
+  for (int i = 1; i <= nx; ++i) {
+    const double* a = &sm[(size_t)(i - 1) * 12];
+    // statistc divides by ny*nz, statistc2 by the plane's fluid count
+    const double cnt = fluid_only ? a[11] : nyz;
+    const double u = a[0] / cnt / ustar, v = a[1] / cnt / ustar, w = a[2] / cnt / ustar;
+    const double us2 = ustar * ustar;
+    double* o = out + (size_t)(i - 1) * ncol;
+    o[0] = (double)i - 0.5;
+    o[1] = i > lxh ? ((double)(nx - i) + 0.5) / ystar : ((double)i - 0.5) / ystar;
+    o[2] = u; o[3] = v; o[4] = w;
+    o[5] = a[6] / cnt / us2 - u * u;
+    o[6] = a[7] / cnt / us2 - v * v;
+    o[7] = a[8] / cnt / us2 - w * w;
+    o[8] = a[3] / cnt / us2 - u * w;
+    o[9] = a[4] / cnt / us2 - u * v;
+    o[10] = a[5] / cnt / us2 - v * w;
+    const double pm = a[9] / cnt / us2;
+    o[11] = pm;
+    o[12] = a[10] / cnt / (us2 * us2) - pm * pm;
+    if (fluid_only) {
+      o[13] = a[11] / nyz;
+      o[14] = 1.0 - o[13];
+    }
+  }
+  return LBM_OK;
+}
+
 int lbm_diag(lbm_ctx* ctx, double* out) {
   if (!ctx || !out) return LBM_ERR_ARG;
   if (int rc = poll_status(ctx)) return rc;

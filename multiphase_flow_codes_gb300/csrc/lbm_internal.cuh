@@ -246,6 +246,11 @@ void spectrum_free(SpectrumWork* w);
 template <typename T>
 int fluid_rms_stats(const Geometry& g, const int32_t* isnodes, const T* ux, const T* uy,
                     const T* uz, SpectrumWork** pw, double* out, cudaStream_t s);
+// per x-plane sums over (y, z) (nx x 12: u, v, w, uw, uv, vw, uu, vv, ww,
+// rho, rho^2, count), all nodes or fluid nodes only
+template <typename T>
+int plane_sums(const Geometry& g, const int32_t* isnodes, int fluid_only, const T* rho,
+               const T* ux, const T* uy, const T* uz, double* sums, cudaStream_t s);
 // diag's max |u| over fluid nodes (B/saveload.f90:1357-1361)
 template <typename T>
 int fluid_vmax(const Geometry& g, const int32_t* isnodes, const T* ux, const T* uy, const T* uz,

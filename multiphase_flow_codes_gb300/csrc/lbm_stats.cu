@@ -629,6 +629,70 @@ int fluid_vmax(const Geometry& g, const int32_t* isnodes, const T* ux, const T* 
   return LBM_OK;
 }
 
+// ---- wall-normal profiles of the channel's statistc / statistc2
+// (C/saveload.f90:1136-1428): per x-plane sums over (y, z) of u, u_a u_b,
+// rho, rho^2 and the fluid count.  Threads run along x (coalesced), blocks
+// over chunks of kProfRows (y, z) rows; a second kernel adds the chunks in
+// chunk order (deterministic).
+constexpr int kProfRows = 64;
+constexpr int kProfQ = 12;  // ux uy uz uxuz uxuy uyuz ux2 uy2 uz2 rho rho2 count
+
+template <typename T>
+__global__ void k_profile_partial(Geometry g, const int32_t* __restrict__ isnodes, int fluid_only,
+                                  const T* __restrict__ rho, const T* __restrict__ ux,
+                                  const T* __restrict__ uy, const T* __restrict__ uz,
+                                  double* __restrict__ part) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= g.nx) return;
+  const int nrows = g.ny * g.nz;
+  const int r0 = blockIdx.y * kProfRows, r1 = min(nrows, r0 + kProfRows);
+  double a[kProfQ];
+#pragma unroll
+  for (int q = 0; q < kProfQ; ++q) a[q] = 0.0;
+  for (int r = r0; r < r1; ++r) {
+    const long long n = (long long)r * g.nx + x;
+    if (fluid_only && isnodes[n] >= 0) continue;
+    const double u = ux[n], v = uy[n], w = uz[n], p = rho[n];
+    a[0] += u; a[1] += v; a[2] += w;
+    a[3] += u * w; a[4] += u * v; a[5] += v * w;
+    a[6] += u * u; a[7] += v * v; a[8] += w * w;
+    a[9] += p; a[10] += p * p; a[11] += 1.0;
+  }
+  double* o = part + ((long long)blockIdx.y * g.nx + x) * kProfQ;
+#pragma unroll
+  for (int q = 0; q < kProfQ; ++q) o[q] = a[q];
+}
+
+__global__ void k_profile_sum(int nx, int nchunks, const double* __restrict__ part,
+                              double* __restrict__ out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;  // (x, q)
+  if (t >= nx * kProfQ) return;
+  double s = 0.0;
+  for (int c = 0; c < nchunks; ++c) s += part[(long long)c * nx * kProfQ + t];
+  out[t] = s;
+}
+
+template <typename T>
+int plane_sums(const Geometry& g, const int32_t* isnodes, int fluid_only, const T* rho,
+               const T* ux, const T* uy, const T* uz, double* sums, cudaStream_t s) {
+  const int nrows = g.ny * g.nz;
+  const int nchunks = (nrows + kProfRows - 1) / kProfRows;
+  double* d = nullptr;
+  const size_t np = (size_t)nchunks * g.nx * kProfQ;
+  if (cudaMalloc((void**)&d, (np + (size_t)g.nx * kProfQ) * sizeof(double)) != cudaSuccess)
+    return LBM_ERR_NOMEM;
+  k_profile_partial<T><<<dim3((g.nx + 127) / 128, nchunks), 128, 0, s>>>(g, isnodes, fluid_only, rho,
+                                                                          ux, uy, uz, d);
+  count_launch();
+  k_profile_sum<<<blocks((long long)g.nx * kProfQ, 256), 256, 0, s>>>(g.nx, nchunks, d, d + np);
+  count_launch();
+  cudaError_t e = cudaMemcpyAsync(sums, d + np, (size_t)g.nx * kProfQ * sizeof(double),
+                                  cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(d);
+  return e == cudaSuccess ? LBM_OK : LBM_ERR_CUDA;
+}
+
 template <typename T>
 void launch_slip(const Geometry& g, const ParticleView& pv, const T* ux, const T* uy, const T* uz,
                  const int32_t* isnodes, double r_in, double r_out, double* slip, cudaStream_t s) {
@@ -644,6 +708,8 @@ void launch_slip(const Geometry& g, const ParticleView& pv, const T* ux, const T
                                   const T*, SpectrumWork**, double*, cudaStream_t);           \
   template int fluid_vmax<T>(const Geometry&, const int32_t*, const T*, const T*, const T*,    \
                              SpectrumWork**, double*, cudaStream_t);                          \
+  template int plane_sums<T>(const Geometry&, const int32_t*, int, const T*, const T*,        \
+                             const T*, const T*, double*, cudaStream_t);                      \
   template void launch_slip<T>(const Geometry&, const ParticleView&, const T*, const T*,      \
                                const T*, const int32_t*, double, double, double*, cudaStream_t); \
   template void launch_summary<T>(const T*, long long, const T*, const T*, const T*, double*,  \

@@ -188,6 +188,15 @@ class LBMBox:
         self._ck(self._L.lbm_rmsstat(self._h, dptr(out)), "rmsstat")
         return dict(zip(self.RMS_COLUMNS, out.tolist()))
 
+    def channel_profiles(self, fluid_only: bool = False, ustar: float = 0.0) -> np.ndarray:
+        """statistc / statistc2 profiles of the channel (C/saveload.f90:1136-1428):
+        (nx, 13) or (nx, 15) rows of profiles.dat / profiles2.dat."""
+        ncol = 15 if fluid_only else 13
+        out = np.zeros((self.nx, ncol))
+        self._ck(self._L.lbm_channel_profiles(self._h, int(bool(fluid_only)), float(ustar), dptr(out)),
+                 "channel_profiles")
+        return out
+
     def diag(self) -> dict:
         """diag's columns (saveload.f90:1342-1400)."""
         out = np.zeros(5)

@@ -137,3 +137,31 @@ def diag(ux, uy, uz, isnodes, wp=None, omgp=None):
         om = np.sqrt((np.asarray(omgp).reshape(-1, 3) ** 2).sum(axis=1))
         out[1:] = [int(np.argmax(wm)) + 1, float(wm.max()), int(np.argmax(om)) + 1, float(om.max())]
     return out
+
+
+def channel_profiles(rho, ux, uy, uz, isnodes, ustar, visc, fluid_only=False):
+    """statistc / statistc2 of the channel (C/saveload.f90:1136-1428); fields
+    (nz, ny, nx), rows per x-plane."""
+    nz, ny, nx = ux.shape
+    ystar = visc / ustar
+    rows = []
+    fl = np.asarray(isnodes) < 0
+    for i in range(1, nx + 1):
+        sl = (slice(None), slice(None), i - 1)
+        m = fl[sl] if fluid_only else np.ones((nz, ny), dtype=bool)
+        cnt = float(m.sum()) if fluid_only else float(ny * nz)
+        S = lambda a: a[sl][m].sum()
+        u, v, w = S(ux) / cnt / ustar, S(uy) / cnt / ustar, S(uz) / cnt / ustar
+        us2 = ustar * ustar
+        pm = S(rho) / cnt / us2
+        yplus = ((nx - i) + 0.5) / ystar if i > nx // 2 else (i - 0.5) / ystar
+        row = [i - 0.5, yplus, u, v, w,
+               S(ux * ux) / cnt / us2 - u * u, S(uy * uy) / cnt / us2 - v * v,
+               S(uz * uz) / cnt / us2 - w * w,
+               S(ux * uz) / cnt / us2 - u * w, S(ux * uy) / cnt / us2 - u * v,
+               S(uy * uz) / cnt / us2 - v * w,
+               pm, S(rho * rho) / cnt / us2 ** 2 - pm * pm]
+        if fluid_only:
+            row += [cnt / (ny * nz), 1.0 - cnt / (ny * nz)]
+        rows.append(row)
+    return np.array(rows)
