@@ -2,6 +2,8 @@
 // kernels: relaxation coefficients, the MRT collision with Guo forcing in
 // moment space, and the direct evaluation of the low-wavenumber body force.
 #pragma once
+#include <cmath>
+
 #include "lbm_internal.cuh"
 
 namespace lbm {
@@ -29,7 +31,22 @@ struct RatesT {
   T B8, H8;                // meq8, mF8 = 2 e8
   T B9, H9;                // meq9 = omegxx meq8, mF9 = -e8
   T B10, H10;              // meq10..12 = u_a u_b, mF = F_a u_b + F_b u_a
+  // the same factors of the terms linear in the populations as exact
+  // fixed-point integers c * 2^sh (FP64 fixed-point collision, collide_fx):
+  // [1..15] A_k, [16] B1r, [17] B2r, [18] 1/19
+  long long Li[19];
+  int Lsh[19];
 };
+
+// c as (integer m, shift sh) with c = m * 2^-sh exactly and |m| in
+// [2^61, 2^62) (m = 0, sh = 64 for c = 0)
+inline void fixed_factor(double c, long long* m, int* sh) {
+  if (c == 0.0) { *m = 0; *sh = 64; return; }
+  int e = 0;
+  std::frexp(c, &e);  // |c| in [2^(e-1), 2^e)
+  *sh = 62 - e;
+  *m = (long long)std::ldexp(c, *sh);  // exact: 53 significant bits
+}
 
 template <typename T>
 RatesT<T> rates_t(const Rates& r) {
@@ -50,6 +67,10 @@ RatesT<T> rates_t(const Rates& r) {
   o.B8 = T(Bk(8)); o.H8 = T(2.0 * Hk(8));
   o.B9 = T(r.omegxx * Bk(9)); o.H9 = T(-Hk(9));
   o.B10 = T(Bk(10)); o.H10 = T(Hk(10));
+  for (int k = 0; k < 16; ++k) fixed_factor(ck[k] * (1.0 - sk[k]), &o.Li[k], &o.Lsh[k]);
+  fixed_factor(-11.0 * Bk(1), &o.Li[16], &o.Lsh[16]);
+  fixed_factor(r.omegepsl * Bk(2), &o.Li[17], &o.Lsh[17]);
+  fixed_factor(1.0 / 19.0, &o.Li[18], &o.Lsh[18]);
   return o;
 }
 
@@ -265,9 +286,27 @@ __host__ __device__ __forceinline__ double fx_to(long long v) {
 }
 
 
-// Same arithmetic as collide_fast (same operands, same FP64 products); only
-// the integer-coefficient sums are exact.  Returns false, leaving f as it
-// was, when a value is out of the fixed-point ranges.
+// round(v * m * 2^-sh_total) with v a fixed-point value (scale 2^-kFxIn),
+// (m, sh) a fixed_factor, the result at scale 2^-kFxOut: one exact 128-bit
+// product and one rounding
+__host__ __device__ __forceinline__ long long fx_mul(long long v, long long m, int sh) {
+  const int s = sh + kFxIn - kFxOut;  // >= 1: |c| < 2^58
+  const __int128 p = (__int128)v * (__int128)m + ((__int128)1 << (s - 1));
+  return (long long)(p >> s);
+}
+
+// |x| < 2^(kFxOutMax) at scale 2^-kFxOut
+__host__ __device__ __forceinline__ unsigned fx_out_of_range(long long x) {
+  const unsigned long long lim = 1ULL << (kFxOut + kFxOutMax);
+  return (unsigned)((unsigned long long)(x + (long long)lim) >= 2 * lim);
+}
+
+// The collision of collide_fast with the integer-coefficient sums of both
+// transforms exact in fixed point, and the terms linear in the populations
+// (A_k m_k, the density terms of meq1, meq2 and rho / 19) as exact integer
+// products rounded once (RatesT::Li); only the terms with velocities and
+// forces stay FP64.  Returns false, leaving f as it was, when a value is
+// out of the fixed-point ranges.
 __host__ __device__ __forceinline__ bool collide_fx(double (&f)[NPOP], double fpx, double fpy,
                                                     double fpz, double fx, double fy, double fz,
                                                     const RatesT<double>& r) {
@@ -296,26 +335,20 @@ __host__ __device__ __forceinline__ bool collide_fx(double (&f)[NPOP], double fp
   const I C = s1112 - s1314, Dd = s1516 - s1718;
   const I sum5 = C + Dd;
   const I sum7 = a3 + a5, sum8 = Sxy + Sxz, sum10 = a3 - a5, sum11 = Sxy - Sxz;
-  const double rho = fx_to<kFxIn>(g[0] + sum1 + sum2);
-  const double jx = fx_to<kFxIn>(d1 + sum3), jy = fx_to<kFxIn>(d3 + sum4),
-               jz = fx_to<kFxIn>(d5 + sum5);
-  const double ev1 = fx_to<kFxIn>(-30 * g[0] - 11 * sum1 + 8 * sum2);
-  const double ev2 = fx_to<kFxIn>(12 * g[0] - 4 * sum1 + sum2);
-  const double ev3 = fx_to<kFxIn>(-4 * d1 + sum3);
-  const double ev4 = fx_to<kFxIn>(-4 * d3 + sum4);
-  const double ev5 = fx_to<kFxIn>(-4 * d5 + sum5);
-  const double ev6 = fx_to<kFxIn>(2 * (a1 - Syz) - sum7 + sum8);
-  const double ev7 = fx_to<kFxIn>(-4 * a1 + 2 * (sum7 - Syz) + sum8);
-  const double ev8 = fx_to<kFxIn>(sum10 + sum11);
-  const double ev9 = fx_to<kFxIn>(-2 * sum10 + sum11);
-  const double ev10 = fx_to<kFxIn>(d78 - d910);
-  const double ev11 = fx_to<kFxIn>(d1516 - d1718);
-  const double ev12 = fx_to<kFxIn>(d1112 - d1314);
-  const double ev13 = fx_to<kFxIn>(D1 - D2);
-  const double ev14 = fx_to<kFxIn>(Bv - A);
-  const double ev15 = fx_to<kFxIn>(C - Dd);
+  const I rho = g[0] + sum1 + sum2;
+  const I ev1 = -30 * g[0] - 11 * sum1 + 8 * sum2;
+  const I ev2 = 12 * g[0] - 4 * sum1 + sum2;
+  const I ev3 = -4 * d1 + sum3;
+  const I ev4 = -4 * d3 + sum4;
+  const I ev5 = -4 * d5 + sum5;
+  const I ev6 = 2 * (a1 - Syz) - sum7 + sum8;
+  const I ev7 = -4 * a1 + 2 * (sum7 - Syz) + sum8;
+  const I ev8 = sum10 + sum11;
+  const I ev9 = -2 * sum10 + sum11;
   // macrovar: u = sum c f + F_prev / 2
-  const double ux = jx + 0.5 * fpx, uy = jy + 0.5 * fpy, uz = jz + 0.5 * fpz;
+  const double ux = fx_to<kFxIn>(d1 + sum3) + 0.5 * fpx;
+  const double uy = fx_to<kFxIn>(d3 + sum4) + 0.5 * fpy;
+  const double uz = fx_to<kFxIn>(d5 + sum5) + 0.5 * fpz;
 
   // equilibrium and forcing moments, FP64 (collision.f90:66-81)
   const double uxs = ux * ux, uys = uy * uy, uzs = uz * uz;
@@ -327,31 +360,36 @@ __host__ __device__ __forceinline__ bool collide_fx(double (&f)[NPOP], double fp
   const double e6 = 2.0 * fa - fb - fc;
   const double e8 = fb - fc;
 
-  // scaled post-collision moments (collision.f90:138-157), then fixed point
+  // scaled post-collision moments (collision.f90:138-157): the linear part
+  // as integer products, the rest converted from FP64
+  auto L = [&](int k, I v) { return fx_mul(v, r.Li[k], r.Lsh[k]); };
+  auto F = [&](double x) { return fx_from<kFxOut, 60 - kFxOut>(x, bad, big); };
   I M[16];
-  M[1] = fx_from<kFxOut, kFxOutMax>(r.A[1] * ev1 + r.B1r * rho + r.B1t * t1 + r.H1 * G3, bad, big);
-  M[2] = fx_from<kFxOut, kFxOutMax>(r.A[2] * ev2 + r.B2r * rho + r.B2t * t1 + r.H2 * G3, bad, big);
-  M[3] = fx_from<kFxOut, kFxOutMax>(r.A[3] * ev3 + r.B3 * ux + r.H3 * fx, bad, big);
-  M[4] = fx_from<kFxOut, kFxOutMax>(r.A[4] * ev4 + r.B3 * uy + r.H3 * fy, bad, big);
-  M[5] = fx_from<kFxOut, kFxOutMax>(r.A[5] * ev5 + r.B3 * uz + r.H3 * fz, bad, big);
-  M[6] = fx_from<kFxOut, kFxOutMax>(r.A[6] * ev6 + r.B6 * eq6 + r.H6 * e6, bad, big);
-  M[7] = fx_from<kFxOut, kFxOutMax>(r.A[7] * ev7 + r.B7 * eq6 + r.H7 * e6, bad, big);
-  M[8] = fx_from<kFxOut, kFxOutMax>(r.A[8] * ev8 + r.B8 * eq8 + r.H8 * e8, bad, big);
-  M[9] = fx_from<kFxOut, kFxOutMax>(r.A[9] * ev9 + r.B9 * eq8 + r.H9 * e8, bad, big);
-  M[10] = fx_from<kFxOut, kFxOutMax>(
-      r.A[10] * ev10 + uy * (r.B10 * ux + r.H10 * fx) + r.H10 * fy * ux, bad, big);
-  M[11] = fx_from<kFxOut, kFxOutMax>(
-      r.A[11] * ev11 + uz * (r.B10 * uy + r.H10 * fy) + r.H10 * fz * uy, bad, big);
-  M[12] = fx_from<kFxOut, kFxOutMax>(
-      r.A[12] * ev12 + uz * (r.B10 * ux + r.H10 * fx) + r.H10 * fz * ux, bad, big);
-  M[13] = fx_from<kFxOut, kFxOutMax>(r.A[13] * ev13, bad, big);
-  M[14] = fx_from<kFxOut, kFxOutMax>(r.A[14] * ev14, bad, big);
-  M[15] = fx_from<kFxOut, kFxOutMax>(r.A[15] * ev15, bad, big);
-  const I tl1 = fx_from<kFxOut, kFxOutMax>((1.0 / 19.0) * rho, bad, big);
-  const I tl6 = fx_from<kFxOut, kFxOutMax>(0.1 * ux + 0.05 * fx, bad, big);
-  const I tl8 = fx_from<kFxOut, kFxOutMax>(0.1 * uy + 0.05 * fy, bad, big);
-  const I tl10 = fx_from<kFxOut, kFxOutMax>(0.1 * uz + 0.05 * fz, bad, big);
-  if (bad) return false;
+  M[1] = L(1, ev1) + L(16, rho) + F(r.B1t * t1 + r.H1 * G3);
+  M[2] = L(2, ev2) + L(17, rho) + F(r.B2t * t1 + r.H2 * G3);
+  M[3] = L(3, ev3) + F(r.B3 * ux + r.H3 * fx);
+  M[4] = L(4, ev4) + F(r.B3 * uy + r.H3 * fy);
+  M[5] = L(5, ev5) + F(r.B3 * uz + r.H3 * fz);
+  M[6] = L(6, ev6) + F(r.B6 * eq6 + r.H6 * e6);
+  M[7] = L(7, ev7) + F(r.B7 * eq6 + r.H7 * e6);
+  M[8] = L(8, ev8) + F(r.B8 * eq8 + r.H8 * e8);
+  M[9] = L(9, ev9) + F(r.B9 * eq8 + r.H9 * e8);
+  M[10] = L(10, d78 - d910) + F(uy * (r.B10 * ux + r.H10 * fx) + r.H10 * fy * ux);
+  M[11] = L(11, d1516 - d1718) + F(uz * (r.B10 * uy + r.H10 * fy) + r.H10 * fz * uy);
+  M[12] = L(12, d1112 - d1314) + F(uz * (r.B10 * ux + r.H10 * fx) + r.H10 * fz * ux);
+  M[13] = L(13, D1 - D2);
+  M[14] = L(14, Bv - A);
+  M[15] = L(15, C - Dd);
+  const I tl1 = L(18, rho);
+  const I tl6 = F(0.1 * ux + 0.05 * fx);
+  const I tl8 = F(0.1 * uy + 0.05 * fy);
+  const I tl10 = F(0.1 * uz + 0.05 * fz);
+  unsigned out = bad;
+#pragma unroll
+  for (int k = 1; k < 16; ++k) out |= fx_out_of_range(M[k]);
+  out |= fx_out_of_range(tl1) | fx_out_of_range(tl6) | fx_out_of_range(tl8) |
+         fx_out_of_range(tl10);
+  if (out) return false;
 
   // inverse transform, exact (collision.f90:160-200)
   I h[NPOP];
