@@ -244,45 +244,44 @@ constexpr int kFxOut = 61, kFxOutMax = -5;  // scaled moments, inverse transform
 // precision through the FP64 path (fixed point resolves 2^-61 absolute)
 constexpr int kFxMinExp = -12;
 
-template <int K, int MAXEXP>
-__host__ __device__ __forceinline__ long long fx_from(double x, unsigned& bad, unsigned& big) {
-  static_assert(64 - K - MAXEXP >= 2, "fixed-point range");
+// x -> round(x * 2^K) (half away from zero); emax collects the largest
+// biased exponent seen (the caller tests the range once for all values).
+// Values below 2^(-K-1) (zero, subnormals) give 0.
+template <int K>
+__host__ __device__ __forceinline__ long long fx_from(double x, int& emax) {
   unsigned long long b;
   memcpy(&b, &x, 8);
-  const int e = (int)((b >> 52) & 0x7ff);
-  bad |= (unsigned)(e >= 1023 + MAXEXP);  // |x| >= 2^MAXEXP, inf, nan
-  big |= (unsigned)(e >= 1023 + kFxMinExp);
+  const int e = (int)(b >> 52) & 0x7ff;
+  emax = emax > e ? emax : e;
   // magnitude with the hidden bit at bit 63: |x| = m * 2^(e - 1086)
   const unsigned long long m = (b << 11) | 0x8000000000000000ULL;
-  // |x| * 2^K = m * 2^-(1086 - K - e); round half up on the magnitude
-  const int r = 1086 - K - e;  // >= 2 under the range test; zero/subnormal: > 64
-  const int rr = (r < 64 ? r : 64) - 1;
-  unsigned long long v = ((m >> rr) + 1) >> 1;
-  if (r > 64 || bad) v = 0;
-  return (b >> 63) ? -(long long)v : (long long)v;
+  // |x| * 2^K = m * 2^-(1086 - K - e): shift by one less, add the half, shift
+  const int r1 = 1085 - K - e;  // >= 0 inside the range
+  const unsigned long long v = ((unsigned)r1 >= 64u ? 0ULL : (m >> r1) + 1) >> 1;
+  const long long sg = (long long)b >> 63;  // 0 or -1
+  return ((long long)v ^ sg) - sg;
 }
 
+// v * 2^-K as a double, rounded to nearest (ties away from zero)
 template <int K>
 __host__ __device__ __forceinline__ double fx_to(long long v) {
-  if (v == 0) return 0.0;
-  const unsigned long long s = v < 0 ? 1ULL : 0ULL;
-  unsigned long long a = s ? 0ULL - (unsigned long long)v : (unsigned long long)v;
+  const long long sg = v >> 63;
+  unsigned long long a = (unsigned long long)((v ^ sg) - sg);
 #ifdef __CUDA_ARCH__
   const int lz = __clzll((long long)a);
 #else
-  const int lz = __builtin_clzll(a);
+  const int lz = a ? __builtin_clzll(a) : 64;
 #endif
-  a <<= lz;  // leading one at bit 63
-  unsigned long long mant = a >> 11;  // 53 bits with the hidden one
-  const unsigned rem = (unsigned)(a & 0x7ff);
-  mant += (unsigned long long)((rem > 0x400u) | ((rem == 0x400u) & (unsigned)(mant & 1)));
-  // value in [2^(63-lz-K), 2^(64-lz-K)); a mantissa carry to 2^53 adds one
+  a = lz >= 64 ? 0ULL : a << lz;  // leading one at bit 63
+  // 53 bits with the hidden one, rounded on bit 10; a carry to 2^53 adds one
   // to the exponent field through the sum below
-  const unsigned long long E = (unsigned long long)(63 - lz - K + 1023);
-  const unsigned long long bits = (s << 63) | (((E - 1) << 52) + mant);
+  const unsigned long long mant = (a >> 11) + ((a >> 10) & 1ULL);
+  const unsigned long long E = (unsigned long long)(1086 - K - lz);  // biased exponent
+  const unsigned long long bits =
+      ((unsigned long long)sg << 63) | (((E - 1) << 52) + mant);
   double d;
   memcpy(&d, &bits, 8);
-  return d;
+  return a ? d : 0.0;
 }
 
 
@@ -311,11 +310,12 @@ __host__ __device__ __forceinline__ bool collide_fx(double (&f)[NPOP], double fp
                                                     double fpz, double fx, double fy, double fz,
                                                     const RatesT<double>& r) {
   typedef long long I;
-  unsigned bad = 0, big = 0;
+  int emax = 0;
   I g[NPOP];
 #pragma unroll
-  for (int q = 0; q < NPOP; ++q) g[q] = fx_from<kFxIn, kFxInMax>(f[q], bad, big);
-  if (bad || !big) return false;
+  for (int q = 0; q < NPOP; ++q) g[q] = fx_from<kFxIn>(f[q], emax);
+  if (emax >= 1023 + kFxInMax || emax < 1023 + kFxMinExp) return false;
+  emax = 0;
   // forward transform, exact (collision.f90:101-118; grouping as collide_fast)
   const I a1 = g[1] + g[2], d1 = g[1] - g[2];
   const I a3 = g[3] + g[4], d3 = g[3] - g[4];
@@ -363,7 +363,7 @@ __host__ __device__ __forceinline__ bool collide_fx(double (&f)[NPOP], double fp
   // scaled post-collision moments (collision.f90:138-157): the linear part
   // as integer products, the rest converted from FP64
   auto L = [&](int k, I v) { return fx_mul(v, r.Li[k], r.Lsh[k]); };
-  auto F = [&](double x) { return fx_from<kFxOut, 60 - kFxOut>(x, bad, big); };
+  auto F = [&](double x) { return fx_from<kFxOut>(x, emax); };
   I M[16];
   M[1] = L(1, ev1) + L(16, rho) + F(r.B1t * t1 + r.H1 * G3);
   M[2] = L(2, ev2) + L(17, rho) + F(r.B2t * t1 + r.H2 * G3);
@@ -384,7 +384,7 @@ __host__ __device__ __forceinline__ bool collide_fx(double (&f)[NPOP], double fp
   const I tl6 = F(0.1 * ux + 0.05 * fx);
   const I tl8 = F(0.1 * uy + 0.05 * fy);
   const I tl10 = F(0.1 * uz + 0.05 * fz);
-  unsigned out = bad;
+  unsigned out = emax >= 1023 - 1;  // FP64 parts below 1/2
 #pragma unroll
   for (int k = 1; k < 16; ++k) out |= fx_out_of_range(M[k]);
   out |= fx_out_of_range(tl1) | fx_out_of_range(tl6) | fx_out_of_range(tl8) |
