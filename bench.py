@@ -459,8 +459,10 @@ def main():
         from multiphase_flow_codes_gb300 import ensemble
         be = ensemble.run(steps=args.batch_steps)
         k = be["kernel"]
-        k["roofline"] = {"bound": "hbm", "achieved": k["achieved_gbs"], "peak": hbm, "unit": "GB/s",
-                         "frac": k["achieved_gbs"] / hbm}
+        # each batch's kernel timed alone by its autotuner; bytes over time summed
+        agg = sum(k["alg_bytes"]) / (sum(k["ms_per_launch"]) / 1e3) / 1e9
+        k["roofline"] = {"bound": "hbm", "achieved": agg, "peak": hbm, "unit": "GB/s",
+                         "frac": agg / hbm}
         line["batched_ensemble"] = be
 
     if args.serve_seconds > 0 and rank == 0 and args.workload in ("config1", "box256_p1000_f64"):

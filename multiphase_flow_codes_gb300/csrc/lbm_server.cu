@@ -43,6 +43,9 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
+// batches stepped side by side on their own streams (regroup)
+constexpr int kConcurrent = 3;
+
 struct Job {
   int64_t id = 0;
   lbm_request req{};
@@ -190,14 +193,32 @@ void regroup(lbm_server* s) {
     groups[{wall, 0}].push_back(j);
   }
   for (auto& kv : groups) {
-    std::vector<lbm_ctx*> ctxs;
-    for (Job* j : kv.second) ctxs.push_back(j->ctx);
-    lbm_batch* b = nullptr;
-    if (lbm_batch_create(ctxs.data(), (int)ctxs.size(), &b) == LBM_OK) {
-      s->batches.push_back(b);
-      s->batch_members.push_back(kv.second);
-    } else {
-      for (Job* j : kv.second) j->batchable = false;
+    // up to kConcurrent batches of about equal node counts per group: each
+    // batch has its own stream, so one batch's particle kernels overlap
+    // another's stream + collide kernel
+    std::vector<Job*> jobs = kv.second;
+    std::sort(jobs.begin(), jobs.end(), [](const Job* a, const Job* b) {
+      return (int64_t)a->req.nx * a->req.ny * a->req.nz > (int64_t)b->req.nx * b->req.ny * b->req.nz;
+    });
+    const int parts = std::max(1, std::min<int>(kConcurrent, (int)jobs.size() / 2));
+    std::vector<std::vector<Job*>> part(parts);
+    std::vector<int64_t> load(parts, 0);
+    for (Job* j : jobs) {
+      const int g = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+      part[g].push_back(j);
+      load[g] += (int64_t)j->req.nx * j->req.ny * j->req.nz;
+    }
+    for (auto& members : part) {
+      if (members.empty()) continue;
+      std::vector<lbm_ctx*> ctxs;
+      for (Job* j : members) ctxs.push_back(j->ctx);
+      lbm_batch* b = nullptr;
+      if (lbm_batch_create(ctxs.data(), (int)ctxs.size(), &b) == LBM_OK) {
+        s->batches.push_back(b);
+        s->batch_members.push_back(members);
+      } else {
+        for (Job* j : members) j->batchable = false;
+      }
     }
   }
   ++s->rebuilds;

@@ -7,9 +7,10 @@ the 64^3 case (E(k) ~ k^4 exp(-2 (k/4)^2), u_rms 0.03).  Spheres are capped
 at a solid volume fraction of 15 % so that the reference's placement
 (initpartpos with a gap of 2) can succeed in the small boxes.
 
-``run`` builds the boxes, lets the batch autotuner pick the schedule of the
-batched stream + collide kernel, and times whole steps of all boxes (graph
-replays of 6-step cycles) with CUDA events on the batch's stream.
+``run`` builds the boxes, splits them into a few batches stepped
+concurrently on their own streams, lets the batch autotuner pick each
+batch's schedule, and times whole steps of all boxes (graph replays of
+6-step cycles) with CUDA events joined over the streams.
 """
 
 from __future__ import annotations
@@ -53,50 +54,91 @@ def make_boxes(box_specs: list, precision: int = capi.LBM_PREC_F32) -> list:
     return boxes
 
 
-def run(steps: int = 500, warmup: int = 6, nboxes: int = 48, tune_reps: int = 3) -> dict:
-    """Time `steps` steps of the ensemble; returns the figures of one run."""
+def split(box_specs: list, parts: int) -> list:
+    """Indices of the boxes in `parts` groups of about equal node counts
+    (largest first into the lightest group)."""
+    order = sorted(range(len(box_specs)), key=lambda i: -box_specs[i][0] ** 3)
+    groups = [[] for _ in range(max(1, min(parts, len(box_specs))))]
+    load = [0] * len(groups)
+    for i in order:
+        g = load.index(min(load))
+        groups[g].append(i)
+        load[g] += box_specs[i][0] ** 3
+    return [sorted(g) for g in groups]
+
+
+def run(steps: int = 500, warmup: int = 6, nboxes: int = 48, tune_reps: int = 3,
+        concurrent: int = 3) -> dict:
+    """Time `steps` steps of the ensemble; returns the figures of one run.
+
+    The boxes form `concurrent` batches of about equal node counts, each on
+    its own stream: while one batch's particle kernels (latency-bound) run,
+    another batch's stream + collide kernel (bandwidth-bound) keeps HBM busy.
+    Steps go in whole 6-step graph cycles, interleaved over the batches."""
     import torch
     sp = specs(nboxes)
     t0 = time.perf_counter()
     boxes = make_boxes(sp)
     setup_s = time.perf_counter() - t0
-    batch = LBMBatch(boxes)
+    groups = split(sp, concurrent)
+    batches = [LBMBatch([boxes[i] for i in g]) for g in groups]
     try:
-        kernel_ms = batch.autotune(tune_reps)
-        sched = batch.schedule()
-        stream = torch.cuda.Stream()
-        batch.set_stream(stream.cuda_stream)
-        batch.step(warmup, graph=True)
-        batch.synchronize()
-        nodes = batch.nodes
-        l0 = LBMBox.kernel_launches()
+        kernel_ms = [b.autotune(tune_reps) for b in batches]
+        scheds = [b.schedule() for b in batches]
+        streams = [torch.cuda.Stream() for _ in batches]
+        for b, st in zip(batches, streams):
+            b.set_stream(st.cuda_stream)
+        for b in batches:
+            b.step(warmup, graph=True)
+        for b in batches:
+            b.synchronize()
+        nodes = sum(b.nodes for b in batches)
+        cycles = max(1, steps // 6)
+        steps = 6 * cycles
+        base = torch.cuda.Stream()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
+        ends = [torch.cuda.Event() for _ in batches]
         torch.cuda.synchronize()
-        e0.record(stream)
-        batch.step(steps, graph=True)
-        e1.record(stream)
-        batch.synchronize()
+        l0 = LBMBox.kernel_launches()
+        e0.record(base)
+        for st in streams:
+            st.wait_event(e0)
+        for _ in range(cycles):
+            for b in batches:
+                b.step(6, graph=True)
+        for ev, st in zip(ends, streams):
+            ev.record(st)
+            base.wait_event(ev)
+        e1.record(base)
+        e1.synchronize()
+        for b in batches:
+            b.synchronize()
         wall = e0.elapsed_time(e1) / 1e3
         launches = LBMBox.kernel_launches() - l0
-        alg = 2 * 19 * 4 * nodes
+        alg = [2 * 19 * 4 * b.nodes for b in batches]
         return {
             "boxes": nboxes, "steps": steps, "nodes": nodes,
             "particles": int(sum(s[1] for s in sp)),
             "edges": {str(e): sum(1 for s in sp if s[0] == e) for e in EDGES},
             "value": nodes * steps / wall / 1e6, "unit": "MLUPS",
             "ms_per_step": wall * 1e3 / steps,
-            "kernel": {"name": "k_fused_batch_x2", "schedule": {"stages": sched[0],
-                       "groups": sched[1], "ctas_per_sm": sched[2]},
+            "concurrent_batches": len(batches),
+            "kernel": {"name": "k_fused_batch_x2",
+                       "schedule": [{"stages": s[0], "groups": s[1], "ctas_per_sm": s[2]}
+                                    for s in scheds],
                        "ms_per_launch": kernel_ms, "alg_bytes": alg,
-                       "achieved_gbs": alg / (kernel_ms / 1e3) / 1e9},
+                       "achieved_gbs": [a / (m / 1e3) / 1e9 for a, m in zip(alg, kernel_ms)]},
             "gpu_launches": launches,
             "setup_s": setup_s,
-            "how": "one lbm_batch over all boxes; autotuned schedule; 6-step cycles replayed "
-                   "from a CUDA graph; CUDA events on the batch stream around the steps",
+            "how": f"{len(batches)} lbm_batches of about equal node counts, each on its own stream "
+                   "(one group's particle kernels overlap another's stream + collide); autotuned "
+                   "schedules; 6-step cycles replayed from CUDA graphs; CUDA events around all "
+                   "streams",
         }
     finally:
-        batch.close()
+        for b in batches:
+            b.close()
         for b in boxes:
             b.close()
 
@@ -110,5 +152,6 @@ if __name__ == "__main__":
     ap.add_argument("--warmup", type=int, default=6)
     ap.add_argument("--boxes", type=int, default=48)
     ap.add_argument("--tune-reps", type=int, default=3)
+    ap.add_argument("--concurrent", type=int, default=3)
     a = ap.parse_args()
-    print(json.dumps(run(a.steps, a.warmup, a.boxes, a.tune_reps)))
+    print(json.dumps(run(a.steps, a.warmup, a.boxes, a.tune_reps, a.concurrent)))
