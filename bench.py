@@ -252,6 +252,7 @@ def cpu_oracle(wl, u, y, steps, threads=None):
     import oracle
     if threads:
         os.environ["OMP_NUM_THREADS"] = str(threads)
+        oracle.set_threads(threads)
     o = oracle.OracleBox(wl.cfg)
     o.initpop(*u)
     o.macrovar()
@@ -296,6 +297,8 @@ def main():
     ap.add_argument("--workload", default="config1")
     ap.add_argument("--cpu-steps", type=int, default=2, help="CPU baseline sample (full steps)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-one-core-steps", type=int, default=1,
+                    help="CPU baseline also on one thread for this many steps (0: skip)")
     ap.add_argument("--no-fp32", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--fp32-report", default="10,100,2000",
@@ -492,6 +495,11 @@ def main():
                                 "kind": "port",
                                 "sample": f"{args.cpu_steps} full steps of {wl.name} on the CPU "
                                           "restatement (OpenMP)"}
+        if args.cpu_one_core_steps > 0:
+            dt1 = cpu_oracle(wl, u, y, args.cpu_one_core_steps, 1)
+            line["cpu_baseline"]["one_core"] = {
+                "value": N * args.cpu_one_core_steps / dt1 / 1e6, "unit": "MLUPS", "cores": 1,
+                "sample": f"{args.cpu_one_core_steps} full step(s) of {wl.name}, one thread"}
     rep.barrier()
     if rep.leader:
         print(json.dumps(line), flush=True)

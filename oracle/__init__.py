@@ -58,11 +58,18 @@ def lib() -> C.CDLL:
         L.orc_release.restype = None
         L.orc_restore.argtypes = [P, C.c_int]
         L.orc_restore.restype = None
+        L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_set_threads.restype = None
         L.orc_step.argtypes = [P, C.c_int]
         L.orc_ran1_sequence.argtypes = [C.c_int32, C.c_int, C.POINTER(C.c_double)]
         L.orc_ran1_sequence.restype = None
         _lib = L
     return _lib
+
+
+def set_threads(n: int):
+    """Host threads of the restatement's parallel loops."""
+    lib().orc_set_threads(int(n))
 
 
 def ran1_sequence(seed: int, n: int) -> np.ndarray:

@@ -26,6 +26,8 @@
 
 #include "../include/lbm.h"
 
+#include <omp.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -1127,6 +1129,8 @@ void orc_initpop(void* h) { static_cast<Oracle*>(h)->initpop(); }
 int orc_initpartpos(void* h, int np) { return static_cast<Oracle*>(h)->initpartpos(np); }
 // positions already in ypglb (set through orc_field), velocities in wp/omgp
 void orc_release(void* h, int np) { static_cast<Oracle*>(h)->release(np); }
+// host threads of the parallel loops (the CPU baseline's core count)
+void orc_set_threads(int n) { omp_set_num_threads(n > 0 ? n : 1); }
 void orc_restore(void* h, int np) { static_cast<Oracle*>(h)->restore(np); }
 int orc_step(void* h, int nsteps) {
   Oracle* o = static_cast<Oracle*>(h);
