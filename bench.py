@@ -268,12 +268,12 @@ def cpu_oracle(wl, u, y, steps, threads=None):
 
 
 def workload(name: str):
-    """config0/1/2, or box{n}[x{ny}x{nz}]_p{npart}_{f64|f32} (radius 4, density ratio 2.5)."""
+    """box64_p16_f64, box256_p1000_f64, box256_p1000_f32, or
+    box{n}[x{ny}x{nz}]_p{npart}_{f64|f32} (radius 4, density ratio 2.5)."""
     from multiphase_flow_codes_gb300 import _capi as capi
     from multiphase_flow_codes_gb300 import config
-    table = {"config0": config.config0, "config1": config.config1, "config2": config.config2,
-             "box64_p16_f64": config.config0, "box256_p1000_f64": config.config1,
-             "box256_p1000_f32": config.config2}
+    table = {"box64_p16_f64": config.box64_p16_f64, "box256_p1000_f64": config.box256_p1000_f64,
+             "box256_p1000_f32": config.box256_p1000_f32}
     if name in table:
         return table[name]()
     import re
@@ -294,7 +294,7 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="config1")
+    ap.add_argument("--workload", default="box256_p1000_f64")
     ap.add_argument("--cpu-steps", type=int, default=2, help="CPU baseline sample (full steps)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-one-core-steps", type=int, default=1,
@@ -428,7 +428,7 @@ def main():
 
     if not args.no_fp32 and dtype == "f64":
         from multiphase_flow_codes_gb300 import config
-        wl32 = config.config2() if args.workload in ("config1", "box256_p1000_f64") else workload(args.workload)
+        wl32 = config.box256_p1000_f32() if args.workload == "box256_p1000_f64" else workload(args.workload)
         if wl32.cfg.precision != capi.LBM_PREC_F32:
             wl32.cfg.precision = capi.LBM_PREC_F32
         ms32, l32, ph32, f32, p32, variant32 = run_device(wl32, u, y, args.steps, args.warmup, local, want_f=True)
@@ -458,7 +458,7 @@ def main():
                        "E(k) and dissipation from lbm_statistics, slip on the R+1..R+3 fluid shell, "
                        "fHIp RMS over particles"}
 
-    if args.batch_steps > 0 and rank == 0 and args.workload in ("config1", "box256_p1000_f64"):
+    if args.batch_steps > 0 and rank == 0 and args.workload == "box256_p1000_f64":
         from multiphase_flow_codes_gb300 import ensemble
         be = ensemble.run(steps=args.batch_steps)
         k = be["kernel"]
@@ -468,7 +468,7 @@ def main():
                          "frac": agg / hbm}
         line["batched_ensemble"] = be
 
-    if args.serve_seconds > 0 and rank == 0 and args.workload in ("config1", "box256_p1000_f64"):
+    if args.serve_seconds > 0 and rank == 0 and args.workload == "box256_p1000_f64":
         from multiphase_flow_codes_gb300 import serving
         sv = serving.poisson_run(rate=args.serve_rate, duration=args.serve_seconds)
         sv["how"] = ("native lbm_server loop: Poisson arrivals, admission by lbm_footprint within a "

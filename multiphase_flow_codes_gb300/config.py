@@ -45,20 +45,20 @@ def channel(nx: int, ny: int, nz: int, npart: int, rad: float = 4.0, rhopart: fl
     return Workload(name or f"channel{nx}x{ny}x{nz}", cfg, npart, 4.0, 0.0, steps)
 
 
-def config0() -> Workload:
+def box64_p16_f64() -> Workload:
     """64^3 periodic box, 16 spheres R = 4.5, density ratio 5, u_rms 0.03,
     spectrum peak k0 = 4, 1000 steps, FP64."""
     return box(64, 16, 4.5, 5.0, 4.0, 0.03, 1000, name="box64_p16_f64")
 
 
-def config1() -> Workload:
+def box256_p1000_f64() -> Workload:
     """256^3 periodic box, 1000 spheres R = 4, density ratio 2.5, u_rms 0.04,
     k0 = 8, 2000 steps, FP64: the roofline workload."""
     return box(256, 1000, 4.0, 2.5, 8.0, 0.04, 2000, name="box256_p1000_f64")
 
 
-def config2() -> Workload:
-    """config1 with populations stored and collided in FP32."""
+def box256_p1000_f32() -> Workload:
+    """The 256^3, 1000-sphere box with populations stored and collided in FP32."""
     w = box(256, 1000, 4.0, 2.5, 8.0, 0.04, 2000, precision=capi.LBM_PREC_F32,
             name="box256_p1000_f32")
     return w

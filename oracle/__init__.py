@@ -1,8 +1,8 @@
 """CPU oracle: ctypes wrapper of the C++ restatement in lbm_oracle.cpp.
 
 TEST INFRASTRUCTURE ONLY.  The parity tests, ``__graft_entry__.smoke()`` and
-the CPU-baseline leg of ``bench.py`` use it as the checker; the engine never
-calls it.
+the CPU-baseline leg of ``bench.py`` compare the engine with it; the engine
+never calls it.
 
 Parity unpinned: the reference (Fortran + MPI + FFTW 2) cannot be compiled
 or run in this environment and ships no golden vectors, so this restatement

@@ -1,7 +1,7 @@
 // lbm_oracle.cpp - CPU restatement of the reference's particle-laden D3Q19
 // MRT lattice Boltzmann time step, used ONLY as test infrastructure: the
-// parity tests, the smoke check and the CPU-baseline leg of bench.py call it
-// as the checker.  Nothing in the product library links or calls this file.
+// parity tests, the smoke check and the CPU-baseline leg of bench.py compare
+// the engine with it.  Nothing in the product library links or calls this file.
 //
 // Parity status: the reference is Fortran 90 + MPI + FFTW 2 and cannot be
 // compiled in this environment (no Fortran compiler, no MPI), and it ships

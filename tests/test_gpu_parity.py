@@ -117,7 +117,7 @@ def test_links_wrapping_particles(require_gpu, oracle_mod):
     check_links(o, box)
 
 
-def test_particles_config0_geometry_10_steps(require_gpu, oracle_mod):
+def test_particles_box64_geometry_10_steps(require_gpu, oracle_mod):
     """The 64^3, 16-sphere (R = 4.5, density ratio 5) workload, 10 steps."""
     o, box = make_pair(oracle_mod, shape=(64, 64, 64), npart=16, rad=4.5, rhopart=5.0)
     for s in range(10):
