@@ -44,6 +44,12 @@ struct lbm_ctx {
   // next step's FORCING, launched early on a side stream (see do_forcing)
   cudaStream_t side = nullptr;
   cudaEvent_t ev_main = nullptr, ev_forcing = nullptr, ev_status = nullptr;
+  // particle work of a fused step that needs no post-collision populations
+  // (the new flag buffer's reset, beads_lubforce) runs here beside the
+  // bounce-back (particle_phase)
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_aux_fork = nullptr, ev_aux_join = nullptr;
+  bool aux_pending = false;
   bool prefetched = false;
   int prefetch_slot = 0;
   ForcingDev* d_forcing_backup = nullptr;
@@ -198,12 +204,13 @@ size_t flag_bytes(const Geometry& g) {
   return (size_t)g.N * sizeof(int32_t) + (size_t)g.ny * g.nz * g.sw * sizeof(uint32_t);
 }
 // all nodes fluid: ids -1, mask clear
-cudaError_t reset_flags(lbm_ctx* c, int i) {
-  cudaError_t e = cudaMemsetAsync(c->flags[i], 0xff, (size_t)c->g.N * sizeof(int32_t), c->stream);
+cudaError_t reset_flags_on(lbm_ctx* c, int i, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(c->flags[i], 0xff, (size_t)c->g.N * sizeof(int32_t), st);
   if (e != cudaSuccess) return e;
   return cudaMemsetAsync(c->flags[i] + c->g.N, 0,
-                         (size_t)c->g.ny * c->g.nz * c->g.sw * sizeof(uint32_t), c->stream);
+                         (size_t)c->g.ny * c->g.nz * c->g.sw * sizeof(uint32_t), st);
 }
+cudaError_t reset_flags(lbm_ctx* c, int i) { return reset_flags_on(c, i, c->stream); }
 
 // ranpp / ranff: Numerical Recipes ran1 (Park-Miller with Bays-Durham
 // shuffle) as B/partlib.f90:83-115 states it
@@ -390,17 +397,37 @@ void cancel_prefetch(lbm_ctx* c) {
   c->prefetched = false;
 }
 
+// The part of the particle step that reads no post-collision populations:
+// the reset of the flag buffer beads_links fills next (last read by the
+// previous step's beads_filling) and beads_lubforce (positions only).  A
+// fused step launches it on the aux stream right after stream + collide, so
+// it runs beside the bounce-back; particle_phase joins it.
+void particle_prelude(lbm_ctx* c) {
+  if (!c->particles_on || c->aux_pending) return;
+  cudaEventRecord(c->ev_aux_fork, c->stream);
+  cudaStreamWaitEvent(c->aux, c->ev_aux_fork, 0);
+  reset_flags_on(c, 1 - c->fcur, c->aux);
+  launch_lubforce(c->g, c->npart, c->pp, mstate(c), c->aux);
+  cudaEventRecord(c->ev_aux_join, c->aux);
+  c->aux_pending = true;
+}
+
 template <typename T>
 void particle_phase(lbm_ctx* c, T* f_plain) {
   // beads_lubforce, beads_move, beads_redistribute, beads_links, beads_filling
+  const bool pre = c->aux_pending;
+  if (pre) {
+    cudaStreamWaitEvent(c->stream, c->ev_aux_join, 0);
+    c->aux_pending = false;
+  }
   prof_begin(c);
-  launch_lubforce(c->g, c->npart, c->pp, mstate(c), c->stream);
+  if (!pre) launch_lubforce(c->g, c->npart, c->pp, mstate(c), c->stream);
   launch_move(c->g, c->npart, c->pp, mstate(c), c->stream);
   launch_redistribute(c->g, c->npart, c->pp, mstate(c), c->status, c->stream);
   prof_end(c, LBM_PHASE_PARTICLES);
   int nf = 1 - c->fcur;
   prof_begin(c);
-  reset_flags(c, nf);
+  if (!pre) reset_flags(c, nf);
   launch_links(c->g, pview(c), c->flags[nf], c->links, c->status, c->f32, c->stream);
   prof_end(c, LBM_PHASE_LINKS);
   prof_begin(c);
@@ -490,6 +517,7 @@ void fused_step_t(lbm_ctx* c) {
   launch_stream_collide<T>(c, fin, fout, true);
   prof_end(c, LBM_PHASE_STREAM_COLLIDE);
   prefetch_forcing(c);
+  particle_prelude(c);
   if (c->particles_on) {
     prof_begin(c);
     launch_bounce_back<T>(c->g, pview(c), fout, 1, c->flags[c->fcur], c->links, c->fHIp,
@@ -769,6 +797,9 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
   }
   ctx->own_stream = true;
   if (cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_aux_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_aux_join, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->ev_main, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->ev_forcing, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->ev_status, cudaEventDisableTiming) != cudaSuccess) {
@@ -926,6 +957,7 @@ int lbm_destroy(lbm_ctx* ctx) {
   if (!ctx) return LBM_OK;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->side) cudaStreamSynchronize(ctx->side);
+  if (ctx->aux) cudaStreamSynchronize(ctx->aux);
   spectrum_free(ctx->spec);
   ctx->spec = nullptr;
   void* ptrs[] = {ctx->f[0], ctx->f[1], ctx->macro, ctx->flags[0], ctx->flags[1], ctx->status,
@@ -943,7 +975,9 @@ int lbm_destroy(lbm_ctx* ctx) {
   if (ctx->partial_host) cudaFreeHost(ctx->partial_host);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   if (ctx->side) cudaStreamDestroy(ctx->side);
-  for (cudaEvent_t e : {ctx->ev_main, ctx->ev_forcing, ctx->ev_status})
+  if (ctx->aux) cudaStreamDestroy(ctx->aux);
+  for (cudaEvent_t e : {ctx->ev_main, ctx->ev_forcing, ctx->ev_status, ctx->ev_aux_fork,
+                        ctx->ev_aux_join})
     if (e) cudaEventDestroy(e);
   delete ctx;
   return LBM_OK;
