@@ -541,6 +541,7 @@ template <typename T>
 struct Acc {
   double s = 0.0;
   __device__ void add(double x) { s += x; }
+  __device__ void add_prod(double a, double b) { s = fma(a, b, s); }
   __device__ double value() const { return s; }
 };
 template <>
@@ -552,8 +553,28 @@ struct Acc<float> {
     c = (t - s) - y;
     s = t;
   }
+  __device__ void add_prod(float a, float b) { add(a * b); }
   __device__ double value() const { return (double)s - (double)c; }
 };
+
+// 1 / x for x in [1/2, 3] (the link-fraction denominators of the bounce-back).
+// FP64: Newton-Raphson reciprocal iteration r <- r + r (1 - x r) from a
+// single-precision seed; each step squares the relative error, so two steps
+// take the seed's 2^-22 below the FP64 rounding.  On this GPU FP64 issues at
+// a small fraction of the FP32 rate, and the iteration is 4 FMAs.
+__device__ __forceinline__ double recip_link(double x) {
+  const float xf = __double2float_rn(x);
+  float r0;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(xf));
+  double r = (double)r0;
+  double e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.0);
+  return fma(r, e, r);
+}
+__device__ __forceinline__ float recip_link(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double fma_r(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fma_r(float a, float b, float c) { return fmaf(a, b, c); }
 
 // post-collision population q at node (i, j, k) (0-based) in either layout.
 // pushed: the fused kernel has already moved it to its streaming target
@@ -598,39 +619,50 @@ __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, Partic
   const R xc0 = R(pv.ypglb[3 * p]), yc0 = R(pv.ypglb[3 * p + 1]), zc0 = R(pv.ypglb[3 * p + 2]);
   const bool channel = g.channel != 0;
   const uint32_t* mask = solid_mask(isnodes, g);
-  // Per axis, the link point coordinate pnt = i + 1/2 and the image of the
-  // centre nearest to it depend on the node's coordinate i alone: tabulate
-  // them once per particle for the kBounceSpan coordinates around the
-  // centre (same operations as per link, so the same values); links outside
-  // the table compute them directly.
-  __shared__ R tpnt[3][kBounceSpan], tcen[3][kBounceSpan];
+  // Per axis, the offset d = pnt - c of the link point pnt = i + 1/2 from the
+  // image c of the centre nearest to it depends on the node's coordinate i
+  // alone: tabulate it once per particle for the kBounceSpan coordinates
+  // around the centre (same operations as per link, so the same values);
+  // links outside the table compute it directly.  Per direction, c_q . w.
+  __shared__ R tdel[3][kBounceSpan];
+  __shared__ R tcw[NPOP];
+  // c_a v with c_a in {-1, 0, 1}: exact, so selected rather than multiplied
+  auto sel = [](int c, R v) { return c == 0 ? R(0) : (c > 0 ? v : -v); };
   int lo[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) lo[a] = (int)floor((double)pv.ypglb[3 * p + a]) - (kBounceSpan / 2);
   {
-    const R cen[3] = {xc0, yc0, zc0};
-    const int nn[3] = {g.nx, g.ny, g.nz}, nh[3] = {g.nxh, g.nyh, g.nzh};
-    for (int a = 0; a < 3; ++a)
-      lo[a] = (int)floor((double)pv.ypglb[3 * p + a]) - (kBounceSpan / 2);
+    // selects rather than arrays indexed by a, which would live in local memory
     for (int t = threadIdx.x; t < 3 * kBounceSpan; t += PB) {
       const int a = t / kBounceSpan, d = t - a * kBounceSpan;
       const bool periodic = !(channel && a == 0);
-      int i = lo[a] + d;
-      if (periodic) i = ((i % nn[a]) + nn[a]) % nn[a];
+      const R cen = a == 0 ? xc0 : (a == 1 ? yc0 : zc0);
+      const int n = a == 0 ? g.nx : (a == 1 ? g.ny : g.nz);
+      const int nh = a == 0 ? g.nxh : (a == 1 ? g.nyh : g.nzh);
+      int i = (a == 0 ? lo[0] : (a == 1 ? lo[1] : lo[2])) + d;
+      if (periodic) i = ((i % n) + n) % n;
       const R pnt = R(i + 1) - R(0.5);
-      tpnt[a][d] = pnt;
-      tcen[a][d] = periodic ? near_img_t<R>(cen[a], pnt, nn[a], nh[a]) : cen[a];
+      tdel[a][d] = pnt - (periodic ? near_img_t<R>(cen, pnt, n, nh) : cen);
+    }
+    if (threadIdx.x < NPOP) {
+      const int q = threadIdx.x;
+      tcw[q] = sel(cix(q), w1) + sel(ciy(q), w2) + sel(ciz(q), w3);
     }
     __syncthreads();
   }
-  auto coord = [&](int a, int i, R cen, int n, int nhalf, bool periodic, R& pnt, R& c) {
+  auto delta = [&](int a, int i, R cen, int n, int nhalf, bool periodic) -> R {
     int d = i - lo[a];
     if (periodic) d = d < 0 ? d + n : (d >= n ? d - n : d);
-    if (d >= 0 && d < kBounceSpan) {
-      pnt = tpnt[a][d];
-      c = tcen[a][d];
-    } else {
-      pnt = R(i + 1) - R(0.5);
-      c = periodic ? near_img_t<R>(cen, pnt, n, nhalf) : cen;
-    }
+    if (d >= 0 && d < kBounceSpan) return tdel[a][d];
+    const R pnt = R(i + 1) - R(0.5);
+    return pnt - (periodic ? near_img_t<R>(cen, pnt, n, nhalf) : cen);
+  };
+  // cb db - cc dc for cb, cc in {-1, 0, 1}: one add at most
+  auto cross = [](int cb, R db, int cc, R dc) -> R {
+    const R u = cb == 0 ? R(0) : (cb > 0 ? db : -db);
+    if (cc == 0) return u;
+    const R v = cc > 0 ? dc : -dc;
+    return cb == 0 ? -v : u - v;
   };
   for (int l = threadIdx.x; l < cnt; l += PB) {
     // 32-bit decode: node < 2^26
@@ -640,16 +672,12 @@ __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, Partic
     const int r = node / g.nx;
     const int i = node - r * g.nx;
     const int k = r / g.ny, j = r - k * g.ny;
-    R alpha = alph[l];
-    int ipp = ipopp(ipop);
-    R xpnt, ypnt, zpnt, xc, yc, zc;
-    coord(0, i, xc0, g.nx, g.nxh, !channel, xpnt, xc);
-    coord(1, j, yc0, g.ny, g.nyh, true, ypnt, yc);
-    coord(2, k, zc0, g.nz, g.nzh, true, zpnt, zc);
-    int ix = cix(ipop), iy = ciy(ipop), iz = ciz(ipop);
+    const R alpha = alph[l];
+    const int ipp = ipopp(ipop);
+    const int ix = cix(ipop), iy = ciy(ipop), iz = ciz(ipop);
     int im1 = i - ix, im2 = i - 2 * ix;
-    int jm1 = wrapi(j - iy, g.ny), km1 = wrapi(k - iz, g.nz);
-    int jm2 = wrapi(j - 2 * iy, g.ny), km2 = wrapi(k - 2 * iz, g.nz);
+    const int jm1 = wrapi(j - iy, g.ny), km1 = wrapi(k - iz, g.nz);
+    const int jm2 = wrapi(j - 2 * iy, g.ny), km2 = wrapi(k - 2 * iz, g.nz);
     bool out1 = false, out2 = false;
     if (channel) {
       out1 = im1 < 0 || im1 >= g.nx;
@@ -658,72 +686,74 @@ __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, Partic
       im1 = wrapi(im1, g.nx);
       im2 = wrapi(im2, g.nx);
     }
-    // c_a alpha with c_a in {-1, 0, 1}: exact, so selected rather than multiplied
-    auto sel = [](int c, R v) { return c == 0 ? R(0) : (c > 0 ? v : -v); };
-    R xx0 = xpnt + sel(ix, alpha) - xc;
-    R yy0 = ypnt + sel(iy, alpha) - yc;
-    R zz0 = zpnt + sel(iz, alpha) - zc;
-    R ff1 = R(read_post(g, f, pushed, ipop, i, j, k));
-    R uwx = w1 + omg2 * zz0 - omg3 * yy0;
-    R uwy = w2 + omg3 * xx0 - omg1 * zz0;
-    R uwz = w3 + omg1 * yy0 - omg2 * xx0;
-    R uwpro = sel(ix, uwx) + sel(iy, uwy) + sel(iz, uwz);
-    const R wwp = ipop <= 6 ? R(1.0 / 18.0) : R(1.0 / 36.0);
-    R f9;
-    if (alpha <= 0.5) {
-      int ibm1, ibm2;
-      R ff2 = R(0), ff3 = R(0);
-      if (out1) ibm1 = 2;
-      else {
-        ibm1 = is_solid(mask, g, km1 * g.ny + jm1, im1) ? 1 : -1;
-        if (ibm1 < 0) ff2 = R(read_post(g, f, pushed, ipop, im1, jm1, km1));
-      }
-      if (out2) ibm2 = 2;
-      else {
-        ibm2 = is_solid(mask, g, km2 * g.ny + jm2, im2) ? 1 : -1;
-        if (ibm1 < 0 && ibm2 < 0) ff3 = R(read_post(g, f, pushed, ipop, im2, jm2, km2));
-      }
-      if (ibm1 > 0) {
-        f9 = ff1 - R(6.0) * wwp * uwpro;
-      } else if (ibm2 > 0) {
-        f9 = R(2.0) * alpha * (ff1 - ff2) + ff2 - R(6.0) * wwp * uwpro;
-      } else {
-        R c1 = alpha * (R(1.0) + R(2.0) * alpha);
-        R c2 = R(1.0) - R(4.0) * alpha * alpha;
-        R c3 = -alpha * (R(1.0) - R(2.0) * alpha);
-        f9 = c1 * ff1 + c2 * ff2 + c3 * ff3 - R(6.0) * wwp * uwpro;
-      }
+    // The reference's lever arm is r = d + alpha c (the boundary point);
+    // every quantity it enters is a product with c: the wall velocity
+    // c . (w + omega x r) = c . w + omega . (r x c) and the torque
+    // dff (r x c), and r x c = d x c.  So the per-link arithmetic needs only
+    // e = d x c, which for c in {-1, 0, 1}^3 is selects and one add.
+    const R dx = delta(0, i, xc0, g.nx, g.nxh, !channel);
+    const R dy = delta(1, j, yc0, g.ny, g.nyh, true);
+    const R dz = delta(2, k, zc0, g.nz, g.nzh, true);
+    const R ex = cross(iz, dy, iy, dz);
+    const R ey = cross(ix, dz, iz, dx);
+    const R ez = cross(iy, dx, ix, dy);
+    const R uwpro = fma_r(omg1, ex, fma_r(omg2, ey, fma_r(omg3, ez, tcw[ipop])));
+    const R ff1 = R(read_post(g, f, pushed, ipop, i, j, k));
+    // The five interpolation cases of beads_collision (B/partlib.f90:1439-1536)
+    // as f9 = c1 ff1 + c2 ff2 + c3 ff3 - 6 w c4 (c . u_w), with the same
+    // populations read and one division (for alpha > 1/2) shared by its two
+    // cases, so that a warp with mixed cases evaluates one formula:
+    //   alpha <= 1/2: ff2, ff3 = f(q) at x - c, x - 2c
+    //     x - c solid:  c1 = 1
+    //     x - 2c solid: c1 = 2 alpha, c2 = 1 - 2 alpha
+    //     else:         c1 = alpha (1 + 2 alpha), c2 = 1 - 4 alpha^2,
+    //                   c3 = -alpha (1 - 2 alpha)
+    //   alpha > 1/2: ff2, ff3 = f(qbar) at x, x - c;  c4 = c1
+    //     x - c solid:  c1 = 1 / (2 alpha), c2 = 1 - c1
+    //     else:         c1 = 1 / (alpha (2 alpha + 1)),
+    //                   c2 = (2 alpha - 1)(2 alpha + 1) c1, c3 = 1 - c1 - c2
+    const bool low = alpha <= R(0.5);
+    int ibm1 = 2, ibm2 = 2;
+    if (!out1) ibm1 = is_solid(mask, g, km1 * g.ny + jm1, im1) ? 1 : -1;
+    if (low && !out2) ibm2 = is_solid(mask, g, km2 * g.ny + jm2, im2) ? 1 : -1;
+    const bool s1 = ibm1 > 0;
+    const bool s2 = low && !s1 && ibm2 > 0;
+    R ff2 = R(0), ff3 = R(0);
+    if (low) {
+      if (!s1) ff2 = R(read_post(g, f, pushed, ipop, im1, jm1, km1));
+      if (!s1 && !s2) ff3 = R(read_post(g, f, pushed, ipop, im2, jm2, km2));
     } else {
-      R ff2 = R(read_post(g, f, pushed, ipp, i, j, k));
-      int ibm1;
-      R ff3 = R(0);
-      if (out1) ibm1 = 2;
-      else {
-        ibm1 = is_solid(mask, g, km1 * g.ny + jm1, im1) ? 1 : -1;
-        if (ibm1 < 0) ff3 = R(read_post(g, f, pushed, ipp, im1, jm1, km1));
-      }
-      if (ibm1 > 0) {
-        R c1 = R(0.5) / alpha;
-        R c2 = R(1.0) - c1;
-        f9 = c1 * ff1 + c2 * ff2 - R(6.0) * wwp * c1 * uwpro;
-      } else {
-        // 1 / alpha / (2 alpha + 1) and (2 alpha - 1) / alpha with one division
-        const R inv = R(1.0) / (alpha * (R(2.0) * alpha + R(1.0)));
-        R c1 = inv;
-        R c2 = (R(2.0) * alpha - R(1.0)) * (R(2.0) * alpha + R(1.0)) * inv;
-        R c3 = R(1.0) - c1 - c2;
-        f9 = c1 * ff1 + c2 * ff2 + c3 * ff3 - R(6.0) * wwp * c1 * uwpro;
-      }
+      ff2 = R(read_post(g, f, pushed, ipp, i, j, k));
+      if (!s1) ff3 = R(read_post(g, f, pushed, ipp, im1, jm1, km1));
     }
+    const R t2 = alpha + alpha;
+    const R opt = R(1.0) + t2;             // 1 + 2 alpha
+    const R omt = R(1.0) - t2;             // 1 - 2 alpha
+    const R xa = alpha * opt;              // alpha (1 + 2 alpha)
+    const R y4 = omt * opt;                // 1 - 4 alpha^2
+    const R rc = recip_link(low ? R(1.0) : (s1 ? alpha : xa));
+    R c1, c2, c3, c4;
+    if (low) {
+      c1 = s1 ? R(1.0) : (s2 ? t2 : xa);
+      c2 = s1 ? R(0.0) : (s2 ? omt : y4);
+      c3 = (s1 || s2) ? R(0.0) : -alpha * omt;
+      c4 = R(1.0);
+    } else {
+      c1 = s1 ? R(0.5) * rc : rc;
+      c2 = s1 ? R(1.0) - c1 : -y4 * rc;
+      c3 = s1 ? R(0.0) : R(1.0) - c1 - c2;
+      c4 = c1;
+    }
+    const R k6 = ipop <= 6 ? R(6.0 / 18.0) : R(6.0 / 36.0);
+    const R f9 = fma_r(c1, ff1, fma_r(c2, ff2, fma_r(c3, ff3, -(k6 * c4) * uwpro)));
     f9s[l] = f9;
-    R dff = ff1 + f9;
-    R dxmom = sel(ix, dff), dymom = sel(iy, dff), dzmom = sel(iz, dff);
-    acc6[0].add(dxmom);
-    acc6[1].add(dymom);
-    acc6[2].add(dzmom);
-    acc6[3].add(dzmom * yy0 - dymom * zz0);
-    acc6[4].add(dxmom * zz0 - dzmom * xx0);
-    acc6[5].add(dymom * xx0 - dxmom * yy0);
+    const R dff = ff1 + f9;
+    if (ix) acc6[0].add(sel(ix, dff));
+    if (iy) acc6[1].add(sel(iy, dff));
+    if (iz) acc6[2].add(sel(iz, dff));
+    acc6[3].add_prod(dff, ex);
+    acc6[4].add_prod(dff, ey);
+    acc6[5].add_prod(dff, ez);
   }
   if constexpr (sizeof(T) == 4) {
     // per warp: exact two-sum tree of the compensated FP32 partial sums;
@@ -753,6 +783,7 @@ __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, Partic
       if (c < 3) fHIp[3 * p + c] = s; else torqp[3 * p + c - 3] = s;
     }
   } else {
+#pragma unroll
     for (int c = 0; c < 6; ++c) {
       double s = Red(red_tmp).Sum(acc6[c].value());
       __syncthreads();
