@@ -422,8 +422,7 @@ void particle_phase(lbm_ctx* c, T* f_plain) {
   }
   prof_begin(c);
   if (!pre) launch_lubforce(c->g, c->npart, c->pp, mstate(c), c->stream);
-  launch_move(c->g, c->npart, c->pp, mstate(c), c->stream);
-  launch_redistribute(c->g, c->npart, c->pp, mstate(c), c->status, c->stream);
+  launch_move_redistribute(c->g, c->npart, c->pp, mstate(c), c->status, c->stream);
   prof_end(c, LBM_PHASE_PARTICLES);
   int nf = 1 - c->fcur;
   prof_begin(c);

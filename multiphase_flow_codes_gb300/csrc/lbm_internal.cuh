@@ -310,6 +310,10 @@ void launch_move(const Geometry& g, int npart, const PartParams& pp, MoveState m
                  cudaStream_t s);
 void launch_redistribute(const Geometry& g, int npart, const PartParams& pp, MoveState ms,
                          DevStatus* st, cudaStream_t s);
+// launch_move then launch_redistribute in two launches: the move and the wrap
+// of a particle in one thread, the overlap check ending the first move
+void launch_move_redistribute(const Geometry& g, int npart, const PartParams& pp, MoveState ms,
+                              DevStatus* st, cudaStream_t s);
 // refill events of one step: node index and particle id per event
 struct FillList {
   int32_t* node;

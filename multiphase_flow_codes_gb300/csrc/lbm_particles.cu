@@ -24,6 +24,10 @@ namespace lbm {
 namespace {
 
 constexpr int PB = 256;  // threads per particle block
+// One thread per particle (or per particle axis) with serial FP64 work: one
+// warp per block spreads the particles over as many SMs as there are warps,
+// since this GPU issues FP64 at a few lanes per clock per SM.
+constexpr int kSmallBlock = 32;
 constexpr int kBounceSpan = 64;  // coordinates per axis tabulated by beads_collision
 
 __device__ __forceinline__ double near_img(double c, double p, int n, int nh) {
@@ -507,16 +511,21 @@ __device__ __forceinline__ void k_links_body(int bx, int gx, Geometry g, Particl
         const float a1 = sqrtf(fmaxf(a0 * a0 - ca, 0.0f));
         alph32[w] = 1.0f - (-a0 + a1);
       } else {
+        // the components of c are +-1 or 0: c . x1 is selects and one add
+        auto pick = [](int c, double v) { return c > 0 ? v : -v; };
         const int lj = row_j[lr], lk = row_k[lr];
-        const double xc = xval[min(lr, 2)][lci], yc = row_y[lr], zc = row_z[lr];
-        double xx1 = (double)(li + ix) - 0.5 - xc;
-        double yy1 = (double)(lj + iy) - 0.5 - yc + 0.0;
-        double zz1 = (double)(lk + iz) - 0.5 - zc + 0.0;
-        double cc = xx1 * xx1 + yy1 * yy1 + zz1 * zz1 - rad2;
-        double bb = -((double)ix * xx1 + (double)iy * yy1 + (double)iz * zz1);
-        double a0 = diag ? 0.5 * bb : bb;
-        double ca = diag ? 0.5 * cc : cc;
-        double a1 = sqrt(fmax(a0 * a0 - ca, 0.0));
+        const double xx1 = (double)(li + ix) - 0.5 - xval[min(lr, 2)][lci];
+        const double yy1 = (double)(lj + iy) - 0.5 - row_y[lr];
+        const double zz1 = (double)(lk + iz) - 0.5 - row_z[lr];
+        double bb;
+        if (ix == 0) bb = iy == 0 ? pick(iz, zz1) : (iz == 0 ? pick(iy, yy1) : pick(iy, yy1) + pick(iz, zz1));
+        else bb = iy != 0 ? pick(ix, xx1) + pick(iy, yy1)
+                          : (iz != 0 ? pick(ix, xx1) + pick(iz, zz1) : pick(ix, xx1));
+        bb = -bb;
+        const double cc = fma(xx1, xx1, fma(yy1, yy1, fma(zz1, zz1, -rad2)));
+        const double a0 = diag ? 0.5 * bb : bb;
+        const double ca = diag ? 0.5 * cc : cc;
+        const double a1 = sqrt(fmax(fma(a0, a0, -ca), 0.0));
         alph[w] = 1.0 - (-a0 + a1);
       }
     }
@@ -995,6 +1004,12 @@ __device__ __forceinline__ void k_wrap_body(int bx, int gx, Geometry g, int npar
 __global__ void k_wrap(Geometry g, int npart, MoveState ms) {
   k_wrap_body(blockIdx.x, gridDim.x, g, npart, ms);
 }
+// beads_move followed by beads_redistribute's wrap, each particle's thread
+// wrapping the centre it has just moved (the fused time step)
+__global__ void k_move_wrap(Geometry g, int npart, PartParams pp, MoveState ms) {
+  k_move_body(blockIdx.x, gridDim.x, npart, pp, ms);
+  k_wrap_body(blockIdx.x, gridDim.x, g, npart, ms);
+}
 
 // ovlpchk after a move (hgap = dist - 2 rad < 0 aborts the reference,
 // B/partlib.f90:2630-2646); here it raises LBM_ERR_OVERLAP.  One warp per
@@ -1018,7 +1033,10 @@ __device__ __forceinline__ void k_overlap_body(int bx, int gx, Geometry g, int n
     if (hgap < 0.0) raise_error(st, LBM_ERR_OVERLAP, p);
   }
 }
-__global__ void k_overlap(Geometry g, int npart, PartParams pp, MoveState ms, DevStatus* st) {
+__global__ void k_overlap(Geometry g, int npart, PartParams pp, MoveState ms, DevStatus* st,
+                          int* clear_first) {
+  // clear_first: beads_move's end of the first move, once every move has read it
+  if (clear_first && blockIdx.x == 0 && threadIdx.x == 0) *clear_first = 0;
   k_overlap_body(blockIdx.x, gridDim.x, g, npart, pp, ms, st);
 }
 
@@ -1234,7 +1252,7 @@ __global__ void __launch_bounds__(128) k_fill_events(Geometry g, ParticleView pv
 void launch_links(const Geometry& g, const ParticleView& pv, int32_t* isnodes, LinkSlab ls,
                   DevStatus* st, int alpha_fp32, cudaStream_t s) {
   if (pv.npart <= 0) return;
-  { k_link_sweeps<<<(3 * pv.npart + 127) / 128, 128, 0, s>>>(g, pv, ls); count_launch(); }
+  { k_link_sweeps<<<(3 * pv.npart + kSmallBlock - 1) / kSmallBlock, kSmallBlock, 0, s>>>(g, pv, ls); count_launch(); }
   { k_links<<<pv.npart, PB, 0, s>>>(g, pv, isnodes, ls, st, alpha_fp32); count_launch(); }
 }
 
@@ -1262,15 +1280,22 @@ void launch_lubforce(const Geometry& g, int npart, const PartParams& pp, MoveSta
 void launch_move(const Geometry& g, int npart, const PartParams& pp, MoveState ms,
                  cudaStream_t s) {
   if (npart <= 0) return;
-  { k_move<<<(npart + 127) / 128, 128, 0, s>>>(npart, pp, ms); count_launch(); }
+  { k_move<<<(npart + kSmallBlock - 1) / kSmallBlock, kSmallBlock, 0, s>>>(npart, pp, ms); count_launch(); }
   { k_clear_first<<<1, 1, 0, s>>>(ms.first_move); count_launch(); }
 }
 
 void launch_redistribute(const Geometry& g, int npart, const PartParams& pp, MoveState ms,
                          DevStatus* st, cudaStream_t s) {
   if (npart <= 0) return;
-  { k_wrap<<<(npart + 127) / 128, 128, 0, s>>>(g, npart, ms); count_launch(); }
-  { k_overlap<<<(npart * 32 + 127) / 128, 128, 0, s>>>(g, npart, pp, ms, st); count_launch(); }
+  { k_wrap<<<(npart + kSmallBlock - 1) / kSmallBlock, kSmallBlock, 0, s>>>(g, npart, ms); count_launch(); }
+  { k_overlap<<<(npart * 32 + 127) / 128, 128, 0, s>>>(g, npart, pp, ms, st, nullptr); count_launch(); }
+}
+
+void launch_move_redistribute(const Geometry& g, int npart, const PartParams& pp, MoveState ms,
+                              DevStatus* st, cudaStream_t s) {
+  if (npart <= 0) return;
+  { k_move_wrap<<<(npart + kSmallBlock - 1) / kSmallBlock, kSmallBlock, 0, s>>>(g, npart, pp, ms); count_launch(); }
+  { k_overlap<<<(npart * 32 + 127) / 128, 128, 0, s>>>(g, npart, pp, ms, st, ms.first_move); count_launch(); }
 }
 
 template <typename T>
@@ -1304,20 +1329,15 @@ __global__ void k_lubforce_multi(const BoxParticles* boxes) {
   BOX_OR_RETURN((B.pv.npart * 32 + 127) / 128)
   k_lubforce_body(blockIdx.x, nblk, B.g, B.pv.npart, B.pp, B.ms);
 }
-__global__ void k_move_multi(const BoxParticles* boxes) {
-  BOX_OR_RETURN((B.pv.npart + 127) / 128)
+__global__ void k_move_wrap_multi(const BoxParticles* boxes) {
+  BOX_OR_RETURN((B.pv.npart + kSmallBlock - 1) / kSmallBlock)
   k_move_body(blockIdx.x, nblk, B.pv.npart, B.pp, B.ms);
-}
-__global__ void k_clear_first_multi(const BoxParticles* boxes) {
-  const BoxParticles& B = boxes[blockIdx.y];
-  if (B.pv.npart > 0 && threadIdx.x == 0) *B.ms.first_move = 0;
-}
-__global__ void k_wrap_multi(const BoxParticles* boxes) {
-  BOX_OR_RETURN((B.pv.npart + 127) / 128)
   k_wrap_body(blockIdx.x, nblk, B.g, B.pv.npart, B.ms);
 }
 __global__ void k_overlap_multi(const BoxParticles* boxes) {
   BOX_OR_RETURN((B.pv.npart * 32 + 127) / 128)
+  // the end of the first move, once every move of this box has read it
+  if (blockIdx.x == 0 && threadIdx.x == 0) *B.ms.first_move = 0;
   k_overlap_body(blockIdx.x, nblk, B.g, B.pv.npart, B.pp, B.ms, B.st);
 }
 // the new step's flags: every id -1, the solid mask clear; the refill list empty
@@ -1335,7 +1355,7 @@ __global__ void k_reset_multi(const BoxParticles* boxes) {
   if (blockIdx.x == 0 && threadIdx.x == 0) *B.fl.count = 0;
 }
 __global__ void k_link_sweeps_multi(const BoxParticles* boxes) {
-  BOX_OR_RETURN((3 * B.pv.npart + 127) / 128)
+  BOX_OR_RETURN((3 * B.pv.npart + kSmallBlock - 1) / kSmallBlock)
   k_link_sweeps_body(blockIdx.x, nblk, B.g, B.pv, B.ls);
 }
 __global__ void __launch_bounds__(PB) k_links_multi(const BoxParticles* boxes) {
@@ -1364,13 +1384,11 @@ void launch_particle_step_multi(const BoxParticles* boxes, int nb, int max_npart
   k_bounce_multi<<<grid(max_npart), PB, 0, s>>>(boxes); count_launch();
   k_bounce_store_multi<<<grid(max_npart), PB, 0, s>>>(boxes); count_launch();
   k_lubforce_multi<<<grid((max_npart * 32 + 127) / 128), 128, 0, s>>>(boxes); count_launch();
-  k_move_multi<<<grid((max_npart + 127) / 128), 128, 0, s>>>(boxes); count_launch();
-  k_clear_first_multi<<<grid(1), 32, 0, s>>>(boxes); count_launch();
-  k_wrap_multi<<<grid((max_npart + 127) / 128), 128, 0, s>>>(boxes); count_launch();
+  k_move_wrap_multi<<<grid((max_npart + kSmallBlock - 1) / kSmallBlock), kSmallBlock, 0, s>>>(boxes); count_launch();
   k_overlap_multi<<<grid((max_npart * 32 + 127) / 128), 128, 0, s>>>(boxes); count_launch();
   const long long rb = (max_reset + 256 * 8 - 1) / (256 * 8);
   k_reset_multi<<<grid(rb < 1024 ? rb : 1024), 256, 0, s>>>(boxes); count_launch();
-  k_link_sweeps_multi<<<grid((3 * max_npart + 127) / 128), 128, 0, s>>>(boxes); count_launch();
+  k_link_sweeps_multi<<<grid((3 * max_npart + kSmallBlock - 1) / kSmallBlock), kSmallBlock, 0, s>>>(boxes); count_launch();
   k_links_multi<<<grid(max_npart), PB, 0, s>>>(boxes); count_launch();
   k_fill_detect_multi<<<grid(max_npart), PB, 0, s>>>(boxes); count_launch();
   k_fill_events_multi<<<grid(kFillBlocks), 128, 0, s>>>(boxes); count_launch();
