@@ -36,6 +36,16 @@ __device__ __forceinline__ double near_img(double c, double p, int n, int nh) {
   return c;
 }
 __device__ __forceinline__ int wrapi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+// -v when neg, v otherwise, as a sign-bit flip: a negation that is not folded
+// into an arithmetic operand would otherwise cost an FP64 add, and FP64
+// issues at a few lanes per clock per SM on this GPU
+__device__ __forceinline__ double flip_if(bool neg, double v) {
+  return __longlong_as_double(
+      (long long)((unsigned long long)__double_as_longlong(v) ^ ((unsigned long long)neg << 63)));
+}
+__device__ __forceinline__ float flip_if(bool neg, float v) {
+  return __int_as_float((int)((unsigned)__float_as_int(v) ^ ((unsigned)neg << 31)));
+}
 template <typename R>
 __device__ __forceinline__ R near_img_t(R c, R p, int n, int nh) {
   if ((c - p) > R(nh)) c = c - R(n);
@@ -512,7 +522,7 @@ __device__ __forceinline__ void k_links_body(int bx, int gx, Geometry g, Particl
         alph32[w] = 1.0f - (-a0 + a1);
       } else {
         // the components of c are +-1 or 0: c . x1 is selects and one add
-        auto pick = [](int c, double v) { return c > 0 ? v : -v; };
+        auto pick = [](int c, double v) { return flip_if(c < 0, v); };
         const int lj = row_j[lr], lk = row_k[lr];
         const double xx1 = (double)(li + ix) - 0.5 - xval[min(lr, 2)][lci];
         const double yy1 = (double)(lj + iy) - 0.5 - row_y[lr];
@@ -521,11 +531,13 @@ __device__ __forceinline__ void k_links_body(int bx, int gx, Geometry g, Particl
         if (ix == 0) bb = iy == 0 ? pick(iz, zz1) : (iz == 0 ? pick(iy, yy1) : pick(iy, yy1) + pick(iz, zz1));
         else bb = iy != 0 ? pick(ix, xx1) + pick(iy, yy1)
                           : (iz != 0 ? pick(ix, xx1) + pick(iz, zz1) : pick(ix, xx1));
-        bb = -bb;
+        // the reference's bb is -(c . x1); its negation folded into a0
         const double cc = fma(xx1, xx1, fma(yy1, yy1, fma(zz1, zz1, -rad2)));
-        const double a0 = diag ? 0.5 * bb : bb;
+        const double a0 = diag ? -0.5 * bb : flip_if(true, bb);
         const double ca = diag ? 0.5 * cc : cc;
-        const double a1 = sqrt(fmax(fma(a0, a0, -ca), 0.0));
+        // max(disc, 0) by the sign bit (an integer select)
+        const double disc = fma(a0, a0, -ca);
+        const double a1 = sqrt(__double_as_longlong(disc) < 0 ? 0.0 : disc);
         alph[w] = 1.0 - (-a0 + a1);
       }
     }
@@ -602,14 +614,19 @@ __device__ __forceinline__ T read_post(const Geometry& g, const T* f, int pushed
   return f[q * N + it + g.nx * (jt + g.ny * kt)];
 }
 
-// beads_collision for one particle per block: every link computes the
-// bounced population f9 (stored per link) and its momentum exchange.
+// threads per particle block of the bounce-back: FP64 links are FP64-pipe
+// bound, and 128 threads leave fewer idle lanes in the last pass over a
+// particle's ~1000 links than 256
 template <typename T>
+constexpr int bounce_threads() { return sizeof(T) == 8 ? 128 : PB; }
+
+// beads_collision for one particle per block of NT threads: every link
+// computes the bounced population f9 (stored per link) and its momentum
+// exchange.
+template <typename T, int NT>
 __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, ParticleView pv, const T* f, int pushed,
                                                const int32_t* __restrict__ isnodes, LinkSlab ls,
                                                double* fHIp, double* torqp) {
-  using Red = cub::BlockReduce<double, PB>;
-  __shared__ typename Red::TempStorage red_tmp;
   const int p = bx;
   if (p >= pv.npart) return;
   const int cnt = ls.count[p];
@@ -636,13 +653,13 @@ __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, Partic
   __shared__ R tdel[3][kBounceSpan];
   __shared__ R tcw[NPOP];
   // c_a v with c_a in {-1, 0, 1}: exact, so selected rather than multiplied
-  auto sel = [](int c, R v) { return c == 0 ? R(0) : (c > 0 ? v : -v); };
+  auto sel = [](int c, R v) { return c == 0 ? R(0) : flip_if(c < 0, v); };
   int lo[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) lo[a] = (int)floor((double)pv.ypglb[3 * p + a]) - (kBounceSpan / 2);
   {
     // selects rather than arrays indexed by a, which would live in local memory
-    for (int t = threadIdx.x; t < 3 * kBounceSpan; t += PB) {
+    for (int t = threadIdx.x; t < 3 * kBounceSpan; t += NT) {
       const int a = t / kBounceSpan, d = t - a * kBounceSpan;
       const bool periodic = !(channel && a == 0);
       const R cen = a == 0 ? xc0 : (a == 1 ? yc0 : zc0);
@@ -668,12 +685,12 @@ __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, Partic
   };
   // cb db - cc dc for cb, cc in {-1, 0, 1}: one add at most
   auto cross = [](int cb, R db, int cc, R dc) -> R {
-    const R u = cb == 0 ? R(0) : (cb > 0 ? db : -db);
+    const R u = cb == 0 ? R(0) : flip_if(cb < 0, db);
     if (cc == 0) return u;
-    const R v = cc > 0 ? dc : -dc;
-    return cb == 0 ? -v : u - v;
+    const R v = flip_if(cc < 0, dc);
+    return cb == 0 ? flip_if(true, v) : u - v;
   };
-  for (int l = threadIdx.x; l < cnt; l += PB) {
+  for (int l = threadIdx.x; l < cnt; l += NT) {
     // 32-bit decode: node < 2^26
     const int cd = code[l];
     const int ipop = cd & 31;
@@ -721,7 +738,11 @@ __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, Partic
     //     x - c solid:  c1 = 1 / (2 alpha), c2 = 1 - c1
     //     else:         c1 = 1 / (alpha (2 alpha + 1)),
     //                   c2 = (2 alpha - 1)(2 alpha + 1) c1, c3 = 1 - c1 - c2
-    const bool low = alpha <= R(0.5);
+    // alpha <= 1/2 on the bit patterns (an integer compare; the same outcome
+    // for every alpha but a NaN with the sign bit set)
+    bool low;
+    if constexpr (sizeof(R) == 8) low = __double_as_longlong(alpha) <= __double_as_longlong(0.5);
+    else low = __float_as_int(alpha) <= __float_as_int(0.5f);
     int ibm1 = 2, ibm2 = 2;
     if (!out1) ibm1 = is_solid(mask, g, km1 * g.ny + jm1, im1) ? 1 : -1;
     if (low && !out2) ibm2 = is_solid(mask, g, km2 * g.ny + jm2, im2) ? 1 : -1;
@@ -757,9 +778,9 @@ __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, Partic
     const R f9 = fma_r(c1, ff1, fma_r(c2, ff2, fma_r(c3, ff3, -(k6 * c4) * uwpro)));
     f9s[l] = f9;
     const R dff = ff1 + f9;
-    if (ix) acc6[0].add(sel(ix, dff));
-    if (iy) acc6[1].add(sel(iy, dff));
-    if (iz) acc6[2].add(sel(iz, dff));
+    if (ix) acc6[0].add(flip_if(ix < 0, dff));
+    if (iy) acc6[1].add(flip_if(iy < 0, dff));
+    if (iz) acc6[2].add(flip_if(iz < 0, dff));
     acc6[3].add_prod(dff, ex);
     acc6[4].add_prod(dff, ey);
     acc6[5].add_prod(dff, ez);
@@ -767,7 +788,7 @@ __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, Partic
   if constexpr (sizeof(T) == 4) {
     // per warp: exact two-sum tree of the compensated FP32 partial sums;
     // across warps: FP64 in a fixed order (deterministic)
-    __shared__ double wsum[6][PB / 32];
+    __shared__ double wsum[6][NT / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
@@ -788,25 +809,35 @@ __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, Partic
     if (threadIdx.x < 6) {
       const int c = threadIdx.x;
       double s = 0.0;
-      for (int w = 0; w < PB / 32; ++w) s += wsum[c][w];
+      for (int w = 0; w < NT / 32; ++w) s += wsum[c][w];
       if (c < 3) fHIp[3 * p + c] = s; else torqp[3 * p + c - 3] = s;
     }
   } else {
+    // the threads' six partial sums through shared memory; one warp per
+    // component adds NT / 32 of them a lane, then the lanes by an xor
+    // butterfly (a fixed order: deterministic)
+    __shared__ double part[6][NT];
 #pragma unroll
-    for (int c = 0; c < 6; ++c) {
-      double s = Red(red_tmp).Sum(acc6[c].value());
-      __syncthreads();
-      if (threadIdx.x == 0) {
+    for (int c = 0; c < 6; ++c) part[c][threadIdx.x] = acc6[c].value();
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int c = warp; c < 6; c += NT / 32) {
+      double s = part[c][lane];
+#pragma unroll
+      for (int w = 1; w < NT / 32; ++w) s += part[c][lane + 32 * w];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) {
         if (c < 3) fHIp[3 * p + c] = s; else torqp[3 * p + c - 3] = s;
       }
     }
   }
 }
 template <typename T>
-__global__ void __launch_bounds__(PB) k_bounce(Geometry g, ParticleView pv, const T* f, int pushed,
+__global__ void __launch_bounds__(bounce_threads<T>()) k_bounce(Geometry g, ParticleView pv, const T* f, int pushed,
                                                const int32_t* __restrict__ isnodes, LinkSlab ls,
                                                double* fHIp, double* torqp) {
-  k_bounce_body<T>(blockIdx.x, gridDim.x, g, pv, f, pushed, isnodes, ls, fHIp, torqp);
+  k_bounce_body<T, bounce_threads<T>()>(blockIdx.x, gridDim.x, g, pv, f, pushed, isnodes, ls, fHIp, torqp);
 }
 
 // the bounce-back stores of beads_collision: f(ipp, x + c) = f9
@@ -1173,7 +1204,12 @@ __device__ __forceinline__ void k_fill_events_body(int bx, int gx, Geometry g, P
     int ipmx = 0;
 #pragma unroll
     for (int ipop = 1; ipop < NPOP; ++ipop) {
-      R prod = R(cix(ipop)) * xx0 + R(ciy(ipop)) * yy0 + R(ciz(ipop)) * zz0;
+      // c . x0 with the zero terms left out (the same value, fewer FP64 ops)
+      const int cx = cix(ipop), cy = ciy(ipop), cz = ciz(ipop);
+      auto term = [](int c, R v) { return flip_if(c < 0, v); };
+      R prod = cx ? term(cx, xx0) : R(0);
+      if (cy) prod = cx ? prod + term(cy, yy0) : term(cy, yy0);
+      if (cz) prod = (cx || cy) ? prod + term(cz, zz0) : term(cz, zz0);
       if (ipop <= 6) prod = prod * sq2;
       if (prod > prod0) { ipmx = ipop; prod0 = prod; }
     }
@@ -1261,7 +1297,7 @@ void launch_bounce_back(const Geometry& g, const ParticleView& pv, const T* f, i
                         const int32_t* isnodes, LinkSlab ls, double* fHIp, double* torqp,
                         cudaStream_t s) {
   if (pv.npart <= 0) return;
-  { k_bounce<T><<<pv.npart, PB, 0, s>>>(g, pv, f, pushed, isnodes, ls, fHIp, torqp); count_launch(); }
+  { k_bounce<T><<<pv.npart, bounce_threads<T>(), 0, s>>>(g, pv, f, pushed, isnodes, ls, fHIp, torqp); count_launch(); }
 }
 
 template <typename T>
@@ -1319,7 +1355,7 @@ namespace {
 
 __global__ void __launch_bounds__(PB) k_bounce_multi(const BoxParticles* boxes) {
   BOX_OR_RETURN(B.pv.npart)
-  k_bounce_body<float>(blockIdx.x, nblk, B.g, B.pv, B.f, 1, B.flags_cur, B.ls, B.ms.fHIp, B.ms.torqp);
+  k_bounce_body<float, PB>(blockIdx.x, nblk, B.g, B.pv, B.f, 1, B.flags_cur, B.ls, B.ms.fHIp, B.ms.torqp);
 }
 __global__ void __launch_bounds__(PB) k_bounce_store_multi(const BoxParticles* boxes) {
   BOX_OR_RETURN(B.pv.npart)
