@@ -422,7 +422,8 @@ void particle_phase(lbm_ctx* c, T* f_plain) {
   }
   prof_begin(c);
   if (!pre) launch_lubforce(c->g, c->npart, c->pp, mstate(c), c->stream);
-  launch_move_redistribute(c->g, c->npart, c->pp, mstate(c), c->status, c->stream);
+  const bool ovl_aux = launch_move_redistribute(c->g, c->npart, c->pp, mstate(c), c->status,
+                                                c->stream, c->aux, c->ev_aux_fork, c->ev_aux_join);
   prof_end(c, LBM_PHASE_PARTICLES);
   int nf = 1 - c->fcur;
   prof_begin(c);
@@ -433,6 +434,7 @@ void particle_phase(lbm_ctx* c, T* f_plain) {
   launch_filling<T>(c->g, pview(c), c->pp, c->ypglbp, c->wpp, c->omgpp, c->flags[nf],
                     c->flags[c->fcur], f_plain, c->fill, c->status, c->stream);
   prof_end(c, LBM_PHASE_FILLING);
+  if (ovl_aux) cudaStreamWaitEvent(c->stream, c->ev_aux_join, 0);  // the overlap check
   c->fcur = nf;
 }
 

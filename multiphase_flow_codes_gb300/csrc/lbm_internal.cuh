@@ -311,9 +311,13 @@ void launch_move(const Geometry& g, int npart, const PartParams& pp, MoveState m
 void launch_redistribute(const Geometry& g, int npart, const PartParams& pp, MoveState ms,
                          DevStatus* st, cudaStream_t s);
 // launch_move then launch_redistribute in two launches: the move and the wrap
-// of a particle in one thread, the overlap check ending the first move
-void launch_move_redistribute(const Geometry& g, int npart, const PartParams& pp, MoveState ms,
-                              DevStatus* st, cudaStream_t s);
+// of a particle in one thread, then the overlap check (which also ends the
+// first move).  The check only reports; with an aux stream it runs there,
+// forked after the move by `fork` and recorded into `join`, beside the link
+// kernels that follow on s (returns true: the caller joins `join`).
+bool launch_move_redistribute(const Geometry& g, int npart, const PartParams& pp, MoveState ms,
+                              DevStatus* st, cudaStream_t s, cudaStream_t aux = nullptr,
+                              cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
 // refill events of one step: node index and particle id per event
 struct FillList {
   int32_t* node;

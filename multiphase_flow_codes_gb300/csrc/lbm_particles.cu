@@ -1327,11 +1327,20 @@ void launch_redistribute(const Geometry& g, int npart, const PartParams& pp, Mov
   { k_overlap<<<(npart * 32 + 127) / 128, 128, 0, s>>>(g, npart, pp, ms, st, nullptr); count_launch(); }
 }
 
-void launch_move_redistribute(const Geometry& g, int npart, const PartParams& pp, MoveState ms,
-                              DevStatus* st, cudaStream_t s) {
-  if (npart <= 0) return;
+bool launch_move_redistribute(const Geometry& g, int npart, const PartParams& pp, MoveState ms,
+                              DevStatus* st, cudaStream_t s, cudaStream_t aux, cudaEvent_t fork,
+                              cudaEvent_t join) {
+  if (npart <= 0) return false;
   { k_move_wrap<<<(npart + kSmallBlock - 1) / kSmallBlock, kSmallBlock, 0, s>>>(g, npart, pp, ms); count_launch(); }
-  { k_overlap<<<(npart * 32 + 127) / 128, 128, 0, s>>>(g, npart, pp, ms, st, ms.first_move); count_launch(); }
+  cudaStream_t so = s;
+  if (aux) {
+    cudaEventRecord(fork, s);
+    cudaStreamWaitEvent(aux, fork, 0);
+    so = aux;
+  }
+  { k_overlap<<<(npart * 32 + 127) / 128, 128, 0, so>>>(g, npart, pp, ms, st, ms.first_move); count_launch(); }
+  if (aux) cudaEventRecord(join, aux);
+  return aux != nullptr;
 }
 
 template <typename T>
