@@ -94,12 +94,32 @@ __device__ SweepEv sweep_events(double c, int n, int nh) {
     if ((c - p1) > dnh) {
       jn = j + 1;
     } else if ((c - ((double)n - 0.5)) < -dnh) {
+      // the first point m in [j + 1, n] where the shift up fires.  In exact
+      // arithmetic that is the first m > c + n/2 + 1/2, and fl(c - p) is
+      // within an ulp of c - p, so the FP64 first point lies within two of
+      // floor(c + n/2 + 1/2) + 1: scan from two below it with the
+      // reference's expression (monotone in m) after checking that the start
+      // is not past it; bisect where either check fails (not expected).
+      auto up = [&](int m) { return (c - ((double)m - 0.5)) < -dnh; };
       int lo = j + 1, hi = n;
-      while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if ((c - ((double)mid - 0.5)) < -dnh) hi = mid; else lo = mid + 1;
+      int m = (int)floor(c + dnh + 0.5) - 1;
+      m = m < lo ? lo : (m > hi ? hi : m);
+      bool found = false;
+      if (m == lo || !up(m - 1)) {
+        for (int t = 0; t < 6 && m <= hi; ++t, ++m)
+          if (up(m)) { found = true; break; }
+        if (!found) lo = m;
+      } else {
+        hi = m - 1;
       }
-      jn = lo;
+      if (!found) {
+        while (lo < hi) {
+          int mid = (lo + hi) >> 1;
+          if (up(mid)) hi = mid; else lo = mid + 1;
+        }
+        m = lo;
+      }
+      jn = m;
     }
     if (jn > n) return s;
     j = jn;
