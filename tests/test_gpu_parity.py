@@ -196,3 +196,56 @@ def test_mass_momentum(require_gpu, oracle_mod):
     ref = [f.sum(), np.tensordot(CIX, f, axes=(0, 0)).sum(), np.tensordot(CIY, f, axes=(0, 0)).sum(),
            np.tensordot(CIZ, f, axes=(0, 0)).sum()]
     assert np.allclose(mm, ref, atol=1e-12)
+
+
+def _bounce_cases(o):
+    """Counts of beads_collision's five interpolation cases over the oracle's
+    links: (alpha <= 1/2: x - c solid, x - 2c solid, neither;
+    alpha > 1/2: x - c solid, not)."""
+    from conftest import CIX, CIY, CIZ
+    part, node, ipop, alpha = oracle_links(o)
+    nx, ny, nz = o.nx, o.ny, o.nz
+    i, j, k = node % nx, (node // nx) % ny, node // (nx * ny)
+    solid = o.ibnodes > 0
+
+    def at(s):
+        return solid[(k - s * CIZ[ipop]) % nz, (j - s * CIY[ipop]) % ny, (i - s * CIX[ipop]) % nx]
+
+    s1, s2, low = at(1), at(2), alpha <= 0.5
+    return [int((low & s1).sum()), int((low & ~s1 & s2).sum()), int((low & ~s1 & ~s2).sum()),
+            int((~low & s1).sum()), int((~low & ~s1).sum())]
+
+
+def test_bounce_cases_near_contact(require_gpu, oracle_mod):
+    """Two spheres 0.6 lattice units apart (inside the lubrication range) and
+    a third alone: the links in the gap see solid nodes at x - c and x - 2c,
+    so every interpolation case of the bounce-back runs; populations, forces
+    and torques against the oracle over 10 steps."""
+    shape = (40, 36, 36)
+    y = np.array([[12.2, 18.3, 17.9], [20.8, 18.6, 18.1], [30.0, 8.0, 26.0]])
+    wp = np.array([[0.01, -0.01, 0.0], [-0.01, 0.01, 0.01], [0.0, 0.03, -0.02]])
+    om = np.array([[0.0, 0.004, -0.002], [0.003, 0.0, 0.001], [0.0, 0.0, 0.005]])
+    from multiphase_flow_codes_gb300.engine import LBMBox
+    cfg = capi.config_init(capi.LBM_PRESET_BOX, *shape, 3, 4.0, 2.5)
+    o = oracle_mod.OracleBox(cfg)
+    u = inputs.spectral_velocity(shape[0], 4.0, 0.03, ny=shape[1], nz=shape[2])
+    o.initpop(*u)
+    o.macrovar()
+    box = LBMBox(cfg)
+    box.set_f(o.f.copy())
+    box.macrovar()
+    o.release_particles(y, wp, om)
+    box.release_particles(y, wp, om)
+    cases = _bounce_cases(o)
+    assert min(cases) > 0, cases
+    for s in range(10):
+        o.step(1)
+        box.step(1)
+        check_flags(o, box)
+        if s == 0:  # the step whose bounce-back ran on the links above
+            assert relerr(box.get_particles()["fHIp"], o.fHIp) <= 1e-10
+    assert relerr(box.get_f(), o.f) <= TOL64
+    p = box.get_particles()
+    assert relerr(p["ypglb"], o.ypglb) <= TOL64
+    assert relerr(p["fHIp"], o.fHIp) <= 1e-10
+    assert relerr(p["omgp"], o.omgp) <= 1e-10
