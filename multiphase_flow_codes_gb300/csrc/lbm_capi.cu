@@ -48,8 +48,9 @@ struct lbm_ctx {
   // (the new flag buffer's reset, beads_lubforce) runs here beside the
   // bounce-back (particle_phase)
   cudaStream_t aux = nullptr;
-  cudaEvent_t ev_aux_fork = nullptr, ev_aux_join = nullptr;
+  cudaEvent_t ev_aux_fork = nullptr, ev_aux_join = nullptr, ev_store = nullptr;
   bool aux_pending = false;
+  bool store_pending = false;  // the bounce-back stores run on aux until ev_store
   bool prefetched = false;
   int prefetch_slot = 0;
   ForcingDev* d_forcing_backup = nullptr;
@@ -412,6 +413,19 @@ void particle_prelude(lbm_ctx* c) {
   c->aux_pending = true;
 }
 
+// The bounce-back stores of a fused step (beads_collision's writes) on the
+// aux stream: they must land before beads_links rewrites the link slab they
+// read and before beads_filling reads populations, so beads_move and the link
+// sweeps run beside them; particle_phase joins them before the links.
+template <typename T>
+void bounce_store_aux(lbm_ctx* c, T* fout) {
+  cudaEventRecord(c->ev_aux_fork, c->stream);
+  cudaStreamWaitEvent(c->aux, c->ev_aux_fork, 0);
+  launch_bounce_scatter<T>(c->g, pview(c), fout, 1, c->links, c->aux);
+  cudaEventRecord(c->ev_store, c->aux);
+  c->store_pending = true;
+}
+
 template <typename T>
 void particle_phase(lbm_ctx* c, T* f_plain) {
   // beads_lubforce, beads_move, beads_redistribute, beads_links, beads_filling
@@ -428,6 +442,10 @@ void particle_phase(lbm_ctx* c, T* f_plain) {
   int nf = 1 - c->fcur;
   prof_begin(c);
   if (!pre) reset_flags(c, nf);
+  if (c->store_pending) {
+    cudaStreamWaitEvent(c->stream, c->ev_store, 0);
+    c->store_pending = false;
+  }
   launch_links(c->g, pview(c), c->flags[nf], c->links, c->status, c->f32, c->stream);
   prof_end(c, LBM_PHASE_LINKS);
   prof_begin(c);
@@ -495,8 +513,8 @@ void step_post_t(lbm_ctx* c) {
     prof_begin(c);
     launch_bounce_back<T>(c->g, pview(c), fout, 1, c->flags[c->fcur], c->links, c->fHIp,
                           c->torqp, c->stream);
-    launch_bounce_scatter<T>(c->g, pview(c), fout, 1, c->links, c->stream);
     prof_end(c, LBM_PHASE_BOUNCE);
+    bounce_store_aux<T>(c, fout);
     particle_phase<T>(c, fout);
   } else {
     // without particles both flag buffers say "all fluid"; flipping keeps
@@ -523,8 +541,8 @@ void fused_step_t(lbm_ctx* c) {
     prof_begin(c);
     launch_bounce_back<T>(c->g, pview(c), fout, 1, c->flags[c->fcur], c->links, c->fHIp,
                           c->torqp, c->stream);
-    launch_bounce_scatter<T>(c->g, pview(c), fout, 1, c->links, c->stream);
     prof_end(c, LBM_PHASE_BOUNCE);
+    bounce_store_aux<T>(c, fout);
     particle_phase<T>(c, fout);
   } else {
     c->fcur = 1 - c->fcur;  // as step_post_t
@@ -792,7 +810,13 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
     return true;
   };
   const long long N = g.N;
-  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+  // The engine's own stream at the greatest priority: the block scheduler
+  // then prefers the critical path (stream + collide, bounce-back, move,
+  // links, filling) over the side and aux streams' kernels (forcing,
+  // lubrication, overlap check, bounce-back stores), which have slack.
+  int prio_least = 0, prio_greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+  if (cudaStreamCreateWithPriority(&ctx->stream, cudaStreamNonBlocking, prio_greatest) != cudaSuccess) {
     delete ctx;
     return LBM_ERR_CUDA;
   }
@@ -801,6 +825,7 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
       cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->ev_aux_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->ev_aux_join, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_store, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->ev_main, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->ev_forcing, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&ctx->ev_status, cudaEventDisableTiming) != cudaSuccess) {
@@ -978,7 +1003,7 @@ int lbm_destroy(lbm_ctx* ctx) {
   if (ctx->side) cudaStreamDestroy(ctx->side);
   if (ctx->aux) cudaStreamDestroy(ctx->aux);
   for (cudaEvent_t e : {ctx->ev_main, ctx->ev_forcing, ctx->ev_status, ctx->ev_aux_fork,
-                        ctx->ev_aux_join})
+                        ctx->ev_aux_join, ctx->ev_store})
     if (e) cudaEventDestroy(e);
   delete ctx;
   return LBM_OK;

@@ -866,8 +866,8 @@ __global__ void __launch_bounds__(bounce_threads<T>()) k_bounce(Geometry g, Part
 template <typename T>
 __device__ __forceinline__ void k_bounce_store_body(int bx, int gx, Geometry g, ParticleView pv, T* f, int pushed,
                                                      LinkSlab ls) {
-  const int p = bx;
-  if (p >= pv.npart) return;
+  // particles bx, bx + gx, ...
+  for (int p = bx; p < pv.npart; p += gx) {
   const int cnt = ls.count[p];
   const int32_t* code = ls.code + (long long)p * ls.cap;
   const T* f9s = reinterpret_cast<const T*>(ls.f9 + (long long)p * ls.cap);
@@ -890,6 +890,7 @@ __device__ __forceinline__ void k_bounce_store_body(int bx, int gx, Geometry g, 
       int jt = wrapi(j + ciy(ipop), g.ny), kt = wrapi(k + ciz(ipop), g.nz);
       f[ipp * g.N + (long long)it + (long long)g.nx * (jt + (long long)g.ny * kt)] = f9s[l];
     }
+  }
   }
 }
 template <typename T>
@@ -1324,7 +1325,18 @@ template <typename T>
 void launch_bounce_scatter(const Geometry& g, const ParticleView& pv, T* f, int pushed,
                            LinkSlab ls, cudaStream_t s) {
   if (pv.npart <= 0) return;
-  { k_bounce_store<T><<<pv.npart, PB, 0, s>>>(g, pv, f, pushed, ls); count_launch(); }
+  // four blocks per SM, looping over particles: the stores run beside the
+  // particle kernels of the critical path and leave half of every SM's
+  // thread slots to them
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+      sms = 1;
+  }
+  const int nblk = pv.npart < 4 * sms ? pv.npart : 4 * sms;
+  { k_bounce_store<T><<<nblk, PB, 0, s>>>(g, pv, f, pushed, ls); count_launch(); }
 }
 
 void launch_lubforce(const Geometry& g, int npart, const PartParams& pp, MoveState ms,
