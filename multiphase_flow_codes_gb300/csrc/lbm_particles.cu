@@ -1162,15 +1162,41 @@ __device__ __forceinline__ int warp_sum(int v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
+// Warp sums of four values, every lane getting all four, in six adds a lane
+// instead of twenty: the first two butterfly levels halve the values a lane
+// carries (lanes below 16 keep a and b, the others c and d; then bit 8 picks
+// one of the two), the last three sum the one value left; a fixed order, so
+// deterministic.  Lane 0, 8, 16, 24 end with the sum of a, b, c, d.
+template <typename R>
+__device__ __forceinline__ void warp_sum4(R& a, R& b, R& c, R& d) {
+  const int lane = threadIdx.x & 31;
+  const bool lo16 = lane < 16;
+  R u = lo16 ? a : c, v = lo16 ? b : d;
+  u += __shfl_xor_sync(0xffffffffu, lo16 ? c : a, 16);
+  v += __shfl_xor_sync(0xffffffffu, lo16 ? d : b, 16);
+  const bool lo8 = (lane & 8) == 0;
+  R w = lo8 ? u : v;
+  w += __shfl_xor_sync(0xffffffffu, lo8 ? v : u, 8);
+#pragma unroll
+  for (int o = 4; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+  a = __shfl_sync(0xffffffffu, w, 0);
+  b = __shfl_sync(0xffffffffu, w, 8);
+  c = __shfl_sync(0xffffffffu, w, 16);
+  d = __shfl_sync(0xffffffffu, w, 24);
+}
 
 // equilibrium of one population, feqpnt (B/partlib.f90:3222-3247)
+// (the same expression with c . u from selected components and FMAs: values
+// to rounding, fewer FP64 instructions)
 template <typename R>
 __device__ __forceinline__ R feq_q(int q, R u9, R v9, R w9, R rho9) {
-  R usqr = R(1.5) * (u9 * u9 + v9 * v9 + w9 * w9);
+  const R usqr = R(1.5) * fma_r(u9, u9, fma_r(v9, v9, w9 * w9));
   if (q == 0) return R(1.0 / 3.0) * (rho9 - usqr);
-  R G = R(cix(q)) * u9 + R(ciy(q)) * v9 + R(ciz(q)) * w9;
-  R wq = q <= 6 ? R(1.0 / 18.0) : R(1.0 / 36.0);
-  return wq * (rho9 + R(3.0) * G + R(4.5) * G * G - usqr);
+  const int cx = cix(q), cy = ciy(q), cz = ciz(q);
+  const R G = (cx == 0 ? R(0) : flip_if(cx < 0, u9)) + (cy == 0 ? R(0) : flip_if(cy < 0, v9)) +
+              (cz == 0 ? R(0) : flip_if(cz < 0, w9));
+  const R wq = q <= 6 ? R(1.0 / 18.0) : R(1.0 / 36.0);
+  return wq * (fma_r(R(4.5) * G, G, fma_r(R(3.0), G, rho9)) - usqr);
 }
 
 template <typename T>
@@ -1211,8 +1237,9 @@ __device__ __forceinline__ void k_fill_events_body(int bx, int gx, Geometry g, P
     const R aa = w1 * w1 + w2 * w2 + w3 * w3;
     const R bb = dx * w1 + dy * w2 + dz * w3;
     const R cc = dx * dx + dy * dy + dz * dz - R(rad) * R(rad);
-    const R ddt0 = bb / aa;
-    const R ddt1 = sqrt(ddt0 * ddt0 - cc / aa);
+    const R inv_aa = R(1) / aa;  // one division for bb / aa and cc / aa
+    const R ddt0 = bb * inv_aa;
+    const R ddt1 = sqrt(ddt0 * ddt0 - cc * inv_aa);
     R ddt = -ddt0 + ddt1;
     if (ddt < R(0)) ddt = R(0);
     if (ddt > R(1)) ddt = R(1);
@@ -1254,10 +1281,11 @@ __device__ __forceinline__ void k_fill_events_body(int bx, int gx, Geometry g, P
       }
       if (have) {
         const R fq = lane < NPOP ? R(f[(size_t)q * g.N + m]) : R(0);
-        const R rho9 = warp_sum(fq);
-        const R u9 = warp_sum(R(cix(q)) * fq);
-        const R v9 = warp_sum(R(ciy(q)) * fq);
-        const R ww9 = warp_sum(R(ciz(q)) * fq);
+        R rho9 = fq;
+        R u9 = cix(q) == 0 ? R(0) : flip_if(cix(q) < 0, fq);
+        R v9 = ciy(q) == 0 ? R(0) : flip_if(ciy(q) < 0, fq);
+        R ww9 = ciz(q) == 0 ? R(0) : flip_if(ciz(q) < 0, fq);
+        warp_sum4(rho9, u9, v9, ww9);
         fnew = fq - feq_q<R>(q, u9, v9, ww9, rho9);
       }
     }
@@ -1383,7 +1411,16 @@ void launch_filling(const Geometry& g, const ParticleView& pv, const PartParams&
   if (pv.npart <= 0) return;
   cudaMemsetAsync(fl.count, 0, sizeof(int), s);
   { k_fill_detect<<<pv.npart, PB, 0, s>>>(g, pv, pp, ypglbp, isnodes, isnodes0, fl, st); count_launch(); }
-  { k_fill_events<T><<<4 * 152, 128, 0, s>>>(g, pv, pp, ypglbp, wpp, omgpp, isnodes, isnodes0, f, fl); count_launch(); }
+  // eight blocks of four warps per SM: one refill event per warp for up to
+  // 32 events an SM (the events' serial FP64 chains then run side by side)
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+      sms = 1;
+  }
+  { k_fill_events<T><<<8 * sms, 128, 0, s>>>(g, pv, pp, ypglbp, wpp, omgpp, isnodes, isnodes0, f, fl); count_launch(); }
 }
 
 // ---- many boxes per launch ------------------------------------------------
