@@ -195,8 +195,28 @@ ForceView<T> fview(lbm_ctx* c, const ForceState& s) {
   return v;
 }
 
+// The FP64 plain path keeps the current populations in 64-bit fixed point
+// between its fused steps (g.pop_fixed; lbm_collide.cuh): its collision then
+// loads and stores the integers it computes with.  Every other use of the
+// current buffer goes through fbuf, which converts it back to FP64 first.
+void pop_format(lbm_ctx* c, bool fixed) {
+  if ((c->g.pop_fixed != 0) == fixed || c->f32) return;
+  launch_pop_format(static_cast<double*>(c->f[c->cur]), 19 * c->g.N, fixed, c->status, c->stream);
+  c->g.pop_fixed = fixed ? 1 : 0;
+}
+// the fused steps that run on fixed-point populations: FP64, fixed-point
+// sums, the direct stream + collide kernel
+bool fixed_path(const lbm_ctx* c) {
+  return !c->f32 && c->sums == LBM_SUMS_FIXED && c->variant == LBM_VARIANT_DIRECT;
+}
 template <typename T>
-T* fbuf(lbm_ctx* c, int i) { return static_cast<T*>(c->f[i]); }
+T* fbuf(lbm_ctx* c, int i) {
+  if (i == c->cur && c->g.pop_fixed) pop_format(c, false);
+  return static_cast<T*>(c->f[i]);
+}
+// the buffer as stored (the fused fixed-point step)
+template <typename T>
+T* fraw(lbm_ctx* c, int i) { return static_cast<T*>(c->f[i]); }
 template <typename T>
 T* mbuf(lbm_ctx* c, int comp) { return static_cast<T*>(c->macro) + comp * c->g.N; }
 
@@ -421,7 +441,7 @@ template <typename T>
 void bounce_store_aux(lbm_ctx* c, T* fout) {
   cudaEventRecord(c->ev_aux_fork, c->stream);
   cudaStreamWaitEvent(c->aux, c->ev_aux_fork, 0);
-  launch_bounce_scatter<T>(c->g, pview(c), fout, 1, c->links, c->aux);
+  launch_bounce_scatter<T>(c->g, pview(c), fout, 1, c->links, c->aux, c->status);
   cudaEventRecord(c->ev_store, c->aux);
   c->store_pending = true;
 }
@@ -474,9 +494,19 @@ void launch_stream_collide(lbm_ctx* c, const T* fin, T* fout, bool use_cache = f
                      c->slot_version[c->fcache_slot] == c->fcache_version;
     mode = hit ? 2 : 1;
   }
-  launch_fused_step<T>(c->g, c->r, fin, fout, c->flags[c->fcur], fview<T>(c, c->fmacro),
-                       fview<T>(c, c->latest), fx, reinterpret_cast<T*>(c->fcache), mode,
-                       c->stream);
+  bool done = false;
+  if constexpr (sizeof(T) == 8) {
+    if (c->g.pop_fixed) {  // fin and fout in fixed point (fixed_path)
+      launch_fused_fixed(c->g, c->r, fin, fout, c->flags[c->fcur], fview<T>(c, c->fmacro),
+                         fview<T>(c, c->latest), reinterpret_cast<T*>(c->fcache), mode,
+                         c->status, c->stream);
+      done = true;
+    }
+  }
+  if (!done)
+    launch_fused_step<T>(c->g, c->r, fin, fout, c->flags[c->fcur], fview<T>(c, c->fmacro),
+                         fview<T>(c, c->latest), fx, reinterpret_cast<T*>(c->fcache), mode,
+                         c->stream);
   if (use_cache) {
     c->fcache_slot = mode ? c->latest.slot : -1;
     c->fcache_version = mode ? c->slot_version[c->latest.slot] : 0;
@@ -530,8 +560,10 @@ void step_post_t(lbm_ctx* c) {
 template <typename T>
 void fused_step_t(lbm_ctx* c) {
   do_forcing(c);
-  T* fin = fbuf<T>(c, c->cur);
-  T* fout = fbuf<T>(c, 1 - c->cur);
+  const bool fixed = fixed_path(c);
+  if (fixed) pop_format(c, true);
+  T* fin = fixed ? fraw<T>(c, c->cur) : fbuf<T>(c, c->cur);
+  T* fout = fraw<T>(c, 1 - c->cur);
   prof_begin(c);
   launch_stream_collide<T>(c, fin, fout, true);
   prof_end(c, LBM_PHASE_STREAM_COLLIDE);
@@ -1798,8 +1830,13 @@ int lbm_autotune(lbm_ctx* ctx, int reps, double* best_ms) {
   for (size_t i = 0; i < cands.size(); ++i) {
     ctx->variant = cands[i].variant;
     ctx->staged = cands[i].p;
+    // the direct FP64 candidate is timed on fixed-point populations, as its
+    // fused steps run
+    if (fixed_path(ctx)) pop_format(ctx, true);
     auto run = [&]() {
       if (ctx->f32) launch_stream_collide<float>(ctx, fbuf<float>(ctx, ctx->cur), fbuf<float>(ctx, 1 - ctx->cur));
+      else if (ctx->g.pop_fixed)
+        launch_stream_collide<double>(ctx, fraw<double>(ctx, ctx->cur), fraw<double>(ctx, 1 - ctx->cur));
       else launch_stream_collide<double>(ctx, fbuf<double>(ctx, ctx->cur), fbuf<double>(ctx, 1 - ctx->cur));
     };
     run();

@@ -306,16 +306,15 @@ __host__ __device__ __forceinline__ unsigned fx_out_of_range(long long x) {
 // products rounded once (RatesT::Li); only the terms with velocities and
 // forces stay FP64.  Returns false, leaving f as it was, when a value is
 // out of the fixed-point ranges.
-__host__ __device__ __forceinline__ bool collide_fx(double (&f)[NPOP], double fpx, double fpy,
-                                                    double fpz, double fx, double fy, double fz,
-                                                    const RatesT<double>& r) {
+//
+// fx_core is the part between the conversions: g the populations at scale
+// 2^-kFxIn (|g| < 2^(kFxIn + kFxInMax)), h the post-collision populations at
+// 2^-kFxOut; false when a moment leaves its range.
+__host__ __device__ __forceinline__ bool fx_core(const long long (&g)[NPOP], double fpx, double fpy,
+                                                 double fpz, double fx, double fy, double fz,
+                                                 const RatesT<double>& r, long long (&h)[NPOP]) {
   typedef long long I;
   int emax = 0;
-  I g[NPOP];
-#pragma unroll
-  for (int q = 0; q < NPOP; ++q) g[q] = fx_from<kFxIn>(f[q], emax);
-  if (emax >= 1023 + kFxInMax || emax < 1023 + kFxMinExp) return false;
-  emax = 0;
   // forward transform, exact (collision.f90:101-118; grouping as collide_fast)
   const I a1 = g[1] + g[2], d1 = g[1] - g[2];
   const I a3 = g[3] + g[4], d3 = g[3] - g[4];
@@ -392,7 +391,6 @@ __host__ __device__ __forceinline__ bool collide_fx(double (&f)[NPOP], double fp
   if (out) return false;
 
   // inverse transform, exact (collision.f90:160-200)
-  I h[NPOP];
   h[0] = tl1 - 30 * M[1] + 12 * M[2];
   const I suma = tl1 - 11 * M[1] - 4 * M[2];
   const I sumb = tl1 + 8 * M[1] + M[2];
@@ -442,8 +440,53 @@ __host__ __device__ __forceinline__ bool collide_fx(double (&f)[NPOP], double fp
     h[16] = bm - Q;
     h[17] = bm + Q;
   }
+  return true;
+}
+
+__host__ __device__ __forceinline__ bool collide_fx(double (&f)[NPOP], double fpx, double fpy,
+                                                    double fpz, double fx, double fy, double fz,
+                                                    const RatesT<double>& r) {
+  int emax = 0;
+  long long g[NPOP], h[NPOP];
+#pragma unroll
+  for (int q = 0; q < NPOP; ++q) g[q] = fx_from<kFxIn>(f[q], emax);
+  if (emax >= 1023 + kFxInMax || emax < 1023 + kFxMinExp) return false;
+  if (!fx_core(g, fpx, fpy, fpz, fx, fy, fz, r, h)) return false;
 #pragma unroll
   for (int q = 0; q < NPOP; ++q) f[q] = fx_to<kFxOut>(h[q]);
+  return true;
+}
+
+// Populations stored as 64-bit fixed point at scale 2^-kFxIn (the FP64 plain
+// path between fused steps): |f| < 2^(63 - kFxIn) = 32 is representable, the
+// absolute resolution is 2^-58 = 3.5e-18 (FP64's own rounding of populations
+// of 0.01 to 0.1 is 1.7e-18 to 1.4e-17).
+__host__ __device__ __forceinline__ double pop_from_fixed(long long v) { return fx_to<kFxIn>(v); }
+// false when v is not finite or |v| >= 32
+__host__ __device__ __forceinline__ bool pop_to_fixed(double v, long long& out) {
+  int e = 0;
+  out = fx_from<kFxIn>(v, e);
+  return e < 1023 + (63 - kFxIn);
+}
+
+// collide_fx on populations already in the stored fixed point: no
+// conversions in or out (the outputs are rounded from 2^-kFxOut to 2^-kFxIn).
+// False, with g as it was, when an input is outside |f| < 2^kFxInMax or a
+// moment leaves its range.
+__host__ __device__ __forceinline__ bool collide_fx_fixed(long long (&g)[NPOP], double fpx,
+                                                          double fpy, double fpz, double fx,
+                                                          double fy, double fz,
+                                                          const RatesT<double>& r) {
+  constexpr unsigned long long lim = 1ULL << (kFxIn + kFxInMax);
+  unsigned long long out = 0;
+#pragma unroll
+  for (int q = 0; q < NPOP; ++q) out |= ((unsigned long long)g[q] + lim) & ~(2 * lim - 1);
+  if (out) return false;
+  long long h[NPOP];
+  if (!fx_core(g, fpx, fpy, fpz, fx, fy, fz, r, h)) return false;
+  constexpr int sh = kFxOut - kFxIn;
+#pragma unroll
+  for (int q = 0; q < NPOP; ++q) g[q] = (h[q] + (1LL << (sh - 1))) >> sh;
   return true;
 }
 

@@ -289,6 +289,82 @@ __global__ void __launch_bounds__(128, FX ? 4 : 1) k_fused(Geometry g, RatesT<T>
   }
 }
 
+// k_fused's FX path on populations stored in fixed point (collide_fx_fixed):
+// the FP64 plain path's kernel between fused steps.  Loads and stores are the
+// 64-bit integers themselves; a node collide_fx_fixed declines is converted
+// to FP64, collided by collide_fast and converted back (a value beyond the
+// fixed-point range, |f| >= 32 or not finite, raises LBM_ERR_NONFINITE).
+template <bool CHANNEL>
+__global__ void __launch_bounds__(128, 4) k_fused_fixed(Geometry g, RatesT<double> r,
+                                                         const long long* __restrict__ fin,
+                                                         long long* __restrict__ fout,
+                                                         const int32_t* __restrict__ isnodes,
+                                                         ForceView<double> fprev,
+                                                         ForceView<double> fnew, double* fcache,
+                                                         int fcache_mode, DevStatus* st) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y, z = blockIdx.z;
+  if (x >= g.nx) return;
+  const int nx = g.nx, nxy = g.nx * g.ny, N = (int)g.N;
+  const int n = x + nx * y + nxy * z;
+  long long f[NPOP];
+  double fp[3], fc[3];
+  if (fcache_mode == 2) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) fp[c] = fcache[(size_t)c * N + n];
+  }
+#pragma unroll
+  for (int q = 0; q < NPOP; ++q) f[q] = fin[(size_t)q * N + n];
+  const bool solid = is_solid(solid_mask(isnodes, g), g, z * g.ny + y, x);
+  if (fcache_mode != 0) {
+    body_force(fnew, g, x, y, z, fc[0], fc[1], fc[2]);
+    if (!solid && fcache_mode != 2) body_force(fprev, g, x, y, z, fp[0], fp[1], fp[2]);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) fcache[(size_t)c * N + n] = fc[c];
+  } else if (!solid) {
+    body_force2(fprev, fnew, x, z * g.ny + y, fp, fc);
+  }
+  if (!solid && !collide_fx_fixed(f, fp[0], fp[1], fp[2], fc[0], fc[1], fc[2], r)) {
+    double d[NPOP];
+#pragma unroll
+    for (int q = 0; q < NPOP; ++q) d[q] = pop_from_fixed(fin[(size_t)q * N + n]);
+    collide_fast(d, fp[0], fp[1], fp[2], fc[0], fc[1], fc[2], r);
+    bool ok = true;
+#pragma unroll
+    for (int q = 0; q < NPOP; ++q) ok &= pop_to_fixed(d[q], f[q]);
+    if (!ok) raise_error(st, LBM_ERR_NONFINITE, n);
+  }
+  const int oxp = (x == nx - 1) ? 1 - nx : 1, oxm = (x == 0) ? nx - 1 : -1;
+  const int oyp = (y == g.ny - 1) ? nx - nxy : nx, oym = (y == 0) ? nxy - nx : -nx;
+  const int ozp = (z == g.nz - 1) ? nxy - N : nxy, ozm = (z == 0) ? N - nxy : -nxy;
+#pragma unroll
+  for (int q = 0; q < NPOP; ++q) {
+    const int cx = cix(q), cy = ciy(q), cz = ciz(q);
+    if (CHANNEL && ((cx == -1 && x == 0) || (cx == 1 && x == nx - 1))) {
+      fout[(size_t)ipopp(q) * N + n] = f[q];
+      continue;
+    }
+    const int off = (cx > 0 ? oxp : (cx < 0 ? oxm : 0)) + (cy > 0 ? oyp : (cy < 0 ? oym : 0)) +
+                    (cz > 0 ? ozp : (cz < 0 ? ozm : 0));
+    fout[(size_t)q * N + (n + off)] = f[q];
+  }
+}
+
+// the stored populations between FP64 and fixed point, in place
+__global__ void k_pop_to_fixed(double* f, long long n, DevStatus* st) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    long long v;
+    if (!pop_to_fixed(f[i], v)) raise_error(st, LBM_ERR_NONFINITE, (int)(i % 2147483647));
+    reinterpret_cast<long long*>(f)[i] = v;
+  }
+}
+__global__ void k_pop_from_fixed(double* f, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    f[i] = pop_from_fixed(reinterpret_cast<const long long*>(f)[i]);
+}
+
 // streaming alone (per-subroutine entry), B/streaming.f90:2-171
 template <typename T, bool CHANNEL>
 __global__ void k_stream(Geometry g, const T* __restrict__ fin, T* __restrict__ fout) {
@@ -606,6 +682,33 @@ void launch_fused_step(const Geometry& g, const Rates& r, const T* fin, T* fout,
     { k_fused<T, true><<<row_grid(g, B), B, 0, s>>>(g, rt, fin, fout, isnodes, fprev, fnew, nullptr, 0); count_launch(); }
   else
     { k_fused<T, false><<<row_grid(g, B), B, 0, s>>>(g, rt, fin, fout, isnodes, fprev, fnew, nullptr, 0); count_launch(); }
+}
+
+void launch_fused_fixed(const Geometry& g, const Rates& r, const double* fin, double* fout,
+                        const int32_t* isnodes, const ForceView<double>& fprev,
+                        const ForceView<double>& fnew, double* fcache, int fcache_mode,
+                        DevStatus* st, cudaStream_t s) {
+  const int B = 128;
+  const RatesT<double> rt = rates_t<double>(r);
+  if (!fcache || fnew.mode != FM_TABLE) fcache_mode = 0;
+  const long long* gi = reinterpret_cast<const long long*>(fin);
+  long long* go = reinterpret_cast<long long*>(fout);
+  if (g.channel)
+    k_fused_fixed<true><<<row_grid(g, B), B, 0, s>>>(g, rt, gi, go, isnodes, fprev, fnew, fcache,
+                                                     fcache_mode, st);
+  else
+    k_fused_fixed<false><<<row_grid(g, B), B, 0, s>>>(g, rt, gi, go, isnodes, fprev, fnew, fcache,
+                                                      fcache_mode, st);
+  count_launch();
+}
+
+void launch_pop_format(double* f, long long n, bool to_fixed, DevStatus* st, cudaStream_t s) {
+  const int B = 256;
+  long long blocks = (n + B - 1) / B;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (to_fixed) k_pop_to_fixed<<<(unsigned)blocks, B, 0, s>>>(f, n, st);
+  else k_pop_from_fixed<<<(unsigned)blocks, B, 0, s>>>(f, n);
+  count_launch();
 }
 
 template <typename T>

@@ -88,6 +88,9 @@ struct Geometry {
   long long N;
   int channel;
   int sw;                   // 32-bit words per row of the solid mask
+  // FP64 populations stored as 64-bit fixed point (between fused steps of the
+  // FP64 plain path; pop_from_fixed / pop_to_fixed) rather than as doubles
+  int pop_fixed = 0;
 };
 
 // the solid mask that follows the N particle ids of a flag buffer
@@ -141,6 +144,15 @@ void launch_fused_step(const Geometry& g, const Rates& r, const T* fin, T* fout,
                        const int32_t* isnodes, const ForceView<T>& fprev,
                        const ForceView<T>& fnew, bool fx, T* fcache, int fcache_mode,
                        cudaStream_t s);
+// the FP64 fixed-point step on populations stored in fixed point (fin and
+// fout hold 64-bit integers at 2^-58; g.pop_fixed)
+void launch_fused_fixed(const Geometry& g, const Rates& r, const double* fin, double* fout,
+                        const int32_t* isnodes, const ForceView<double>& fprev,
+                        const ForceView<double>& fnew, double* fcache, int fcache_mode,
+                        DevStatus* st, cudaStream_t s);
+// n stored populations between FP64 and fixed point, in place; to fixed
+// point, a value beyond |f| < 32 or not finite raises LBM_ERR_NONFINITE
+void launch_pop_format(double* f, long long n, bool to_fixed, DevStatus* st, cudaStream_t s);
 // the same step with its rows staged through shared memory by bulk copies
 // (lbm_staged.cu); periodic boxes with nx a multiple of 4
 struct StagedPlan {
@@ -289,7 +301,8 @@ void launch_bounce_back(const Geometry& g, const ParticleView& pv, const T* f,
                         double* fHIp, double* torqp, cudaStream_t s);
 template <typename T>
 void launch_bounce_scatter(const Geometry& g, const ParticleView& pv, T* f,
-                           int pushed_layout, LinkSlab ls, cudaStream_t s);
+                           int pushed_layout, LinkSlab ls, cudaStream_t s,
+                           DevStatus* st = nullptr);
 template <typename T>
 void launch_slip(const Geometry& g, const ParticleView& pv, const T* ux, const T* uy, const T* uz,
                  const int32_t* isnodes, double r_in, double r_out, double* slip, cudaStream_t s);

@@ -18,6 +18,7 @@
 #include <cub/block/block_scan.cuh>
 
 #include "lbm_internal.cuh"
+#include "lbm_collide.cuh"  // the fixed-point population format
 
 namespace lbm {
 
@@ -617,6 +618,29 @@ __device__ __forceinline__ float recip_link(float x) { return __frcp_rn(x); }
 __device__ __forceinline__ double fma_r(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ float fma_r(float a, float b, float c) { return fmaf(a, b, c); }
 
+// a stored population: FP64 populations are 64-bit fixed point while
+// g.pop_fixed is set (between fused steps of the FP64 plain path)
+template <typename T>
+__device__ __forceinline__ T ld_pop(const Geometry& g, const T* f, long long idx) {
+  if constexpr (sizeof(T) == 8) {
+    if (g.pop_fixed) return pop_from_fixed(reinterpret_cast<const long long*>(f)[idx]);
+  }
+  return f[idx];
+}
+template <typename T>
+__device__ __forceinline__ void st_pop(const Geometry& g, T* f, long long idx, T v, DevStatus* st,
+                                       int where) {
+  if constexpr (sizeof(T) == 8) {
+    if (g.pop_fixed) {
+      long long w;
+      if (!pop_to_fixed(v, w)) raise_error(st, LBM_ERR_NONFINITE, where);
+      reinterpret_cast<long long*>(f)[idx] = w;
+      return;
+    }
+  }
+  f[idx] = v;
+}
+
 // post-collision population q at node (i, j, k) (0-based) in either layout.
 // pushed: the fused kernel has already moved it to its streaming target
 // (or bounced it back in place at a channel wall).
@@ -626,12 +650,12 @@ __device__ __forceinline__ T read_post(const Geometry& g, const T* f, int pushed
   // 32-bit element indices: 19 N < 2^31 (N < 2^26 is enforced)
   const int N = (int)g.N;
   const int n = i + g.nx * (j + g.ny * k);
-  if (!pushed) return f[q * N + n];
+  if (!pushed) return ld_pop(g, f, q * N + n);
   int it = i + cix(q);
-  if (g.channel && (it < 0 || it >= g.nx)) return f[ipopp(q) * N + n];
+  if (g.channel && (it < 0 || it >= g.nx)) return ld_pop(g, f, ipopp(q) * N + n);
   it = wrapi(it, g.nx);
   const int jt = wrapi(j + ciy(q), g.ny), kt = wrapi(k + ciz(q), g.nz);
-  return f[q * N + it + g.nx * (jt + g.ny * kt)];
+  return ld_pop(g, f, q * N + it + g.nx * (jt + g.ny * kt));
 }
 
 // threads per particle block of the bounce-back: FP64 links are FP64-pipe
@@ -865,7 +889,7 @@ __global__ void __launch_bounds__(bounce_threads<T>()) k_bounce(Geometry g, Part
 // already sits at its streaming target, the fluid node x itself.
 template <typename T>
 __device__ __forceinline__ void k_bounce_store_body(int bx, int gx, Geometry g, ParticleView pv, T* f, int pushed,
-                                                     LinkSlab ls) {
+                                                     LinkSlab ls, DevStatus* st = nullptr) {
   // particles bx, bx + gx, ...
   for (int p = bx; p < pv.npart; p += gx) {
   const int cnt = ls.count[p];
@@ -881,22 +905,22 @@ __device__ __forceinline__ void k_bounce_store_body(int bx, int gx, Geometry g, 
     if (pushed) {
       int it = i + cix(ipop);
       if (g.channel && (it < 0 || it >= g.nx)) continue;
-      f[ipp * g.N + node] = f9s[l];
+      st_pop(g, f, ipp * g.N + node, f9s[l], st, p);
     } else {
       const int k = r / g.ny, j = r - k * g.ny;
       int it = i + cix(ipop);
       if (g.channel && (it < 0 || it >= g.nx)) continue;
       it = wrapi(it, g.nx);
       int jt = wrapi(j + ciy(ipop), g.ny), kt = wrapi(k + ciz(ipop), g.nz);
-      f[ipp * g.N + (long long)it + (long long)g.nx * (jt + (long long)g.ny * kt)] = f9s[l];
+      st_pop(g, f, ipp * g.N + (long long)it + (long long)g.nx * (jt + (long long)g.ny * kt), f9s[l], st, p);
     }
   }
   }
 }
 template <typename T>
 __global__ void __launch_bounds__(PB) k_bounce_store(Geometry g, ParticleView pv, T* f, int pushed,
-                                                     LinkSlab ls) {
-  k_bounce_store_body<T>(blockIdx.x, gridDim.x, g, pv, f, pushed, ls);
+                                                     LinkSlab ls, DevStatus* st) {
+  k_bounce_store_body<T>(blockIdx.x, gridDim.x, g, pv, f, pushed, ls, st);
 }
 
 // beads_lubforce, one warp per particle.  Contributions to particle p are
@@ -1206,7 +1230,7 @@ __device__ __forceinline__ void k_fill_events_body(int bx, int gx, Geometry g, P
                                                      const double* __restrict__ omgpp,
                                                      const int32_t* __restrict__ isnodes,
                                                      const int32_t* __restrict__ isnodes0, T* f,
-                                                     FillList fl) {
+                                                     FillList fl, DevStatus* st) {
   using R = T;  // refill arithmetic in the population precision
   const int lane = threadIdx.x & 31;
   const int warp = (bx * blockDim.x + threadIdx.x) >> 5;
@@ -1280,7 +1304,7 @@ __device__ __forceinline__ void k_fill_events_body(int bx, int gx, Geometry g, P
         }
       }
       if (have) {
-        const R fq = lane < NPOP ? R(f[(size_t)q * g.N + m]) : R(0);
+        const R fq = lane < NPOP ? R(ld_pop(g, f, (long long)q * g.N + m)) : R(0);
         R rho9 = fq;
         R u9 = cix(q) == 0 ? R(0) : flip_if(cix(q) < 0, fq);
         R v9 = ciy(q) == 0 ? R(0) : flip_if(ciy(q) < 0, fq);
@@ -1305,7 +1329,7 @@ __device__ __forceinline__ void k_fill_events_body(int bx, int gx, Geometry g, P
         if (isnodes[m] < 0 && isnodes0[m] < 0) {
           cnt = 1;
 #pragma unroll
-          for (int ii = 0; ii < NPOP; ++ii) rs += R(f[(size_t)ii * g.N + m]);
+          for (int ii = 0; ii < NPOP; ++ii) rs += R(ld_pop(g, f, (long long)ii * g.N + m));
         }
       }
     }
@@ -1318,7 +1342,7 @@ __device__ __forceinline__ void k_fill_events_body(int bx, int gx, Geometry g, P
     const R u9 = wx + oy * dz - oz * dy;
     const R v9 = wy + oz * dx - ox * dz;
     const R w9 = wz + ox * dy - oy * dx;
-    if (lane < NPOP) f[(size_t)q * g.N + n] = T(fnew + feq_q<R>(q, u9, v9, w9, rho9));
+    if (lane < NPOP) st_pop(g, f, (long long)q * g.N + n, T(fnew + feq_q<R>(q, u9, v9, w9, rho9)), st, id);
   }
 }
 template <typename T>
@@ -1328,8 +1352,8 @@ __global__ void __launch_bounds__(128) k_fill_events(Geometry g, ParticleView pv
                                                      const double* __restrict__ omgpp,
                                                      const int32_t* __restrict__ isnodes,
                                                      const int32_t* __restrict__ isnodes0, T* f,
-                                                     FillList fl) {
-  k_fill_events_body<T>(blockIdx.x, gridDim.x, g, pv, pp, ypglbp, wpp, omgpp, isnodes, isnodes0, f, fl);
+                                                     FillList fl, DevStatus* st) {
+  k_fill_events_body<T>(blockIdx.x, gridDim.x, g, pv, pp, ypglbp, wpp, omgpp, isnodes, isnodes0, f, fl, st);
 }
 
 }  // namespace
@@ -1351,7 +1375,7 @@ void launch_bounce_back(const Geometry& g, const ParticleView& pv, const T* f, i
 
 template <typename T>
 void launch_bounce_scatter(const Geometry& g, const ParticleView& pv, T* f, int pushed,
-                           LinkSlab ls, cudaStream_t s) {
+                           LinkSlab ls, cudaStream_t s, DevStatus* st) {
   if (pv.npart <= 0) return;
   // four blocks per SM, looping over particles: the stores run beside the
   // particle kernels of the critical path and leave half of every SM's
@@ -1364,7 +1388,7 @@ void launch_bounce_scatter(const Geometry& g, const ParticleView& pv, T* f, int 
       sms = 1;
   }
   const int nblk = pv.npart < 4 * sms ? pv.npart : 4 * sms;
-  { k_bounce_store<T><<<nblk, PB, 0, s>>>(g, pv, f, pushed, ls); count_launch(); }
+  { k_bounce_store<T><<<nblk, PB, 0, s>>>(g, pv, f, pushed, ls, st); count_launch(); }
 }
 
 void launch_lubforce(const Geometry& g, int npart, const PartParams& pp, MoveState ms,
@@ -1420,7 +1444,7 @@ void launch_filling(const Geometry& g, const ParticleView& pv, const PartParams&
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
       sms = 1;
   }
-  { k_fill_events<T><<<8 * sms, 128, 0, s>>>(g, pv, pp, ypglbp, wpp, omgpp, isnodes, isnodes0, f, fl); count_launch(); }
+  { k_fill_events<T><<<8 * sms, 128, 0, s>>>(g, pv, pp, ypglbp, wpp, omgpp, isnodes, isnodes0, f, fl, st); count_launch(); }
 }
 
 // ---- many boxes per launch ------------------------------------------------
@@ -1485,7 +1509,7 @@ constexpr int kFillBlocks = 8;
 __global__ void __launch_bounds__(128) k_fill_events_multi(const BoxParticles* boxes) {
   BOX_OR_RETURN(B.pv.npart > 0 ? kFillBlocks : 0)
   k_fill_events_body<float>(blockIdx.x, nblk, B.g, B.pv, B.pp, B.ms.ypglbp, B.ms.wpp, B.ms.omgpp,
-                            B.flags_next, B.flags_cur, B.f, B.fl);
+                            B.flags_next, B.flags_cur, B.f, B.fl, B.st);
 }
 #undef BOX_OR_RETURN
 
@@ -1515,9 +1539,9 @@ template void launch_bounce_back<float>(const Geometry&, const ParticleView&, co
                                         const int32_t*, LinkSlab, double*, double*,
                                         cudaStream_t);
 template void launch_bounce_scatter<double>(const Geometry&, const ParticleView&, double*, int,
-                                            LinkSlab, cudaStream_t);
+                                            LinkSlab, cudaStream_t, DevStatus*);
 template void launch_bounce_scatter<float>(const Geometry&, const ParticleView&, float*, int,
-                                           LinkSlab, cudaStream_t);
+                                           LinkSlab, cudaStream_t, DevStatus*);
 template void launch_filling<double>(const Geometry&, const ParticleView&, const PartParams&,
                                      const double*, const double*, const double*,
                                      const int32_t*, const int32_t*, double*, FillList,
