@@ -94,6 +94,8 @@ struct lbm_ctx {
   void* ytw = nullptr;   // (cos, sin) of 2 pi ky y / ny, [5][ny], population precision
   double* ztw = nullptr;  // (cos, sin) of 2 pi kz z / nz, [5][nz]
   void* rowtab[3] = {nullptr, nullptr, nullptr};
+  long long* rowtab_i[3] = {nullptr, nullptr, nullptr};  // FP64: coefficients in fixed point
+  long long* xtw_i = nullptr;                            // FP64: twiddles in fixed point
   void* xtw = nullptr;
   ForceState latest{FM_NONE, 0}, fmacro{FM_NONE, 0};
   double var = 0, tf = 0, pi2 = 0;
@@ -189,6 +191,10 @@ ForceView<T> fview(lbm_ctx* c, const ForceState& s) {
   v.mode = s.mode;
   v.rowtab = s.mode == FM_TABLE ? static_cast<const T*>(c->rowtab[s.slot]) : nullptr;
   v.xtw = static_cast<const T*>(c->xtw);
+  if (!c->f32) {
+    v.rowtab_i = s.mode == FM_TABLE ? c->rowtab_i[s.slot] : nullptr;
+    v.xtw_i = c->xtw_i;
+  }
   v.cfx = T(0);
   v.cfy = T(c->cfg.force_y);
   v.cfz = T(0);
@@ -207,7 +213,9 @@ void pop_format(lbm_ctx* c, bool fixed) {
 // the fused steps that run on fixed-point populations: FP64, fixed-point
 // sums, the direct stream + collide kernel
 bool fixed_path(const lbm_ctx* c) {
-  return !c->f32 && c->sums == LBM_SUMS_FIXED && c->variant == LBM_VARIANT_DIRECT;
+  // (a constant body force must fit the fixed-point force range, |F| < 2^-7)
+  return !c->f32 && c->sums == LBM_SUMS_FIXED && c->variant == LBM_VARIANT_DIRECT &&
+         std::fabs(c->cfg.force_y) < 0.0078125;
 }
 template <typename T>
 T* fbuf(lbm_ctx* c, int i) {
@@ -356,7 +364,7 @@ void launch_forcing_into(lbm_ctx* c, int slot, cudaStream_t st) {
   else
     launch_forcing_tables<double>(c->g, c->d_forcing, static_cast<const double*>(c->ytw),
                                   c->ztw, static_cast<double*>(c->rowtab[slot]),
-                                  static_cast<double*>(c->ztab), st);
+                                  static_cast<double*>(c->ztab), st, c->rowtab_i[slot], c->status);
 }
 
 // FORCING: advance the stochastic state and tabulate the new field.  If the
@@ -503,10 +511,13 @@ void launch_stream_collide(lbm_ctx* c, const T* fin, T* fout, bool use_cache = f
       done = true;
     }
   }
-  if (!done)
+  if (!done) {
+    // the force cache holds fixed-point forces of the fixed-point kernel only
+    mode = 0;
     launch_fused_step<T>(c->g, c->r, fin, fout, c->flags[c->fcur], fview<T>(c, c->fmacro),
                          fview<T>(c, c->latest), fx, reinterpret_cast<T*>(c->fcache), mode,
                          c->stream);
+  }
   if (use_cache) {
     c->fcache_slot = mode ? c->latest.slot : -1;
     c->fcache_version = mode ? c->slot_version[c->latest.slot] : 0;
@@ -873,6 +884,7 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
   al((void**)&ctx->staging, std::min<long long>(19 * N, kStagingDoubles) * sizeof(double));
   al((void**)&ctx->partial, 6 * 1024 * sizeof(double));
   al(&ctx->xtw, 4 * g.nx * ctx->esz);
+  if (!ctx->f32) al((void**)&ctx->xtw_i, 4 * g.nx * sizeof(long long));
   if (!rc && cudaMallocHost((void**)&ctx->status_host, sizeof(DevStatus)) != cudaSuccess)
     rc = fail(ctx, LBM_ERR_NOMEM, "cudaMallocHost");
   if (!rc && cudaMallocHost((void**)&ctx->partial_host, 4 * 1024 * sizeof(double)) != cudaSuccess)
@@ -887,7 +899,11 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
     al(&ctx->ytw, 5LL * g.ny * 2 * sizeof(double));
     al((void**)&ctx->ztw, 5LL * g.nz * 2 * sizeof(double));
     for (int s = 0; s < 3; ++s) al(&ctx->rowtab[s], (long long)kRowCoef * g.ny * g.nz * ctx->esz);
-    if (!ctx->f32) al((void**)&ctx->fcache, 3 * (size_t)g.N * sizeof(double));
+    if (!ctx->f32) {
+      al((void**)&ctx->fcache, 3 * (size_t)g.N * sizeof(double));
+      for (int s = 0; s < 3; ++s)
+        al((void**)&ctx->rowtab_i[s], (long long)kRowCoef * g.ny * g.nz * sizeof(long long));
+    }
   }
   ctx->npmax = cfg->npart_max > 0 ? cfg->npart_max : 0;
   if (ctx->npmax > 0) {
@@ -943,6 +959,11 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
       cudaMemcpy(ctx->xtw, twf.data(), twf.size() * sizeof(float), cudaMemcpyHostToDevice);
     } else {
       cudaMemcpy(ctx->xtw, tw.data(), tw.size() * sizeof(double), cudaMemcpyHostToDevice);
+      // the same twiddles at 2^-kTwFix (|cos|, |sin| <= 1; exact for values
+      // of 2^-8 and more)
+      std::vector<long long> twi(tw.size());
+      for (size_t i = 0; i < tw.size(); ++i) twi[i] = std::llround(std::ldexp(tw[i], kTwFix));
+      cudaMemcpy(ctx->xtw_i, twi.data(), twi.size() * sizeof(long long), cudaMemcpyHostToDevice);
     }
   }
   if (cfg->forcing == LBM_FORCING_STOCHASTIC) {
@@ -1025,7 +1046,8 @@ int lbm_destroy(lbm_ctx* ctx) {
                   ctx->rowtab[2], ctx->pbuf, ctx->first_move, ctx->links.code,
                   ctx->links.alpha, ctx->links.f9, ctx->links.count, ctx->links.sweeps,
                   ctx->links.sweep_ok, ctx->fill.node,
-                  ctx->fill.part, ctx->fill.count, ctx->fcache};
+                  ctx->fill.part, ctx->fill.count, ctx->fcache, ctx->xtw_i,
+                  ctx->rowtab_i[0], ctx->rowtab_i[1], ctx->rowtab_i[2]};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);

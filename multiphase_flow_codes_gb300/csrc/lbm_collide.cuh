@@ -3,6 +3,7 @@
 // moment space, and the direct evaluation of the low-wavenumber body force.
 #pragma once
 #include <cmath>
+#include <type_traits>
 
 #include "lbm_internal.cuh"
 
@@ -309,9 +310,13 @@ __host__ __device__ __forceinline__ unsigned fx_out_of_range(long long x) {
 //
 // fx_core is the part between the conversions: g the populations at scale
 // 2^-kFxIn (|g| < 2^(kFxIn + kFxInMax)), h the post-collision populations at
-// 2^-kFxOut; false when a moment leaves its range.
-__host__ __device__ __forceinline__ bool fx_core(const long long (&g)[NPOP], double fpx, double fpy,
-                                                 double fpz, double fx, double fy, double fz,
+// 2^-kFxOut; false when a moment leaves its range.  The previous step's body
+// force fp (the velocity's F/2) is FP64, or (FP = long long) fixed point at
+// 2^-kFxF, added to the momentum sums exactly.
+constexpr int kFxF = 70;  // body forces in fixed point: |F| < 2^-7 at 2^-70
+template <typename FP>
+__host__ __device__ __forceinline__ bool fx_core(const long long (&g)[NPOP], FP fpx, FP fpy,
+                                                 FP fpz, double fx, double fy, double fz,
                                                  const RatesT<double>& r, long long (&h)[NPOP]) {
   typedef long long I;
   int emax = 0;
@@ -345,9 +350,19 @@ __host__ __device__ __forceinline__ bool fx_core(const long long (&g)[NPOP], dou
   const I ev8 = sum10 + sum11;
   const I ev9 = -2 * sum10 + sum11;
   // macrovar: u = sum c f + F_prev / 2
-  const double ux = fx_to<kFxIn>(d1 + sum3) + 0.5 * fpx;
-  const double uy = fx_to<kFxIn>(d3 + sum4) + 0.5 * fpy;
-  const double uz = fx_to<kFxIn>(d5 + sum5) + 0.5 * fpz;
+  double ux, uy, uz;
+  if constexpr (std::is_integral<FP>::value) {
+    // F/2 from 2^-kFxF to 2^-kFxIn, rounded
+    constexpr int sh = kFxF - kFxIn + 1;
+    auto half = [](long long v) { return (v + (1LL << (sh - 1))) >> sh; };
+    ux = fx_to<kFxIn>(d1 + sum3 + half(fpx));
+    uy = fx_to<kFxIn>(d3 + sum4 + half(fpy));
+    uz = fx_to<kFxIn>(d5 + sum5 + half(fpz));
+  } else {
+    ux = fx_to<kFxIn>(d1 + sum3) + 0.5 * fpx;
+    uy = fx_to<kFxIn>(d3 + sum4) + 0.5 * fpy;
+    uz = fx_to<kFxIn>(d5 + sum5) + 0.5 * fpz;
+  }
 
   // equilibrium and forcing moments, FP64 (collision.f90:66-81)
   const double uxs = ux * ux, uys = uy * uy, uzs = uz * uz;
@@ -451,7 +466,7 @@ __host__ __device__ __forceinline__ bool collide_fx(double (&f)[NPOP], double fp
 #pragma unroll
   for (int q = 0; q < NPOP; ++q) g[q] = fx_from<kFxIn>(f[q], emax);
   if (emax >= 1023 + kFxInMax || emax < 1023 + kFxMinExp) return false;
-  if (!fx_core(g, fpx, fpy, fpz, fx, fy, fz, r, h)) return false;
+  if (!fx_core<double>(g, fpx, fpy, fpz, fx, fy, fz, r, h)) return false;
 #pragma unroll
   for (int q = 0; q < NPOP; ++q) f[q] = fx_to<kFxOut>(h[q]);
   return true;
@@ -473,9 +488,9 @@ __host__ __device__ __forceinline__ bool pop_to_fixed(double v, long long& out) 
 // conversions in or out (the outputs are rounded from 2^-kFxOut to 2^-kFxIn).
 // False, with g as it was, when an input is outside |f| < 2^kFxInMax or a
 // moment leaves its range.
-__host__ __device__ __forceinline__ bool collide_fx_fixed(long long (&g)[NPOP], double fpx,
-                                                          double fpy, double fpz, double fx,
-                                                          double fy, double fz,
+template <typename FP>
+__host__ __device__ __forceinline__ bool collide_fx_fixed(long long (&g)[NPOP], FP fpx, FP fpy,
+                                                          FP fpz, double fx, double fy, double fz,
                                                           const RatesT<double>& r) {
   constexpr unsigned long long lim = 1ULL << (kFxIn + kFxInMax);
   unsigned long long out = 0;
@@ -483,7 +498,7 @@ __host__ __device__ __forceinline__ bool collide_fx_fixed(long long (&g)[NPOP], 
   for (int q = 0; q < NPOP; ++q) out |= ((unsigned long long)g[q] + lim) & ~(2 * lim - 1);
   if (out) return false;
   long long h[NPOP];
-  if (!fx_core(g, fpx, fpy, fpz, fx, fy, fz, r, h)) return false;
+  if (!fx_core<FP>(g, fpx, fpy, fpz, fx, fy, fz, r, h)) return false;
   constexpr int sh = kFxOut - kFxIn;
 #pragma unroll
   for (int q = 0; q < NPOP; ++q) g[q] = (h[q] + (1LL << (sh - 1))) >> sh;

@@ -289,26 +289,58 @@ __global__ void __launch_bounds__(128, FX ? 4 : 1) k_fused(Geometry g, RatesT<T>
   }
 }
 
+// The body force of a view as fixed point at 2^-kFxF.  Table mode: the row's
+// x series with exact 128-bit products of the fixed-point coefficients
+// (2^-kFxF, |k| < 2^-7) and twiddles (2^-kTwFix), rounded once; on this GPU
+// the integer products run on otherwise idle pipes while FP64 issues at a
+// few lanes per clock.
+__device__ __forceinline__ void body_force_fx(const ForceView<double>& fv, const Geometry& g, int x,
+                                              int y, int z, long long (&o)[3]) {
+  if (fv.mode != FM_TABLE) {
+    int e = 0;
+    const bool cst = fv.mode == FM_CONST;
+    o[0] = cst ? fx_from<kFxF>(fv.cfx, e) : 0;
+    o[1] = cst ? fx_from<kFxF>(fv.cfy, e) : 0;
+    o[2] = cst ? fx_from<kFxF>(fv.cfz, e) : 0;
+    return;
+  }
+  const long long* t = fv.xtw_i + 4 * x;
+  const long long c1 = t[0], s1 = t[1], c2 = t[2], s2 = t[3];
+  const long long* k = fv.rowtab_i + ((long long)z * g.ny + y) * kRowCoef;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    // |products| < 2^124, the sum of five < 2^127
+    const __int128 a = (__int128)k[5 * c] * ((__int128)1 << kTwFix) + (__int128)k[5 * c + 1] * c1 +
+                       (__int128)k[5 * c + 2] * s1 + (__int128)k[5 * c + 3] * c2 +
+                       (__int128)k[5 * c + 4] * s2;
+    o[c] = (long long)((a + ((__int128)1 << (kTwFix - 1))) >> kTwFix);
+  }
+}
+
 // k_fused's FX path on populations stored in fixed point (collide_fx_fixed):
 // the FP64 plain path's kernel between fused steps.  Loads and stores are the
 // 64-bit integers themselves; a node collide_fx_fixed declines is converted
 // to FP64, collided by collide_fast and converted back (a value beyond the
 // fixed-point range, |f| >= 32 or not finite, raises LBM_ERR_NONFINITE).
+// The body forces are fixed point too (body_force_fx): the previous step's
+// enters the velocity as an exact integer add; the force cache (fcache_mode
+// as in k_fused) holds them as 64-bit integers at 2^-kFxF.
 template <bool CHANNEL>
 __global__ void __launch_bounds__(128, 4) k_fused_fixed(Geometry g, RatesT<double> r,
                                                          const long long* __restrict__ fin,
                                                          long long* __restrict__ fout,
                                                          const int32_t* __restrict__ isnodes,
                                                          ForceView<double> fprev,
-                                                         ForceView<double> fnew, double* fcache,
-                                                         int fcache_mode, DevStatus* st) {
+                                                         ForceView<double> fnew,
+                                                         long long* fcache, int fcache_mode,
+                                                         DevStatus* st) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y, z = blockIdx.z;
   if (x >= g.nx) return;
   const int nx = g.nx, nxy = g.nx * g.ny, N = (int)g.N;
   const int n = x + nx * y + nxy * z;
   long long f[NPOP];
-  double fp[3], fc[3];
+  long long fp[3], fc[3];
   if (fcache_mode == 2) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) fp[c] = fcache[(size_t)c * N + n];
@@ -317,22 +349,26 @@ __global__ void __launch_bounds__(128, 4) k_fused_fixed(Geometry g, RatesT<doubl
   for (int q = 0; q < NPOP; ++q) f[q] = fin[(size_t)q * N + n];
   const bool solid = is_solid(solid_mask(isnodes, g), g, z * g.ny + y, x);
   if (fcache_mode != 0) {
-    body_force(fnew, g, x, y, z, fc[0], fc[1], fc[2]);
-    if (!solid && fcache_mode != 2) body_force(fprev, g, x, y, z, fp[0], fp[1], fp[2]);
+    body_force_fx(fnew, g, x, y, z, fc);
+    if (!solid && fcache_mode != 2) body_force_fx(fprev, g, x, y, z, fp);
 #pragma unroll
     for (int c = 0; c < 3; ++c) fcache[(size_t)c * N + n] = fc[c];
   } else if (!solid) {
-    body_force2(fprev, fnew, x, z * g.ny + y, fp, fc);
+    body_force_fx(fprev, g, x, y, z, fp);
+    body_force_fx(fnew, g, x, y, z, fc);
   }
-  if (!solid && !collide_fx_fixed(f, fp[0], fp[1], fp[2], fc[0], fc[1], fc[2], r)) {
-    double d[NPOP];
+  if (!solid) {
+    const double fx = fx_to<kFxF>(fc[0]), fy = fx_to<kFxF>(fc[1]), fz = fx_to<kFxF>(fc[2]);
+    if (!collide_fx_fixed<long long>(f, fp[0], fp[1], fp[2], fx, fy, fz, r)) {
+      double d[NPOP];
 #pragma unroll
-    for (int q = 0; q < NPOP; ++q) d[q] = pop_from_fixed(fin[(size_t)q * N + n]);
-    collide_fast(d, fp[0], fp[1], fp[2], fc[0], fc[1], fc[2], r);
-    bool ok = true;
+      for (int q = 0; q < NPOP; ++q) d[q] = pop_from_fixed(fin[(size_t)q * N + n]);
+      collide_fast(d, fx_to<kFxF>(fp[0]), fx_to<kFxF>(fp[1]), fx_to<kFxF>(fp[2]), fx, fy, fz, r);
+      bool ok = true;
 #pragma unroll
-    for (int q = 0; q < NPOP; ++q) ok &= pop_to_fixed(d[q], f[q]);
-    if (!ok) raise_error(st, LBM_ERR_NONFINITE, n);
+      for (int q = 0; q < NPOP; ++q) ok &= pop_to_fixed(d[q], f[q]);
+      if (!ok) raise_error(st, LBM_ERR_NONFINITE, n);
+    }
   }
   const int oxp = (x == nx - 1) ? 1 - nx : 1, oxm = (x == 0) ? nx - 1 : -1;
   const int oyp = (y == g.ny - 1) ? nx - nxy : nx, oym = (y == 0) ? nxy - nx : -nx;
@@ -619,7 +655,8 @@ __global__ void k_force_ztab(Geometry g, const ForcingDev* st, const double* __r
 // real inverse transform enter twice (kx and -kx), hence the factor 2.
 template <typename T>
 __device__ __forceinline__ void k_force_rowtab_body(int bx, int gx, Geometry g, const T* __restrict__ ztab,
-                               const T* __restrict__ ytw, T* __restrict__ rowtab) {
+                               const T* __restrict__ ytw, T* __restrict__ rowtab,
+                               long long* rowtab_i = nullptr, DevStatus* status = nullptr) {
   long long t = bx * (long long)blockDim.x + threadIdx.x;  // over (c,kx,z,y)
   long long total = 9LL * g.nz * g.ny;
   if (t >= total) return;
@@ -637,19 +674,36 @@ __device__ __forceinline__ void k_force_rowtab_body(int bx, int gx, Geometry g, 
     si += ar * sn + aim * cs;
   }
   const int c = ckx / 3, kx = ckx % 3;
-  T* k = rowtab + ((long long)z * g.ny + y) * kRowCoef + 5 * c;
+  const long long row = ((long long)z * g.ny + y) * kRowCoef;
+  T* k = rowtab + row + 5 * c;
+  T v0, v1 = T(0);
+  int j0;
   if (kx == 0) {
-    k[0] = sr;
-    if (c == 0) rowtab[((long long)z * g.ny + y) * kRowCoef + 15] = T(0);
+    k[0] = v0 = sr;
+    j0 = 0;
+    if (c == 0) rowtab[row + 15] = T(0);
   } else {
-    k[2 * kx - 1] = T(2.0) * sr;
-    k[2 * kx] = T(-2.0) * si;
+    k[2 * kx - 1] = v0 = T(2.0) * sr;
+    k[2 * kx] = v1 = T(-2.0) * si;
+    j0 = 2 * kx - 1;
+  }
+  if constexpr (sizeof(T) == 8) {
+    if (rowtab_i) {
+      // fixed point at 2^-kFxF: exact for |k| >= 2^-(kFxF - 52), range |k| < 2^-7
+      long long* ki = rowtab_i + row + 5 * c;
+      int e = 0;
+      ki[j0] = fx_from<kFxF>(double(v0), e);
+      if (kx != 0) ki[j0 + 1] = fx_from<kFxF>(double(v1), e);
+      if (kx == 0 && c == 0) rowtab_i[row + 15] = 0;
+      if (e >= 1023 + (63 - kFxF)) raise_error(status, LBM_ERR_STATE, (int)(t % 2147483647));
+    }
   }
 }
 template <typename T>
 __global__ void k_force_rowtab(Geometry g, const T* __restrict__ ztab,
-                               const T* __restrict__ ytw, T* __restrict__ rowtab) {
-  k_force_rowtab_body<T>(blockIdx.x, gridDim.x, g, ztab, ytw, rowtab);
+                               const T* __restrict__ ytw, T* __restrict__ rowtab,
+                               long long* rowtab_i, DevStatus* status) {
+  k_force_rowtab_body<T>(blockIdx.x, gridDim.x, g, ztab, ytw, rowtab, rowtab_i, status);
 }
 
 inline dim3 row_grid(const Geometry& g, int bx) { return dim3((g.nx + bx - 1) / bx, g.ny, g.nz); }
@@ -693,11 +747,12 @@ void launch_fused_fixed(const Geometry& g, const Rates& r, const double* fin, do
   if (!fcache || fnew.mode != FM_TABLE) fcache_mode = 0;
   const long long* gi = reinterpret_cast<const long long*>(fin);
   long long* go = reinterpret_cast<long long*>(fout);
+  long long* fci = reinterpret_cast<long long*>(fcache);
   if (g.channel)
-    k_fused_fixed<true><<<row_grid(g, B), B, 0, s>>>(g, rt, gi, go, isnodes, fprev, fnew, fcache,
+    k_fused_fixed<true><<<row_grid(g, B), B, 0, s>>>(g, rt, gi, go, isnodes, fprev, fnew, fci,
                                                      fcache_mode, st);
   else
-    k_fused_fixed<false><<<row_grid(g, B), B, 0, s>>>(g, rt, gi, go, isnodes, fprev, fnew, fcache,
+    k_fused_fixed<false><<<row_grid(g, B), B, 0, s>>>(g, rt, gi, go, isnodes, fprev, fnew, fci,
                                                       fcache_mode, st);
   count_launch();
 }
@@ -809,11 +864,12 @@ void launch_forcing_multi(const BoxForcing* boxes, int nb, int max_nz, long long
 
 template <typename T>
 void launch_forcing_tables(const Geometry& g, const ForcingDev* st, const T* ytw,
-                           const double* ztw, T* rowtab, T* ztab, cudaStream_t s) {
+                           const double* ztw, T* rowtab, T* ztab, cudaStream_t s,
+                           long long* rowtab_i, DevStatus* status) {
   int nz_t = 45 * g.nz;
   { k_force_ztab<T><<<blocks_for(nz_t, 128), 128, 0, s>>>(g, st, ztw, ztab); count_launch(); }
   long long nr = 9LL * g.nz * g.ny;
-  { k_force_rowtab<T><<<blocks_for(nr, 256), 256, 0, s>>>(g, ztab, ytw, rowtab); count_launch(); }
+  { k_force_rowtab<T><<<blocks_for(nr, 256), 256, 0, s>>>(g, ztab, ytw, rowtab, rowtab_i, status); count_launch(); }
 }
 
 #define LBM_INSTANTIATE(T)                                                                   \
@@ -843,7 +899,8 @@ void launch_forcing_tables(const Geometry& g, const ForcingDev* st, const T* ytw
   template void launch_mass_momentum<T>(const Geometry&, const T*, double*, int,            \
                                         cudaStream_t);                                      \
   template void launch_forcing_tables<T>(const Geometry&, const ForcingDev*, const T*, \
-                                         const double*, T*, T*, cudaStream_t);
+                                         const double*, T*, T*, cudaStream_t, long long*, \
+                                         DevStatus*);
 
 LBM_INSTANTIATE(double)
 LBM_INSTANTIATE(float)

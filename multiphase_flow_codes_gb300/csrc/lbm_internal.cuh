@@ -80,6 +80,11 @@ struct ForceView {
   const T* rowtab;          // [z*ny + y][kRowCoef] x-series coefficients, see below
   const T* xtw;             // per x: cos1, sin1, cos2, sin2
   T cfx, cfy, cfz;          // constant force (FM_CONST)
+  // FP64 tables only: rowtab's coefficients as 64-bit fixed point at 2^-70
+  // (|k| < 2^-7) and the twiddles at 2^-61, for the exact integer evaluation
+  // of the series in the fixed-point fluid kernel
+  const long long* rowtab_i = nullptr;
+  const long long* xtw_i = nullptr;
 };
 
 struct Geometry {
@@ -153,6 +158,8 @@ void launch_fused_fixed(const Geometry& g, const Rates& r, const double* fin, do
 // n stored populations between FP64 and fixed point, in place; to fixed
 // point, a value beyond |f| < 32 or not finite raises LBM_ERR_NONFINITE
 void launch_pop_format(double* f, long long n, bool to_fixed, DevStatus* st, cudaStream_t s);
+// twiddles at 2^-61 and the fixed-point row coefficients' range check
+constexpr int kTwFix = 61;
 // the same step with its rows staged through shared memory by bulk copies
 // (lbm_staged.cu); periodic boxes with nx a multiple of 4
 struct StagedPlan {
@@ -245,8 +252,12 @@ template <typename T>
 // ytw[jy][y], ztw[kz][z]: (cos, sin) of 2 pi k n / N for the five low
 // wavenumbers of each axis, tabulated once per box (ytw in the populations'
 // precision, ztw in FP64); ztab: the (kx, z) partial sums, T
+// rowtab_i (FP64 only, may be null): the coefficients again as fixed point
+// (ForceView::rowtab_i); a coefficient beyond its range raises LBM_ERR_STATE
+// in status
 void launch_forcing_tables(const Geometry& g, const ForcingDev* st, const T* ytw,
-                           const double* ztw, T* rowtab, T* ztab, cudaStream_t s);
+                           const double* ztw, T* rowtab, T* ztab, cudaStream_t s,
+                           long long* rowtab_i = nullptr, DevStatus* status = nullptr);
 
 // statistics (lbm_stats.cu): spectrum, dissipation and derivative moments
 // of statistc; per-particle slip velocity
