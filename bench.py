@@ -194,13 +194,16 @@ def run_device(wl, u, y, steps, warmup, device, want_f=False, variant=None, sums
     return ms, launches, phases, f, parts, variant
 
 
-def kernel_name(variant):
+def kernel_name(variant, fixed=False):
     v, st, groups, per_sm = variant
     if v == 3:
         return (f"k_fused_staged_x2 (stream + MRT collide + forcing, FP32 pairs on f32x2; "
                 f"{st} stages, {groups} consumer groups, {per_sm} CTAs/SM)")
     if v == 2:
         return f"k_fused_staged (stream + MRT collide + forcing; {st} stages, {per_sm} CTAs/SM)"
+    if fixed:
+        return ("k_fused_fixed (stream + MRT collide + forcing; direct, populations and forces in "
+                "64-bit fixed point)")
     return "k_fused (stream + MRT collide + forcing; direct)"
 
 
@@ -395,7 +398,7 @@ def main():
         traffic = figs[key]["dram_bytes_per_node"] * N
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
-            "kernel": kernel_name(variant),
+            "kernel": kernel_name(variant, dtype == "f64" and args.sums == "fixed"),
             "alg_bytes_per_launch": alg_bytes, "peak_source": peak_src}
     fp64 = {}
     if dtype == "f64" and key in figs and figs[key].get("fp64_flop_per_node") and sc_n:
