@@ -128,6 +128,7 @@ struct DevStatus {
 };
 
 __device__ inline void raise_error(DevStatus* st, int code, int where) {
+  if (!st) return;
   if (atomicCAS(&st->code, 0, code) == 0) st->where = where;
 }
 
