@@ -644,9 +644,13 @@ uint64_t footprint(const lbm_config& c, int64_t* cap_out) {
   if (c.forcing == LBM_FORCING_STOCHASTIC) {
     b += 3ull * kRowCoef * c.ny * c.nz * es + 45ull * c.nz * 2 * 8;  // row tables, z table
     b += 10ull * (c.ny + c.nz) * 8 + 2 * sizeof(ForcingDev) + 32 * 8;
-    if (c.precision != LBM_PREC_F32) b += 3 * N * 8;  // per-node force cache
+    if (c.precision != LBM_PREC_F32) {
+      b += 3 * N * 8;                              // per-node force cache
+      b += 3ull * kRowCoef * c.ny * c.nz * 8;      // row tables in fixed point
+    }
   }
   b += 4ull * c.nx * es;
+  if (c.precision != LBM_PREC_F32) b += 4ull * c.nx * 8;  // twiddles in fixed point
   uint64_t stage = std::min<uint64_t>(19 * N, kStagingDoubles) * 8;
   b += stage;
   return b;
