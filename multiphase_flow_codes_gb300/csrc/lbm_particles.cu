@@ -1140,26 +1140,48 @@ __device__ __forceinline__ void k_fill_detect_body(int bx, int gx, Geometry g, P
             bz0 = (int)floor(cz0 - 0.5) - r;
   const int w = 2 * r + 2;
   const int wx = min(w, g.nx), wy = min(w, g.ny), wz = min(w, g.nz);
-  const int total = wx * wy * wz;
-  for (int t = threadIdx.x; t < total; t += PB) {
-    int ox = t % wx, rr = t / wx;
-    int oy = rr % wy, oz = rr / wy;
-    int i = bx0 + ox, j = by0 + oy, k = bz0 + oz;
+  // One thread per row of the box: the nodes solid last step and fluid now
+  // are the set bits of (old mask & ~new mask), so a row costs one or two
+  // 32-bit words of each mask; only those nodes' ids are read.
+  const uint32_t* m0 = solid_mask(isnodes0, g);
+  const uint32_t* m1 = solid_mask(isnodes, g);
+  for (int rr = threadIdx.x; rr < wy * wz; rr += PB) {
+    const int oy = rr % wy, oz = rr / wy;
+    const int j = ((by0 + oy) % g.ny + g.ny) % g.ny, k = ((bz0 + oz) % g.nz + g.nz) % g.nz;
+    const size_t rowbase = ((size_t)k * g.ny + j) * g.sw;
+    // the box's x range as up to two segments [a, b) of [0, nx)
+    int sa[2], sb[2], ns = 0;
     if (channel) {
-      if (i < 0 || i >= g.nx) continue;
+      const int a = max(bx0, 0), b = min(bx0 + wx, g.nx);
+      if (a < b) { sa[0] = a; sb[0] = b; ns = 1; }
+    } else if (wx == g.nx) {
+      sa[0] = 0; sb[0] = g.nx; ns = 1;
     } else {
-      i = ((i % g.nx) + g.nx) % g.nx;
+      const int a = ((bx0 % g.nx) + g.nx) % g.nx;
+      if (a + wx <= g.nx) { sa[0] = a; sb[0] = a + wx; ns = 1; }
+      else { sa[0] = a; sb[0] = g.nx; sa[1] = 0; sb[1] = a + wx - g.nx; ns = 2; }
     }
-    j = ((j % g.ny) + g.ny) % g.ny;
-    k = ((k % g.nz) + g.nz) % g.nz;
-    const int n = i + g.nx * (j + g.ny * k);
-    if (isnodes0[n] != id || isnodes[n] >= 0) continue;
-    const int e = atomicAdd(fl.count, 1);
-    if (e < fl.cap) {
-      fl.node[e] = n;
-      fl.part[e] = id;
-    } else {
-      raise_error(st, LBM_ERR_CAPACITY, id);
+    for (int sgm = 0; sgm < ns; ++sgm) {
+      const int a = sa[sgm], b = sb[sgm];
+      for (int wi = a >> 5; wi <= (b - 1) >> 5; ++wi) {
+        uint32_t bits = m0[rowbase + wi] & ~m1[rowbase + wi];
+        const int lo = max(a - 32 * wi, 0), hi = min(b - 32 * wi, 32);
+        const uint32_t keep = (hi >= 32 ? 0xffffffffu : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
+        bits &= keep;
+        while (bits) {
+          const int i = 32 * wi + __ffs(bits) - 1;
+          bits &= bits - 1;
+          const int n = i + g.nx * (j + g.ny * k);
+          if (isnodes0[n] != id) continue;
+          const int e = atomicAdd(fl.count, 1);
+          if (e < fl.cap) {
+            fl.node[e] = n;
+            fl.part[e] = id;
+          } else {
+            raise_error(st, LBM_ERR_CAPACITY, id);
+          }
+        }
+      }
     }
   }
 }
