@@ -464,8 +464,10 @@ void particle_phase(lbm_ctx* c, T* f_plain) {
   }
   prof_begin(c);
   if (!pre) launch_lubforce(c->g, c->npart, c->pp, mstate(c), c->stream);
+  const ParticleView pv = pview(c);
   const bool ovl_aux = launch_move_redistribute(c->g, c->npart, c->pp, mstate(c), c->status,
-                                                c->stream, c->aux, c->ev_aux_fork, c->ev_aux_join);
+                                                c->stream, c->aux, c->ev_aux_fork, c->ev_aux_join,
+                                                &pv, &c->links);
   prof_end(c, LBM_PHASE_PARTICLES);
   int nf = 1 - c->fcur;
   prof_begin(c);
@@ -474,7 +476,7 @@ void particle_phase(lbm_ctx* c, T* f_plain) {
     cudaStreamWaitEvent(c->stream, c->ev_store, 0);
     c->store_pending = false;
   }
-  launch_links(c->g, pview(c), c->flags[nf], c->links, c->status, c->f32, c->stream);
+  launch_links(c->g, pview(c), c->flags[nf], c->links, c->status, c->f32, c->stream, true);
   prof_end(c, LBM_PHASE_LINKS);
   prof_begin(c);
   launch_filling<T>(c->g, pview(c), c->pp, c->ypglbp, c->wpp, c->omgpp, c->flags[nf],

@@ -306,7 +306,8 @@ struct LinkSlab {
 constexpr int kSweepBytes = 7 * 96;
 // alpha_fp32: link fractions in single precision (the FP32 population path)
 void launch_links(const Geometry& g, const ParticleView& pv, int32_t* isnodes,
-                  LinkSlab ls, DevStatus* st, int alpha_fp32, cudaStream_t s);
+                  LinkSlab ls, DevStatus* st, int alpha_fp32, cudaStream_t s,
+                  bool sweeps_done = false);
 template <typename T>
 void launch_bounce_back(const Geometry& g, const ParticleView& pv, const T* f,
                         int pushed_layout, const int32_t* isnodes, LinkSlab ls,
@@ -340,9 +341,12 @@ void launch_redistribute(const Geometry& g, int npart, const PartParams& pp, Mov
 // first move).  The check only reports; with an aux stream it runs there,
 // forked after the move by `fork` and recorded into `join`, beside the link
 // kernels that follow on s (returns true: the caller joins `join`).
+// With pv and ls, the same launch also runs beads_links' nearest-image
+// sweeps of every moved particle (launch_links then skips them).
 bool launch_move_redistribute(const Geometry& g, int npart, const PartParams& pp, MoveState ms,
                               DevStatus* st, cudaStream_t s, cudaStream_t aux = nullptr,
-                              cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr);
+                              cudaEvent_t fork = nullptr, cudaEvent_t join = nullptr,
+                              const ParticleView* pv = nullptr, LinkSlab* ls = nullptr);
 // refill events of one step: node index and particle id per event
 struct FillList {
   int32_t* node;

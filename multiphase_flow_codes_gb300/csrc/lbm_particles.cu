@@ -1013,8 +1013,7 @@ __global__ void k_lubforce(Geometry g, int npart, PartParams pp, MoveState ms) {
 
 // beads_move, B/partlib.f90:2305-2370, one thread per particle.  Also saves
 // the pre-move centre (ypglbp, used by beads_filling).
-__device__ __forceinline__ void k_move_body(int bx, int gx, int npart, PartParams pp, MoveState ms) {
-  int p = bx * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void move_particle(int p, int npart, PartParams pp, MoveState ms) {
   if (p >= npart) return;
   const bool first = *ms.first_move != 0;
   const double dt = 1.0;
@@ -1056,6 +1055,9 @@ __device__ __forceinline__ void k_move_body(int bx, int gx, int npart, PartParam
     ms.torqpp[3 * p + c] = ms.torqp[3 * p + c];
   }
 }
+__device__ __forceinline__ void k_move_body(int bx, int gx, int npart, PartParams pp, MoveState ms) {
+  move_particle(bx * blockDim.x + threadIdx.x, npart, pp, ms);
+}
 __global__ void k_move(int npart, PartParams pp, MoveState ms) {
   k_move_body(blockIdx.x, gridDim.x, npart, pp, ms);
 }
@@ -1063,8 +1065,7 @@ __global__ void k_move(int npart, PartParams pp, MoveState ms) {
 __global__ void k_clear_first(int* first_move) { *first_move = 0; }
 
 // beads_redistribute's periodic wrap, B/partlib.f90:2600-2613
-__device__ __forceinline__ void k_wrap_body(int bx, int gx, Geometry g, int npart, MoveState ms) {
-  int p = bx * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void wrap_particle(int p, Geometry g, int npart, MoveState ms) {
   if (p >= npart) return;
   double* y = ms.ypglb + 3 * p;
   double xc = y[0], yc = y[1], zc = y[2];
@@ -1077,11 +1078,30 @@ __device__ __forceinline__ void k_wrap_body(int bx, int gx, Geometry g, int npar
   if (zc >= (double)g.nz) y[2] = y[2] - (double)g.nz;
   if (zc < 0.0) y[2] = y[2] + (double)g.nz;
 }
+__device__ __forceinline__ void k_wrap_body(int bx, int gx, Geometry g, int npart, MoveState ms) {
+  wrap_particle(bx * blockDim.x + threadIdx.x, g, npart, ms);
+}
 __global__ void k_wrap(Geometry g, int npart, MoveState ms) {
   k_wrap_body(blockIdx.x, gridDim.x, g, npart, ms);
 }
+// beads_move, the wrap and the nearest-image sweeps of beads_links for 32
+// particles per block of 96 threads: thread t < 32 moves and wraps particle
+// 32 bx + t, then thread t sweeps axis t % 3 of particle 32 bx + t / 3 (the
+// fused time step; the sweeps need only their own particle's new centre)
+constexpr int kMoveSweepThreads = 96;
+__global__ void __launch_bounds__(kMoveSweepThreads) k_move_wrap_sweeps(Geometry g, int npart, PartParams pp,
+                                                                     MoveState ms, ParticleView pv,
+                                                                     LinkSlab ls) {
+  if (threadIdx.x < 32) {
+    const int p = blockIdx.x * 32 + threadIdx.x;
+    move_particle(p, npart, pp, ms);
+    wrap_particle(p, g, npart, ms);
+  }
+  __syncthreads();
+  k_link_sweeps_body(blockIdx.x, gridDim.x, g, pv, ls);
+}
 // beads_move followed by beads_redistribute's wrap, each particle's thread
-// wrapping the centre it has just moved (the fused time step)
+// wrapping the centre it has just moved
 __global__ void k_move_wrap(Geometry g, int npart, PartParams pp, MoveState ms) {
   k_move_body(blockIdx.x, gridDim.x, npart, pp, ms);
   k_wrap_body(blockIdx.x, gridDim.x, g, npart, ms);
@@ -1381,9 +1401,10 @@ __global__ void __launch_bounds__(128) k_fill_events(Geometry g, ParticleView pv
 }  // namespace
 
 void launch_links(const Geometry& g, const ParticleView& pv, int32_t* isnodes, LinkSlab ls,
-                  DevStatus* st, int alpha_fp32, cudaStream_t s) {
+                  DevStatus* st, int alpha_fp32, cudaStream_t s, bool sweeps_done) {
   if (pv.npart <= 0) return;
-  { k_link_sweeps<<<(3 * pv.npart + kSmallBlock - 1) / kSmallBlock, kSmallBlock, 0, s>>>(g, pv, ls); count_launch(); }
+  if (!sweeps_done)
+    { k_link_sweeps<<<(3 * pv.npart + kSmallBlock - 1) / kSmallBlock, kSmallBlock, 0, s>>>(g, pv, ls); count_launch(); }
   { k_links<<<pv.npart, PB, 0, s>>>(g, pv, isnodes, ls, st, alpha_fp32); count_launch(); }
 }
 
@@ -1435,9 +1456,12 @@ void launch_redistribute(const Geometry& g, int npart, const PartParams& pp, Mov
 
 bool launch_move_redistribute(const Geometry& g, int npart, const PartParams& pp, MoveState ms,
                               DevStatus* st, cudaStream_t s, cudaStream_t aux, cudaEvent_t fork,
-                              cudaEvent_t join) {
+                              cudaEvent_t join, const ParticleView* pv, LinkSlab* ls) {
   if (npart <= 0) return false;
-  { k_move_wrap<<<(npart + kSmallBlock - 1) / kSmallBlock, kSmallBlock, 0, s>>>(g, npart, pp, ms); count_launch(); }
+  if (pv && ls)
+    { k_move_wrap_sweeps<<<(npart + 31) / 32, kMoveSweepThreads, 0, s>>>(g, npart, pp, ms, *pv, *ls); count_launch(); }
+  else
+    { k_move_wrap<<<(npart + kSmallBlock - 1) / kSmallBlock, kSmallBlock, 0, s>>>(g, npart, pp, ms); count_launch(); }
   cudaStream_t so = s;
   if (aux) {
     cudaEventRecord(fork, s);
