@@ -878,9 +878,9 @@ __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, Partic
   }
 }
 template <typename T>
-// (FP64: eight 128-thread blocks per SM, 64 registers, so that the 1000
-// particle blocks of the workload run in one wave)
-__global__ void __launch_bounds__(bounce_threads<T>(), (sizeof(T) == 8 ? 8 : 1)) k_bounce(Geometry g, ParticleView pv, const T* f, int pushed,
+// (64 registers: FP64 eight 128-thread blocks per SM, FP32 four 256-thread
+// blocks, so that the 1000 particle blocks of the workload take fewer waves)
+__global__ void __launch_bounds__(bounce_threads<T>(), (sizeof(T) == 8 ? 8 : 4)) k_bounce(Geometry g, ParticleView pv, const T* f, int pushed,
                                                const int32_t* __restrict__ isnodes, LinkSlab ls,
                                                double* fHIp, double* torqp) {
   k_bounce_body<T, bounce_threads<T>()>(blockIdx.x, gridDim.x, g, pv, f, pushed, isnodes, ls, fHIp, torqp);
