@@ -1503,7 +1503,7 @@ namespace {
   const int nblk = (nblocks_expr);                   \
   if ((int)blockIdx.x >= nblk) return;
 
-__global__ void __launch_bounds__(PB) k_bounce_multi(const BoxParticles* boxes) {
+__global__ void __launch_bounds__(PB, 4) k_bounce_multi(const BoxParticles* boxes) {
   BOX_OR_RETURN(B.pv.npart)
   k_bounce_body<float, PB>(blockIdx.x, nblk, B.g, B.pv, B.f, 1, B.flags_cur, B.ls, B.ms.fHIp, B.ms.torqp);
 }
