@@ -1390,7 +1390,7 @@ __device__ __forceinline__ void k_fill_events_body(int bx, int gx, Geometry g, P
   }
 }
 template <typename T>
-__global__ void __launch_bounds__(128) k_fill_events(Geometry g, ParticleView pv, PartParams pp,
+__global__ void __launch_bounds__(128, 8) k_fill_events(Geometry g, ParticleView pv, PartParams pp,
                                                      const double* __restrict__ ypglbp,
                                                      const double* __restrict__ wpp,
                                                      const double* __restrict__ omgpp,
