@@ -6,10 +6,9 @@ These tests hold that path to the FP64 contract against the CPU oracle, to
 rounding against the all-FP64 arithmetic, and exercise the nodes it hands
 back to the FP64 path: populations of 1/8 and more, and (staged kernel, FP64
 storage) quiescent nodes whose populations are all below 2^-12.  The direct
-kernel's fused steps keep the populations in 64-bit fixed point at 2^-58;
-the reference stores full populations w rho0 + f' in FP64, whose resolution
-at the rest population 1/3 is 2^-54 = 5.6e-17, so the fixed-point storage
-resolves every population 16 times finer than the reference itself.
+kernel's fused steps keep the populations in 64-bit fixed point at 2^-58:
+absolute resolution 3.5e-18, the FP64 rounding of the largest deviations of
+a flowing field, but absolute rather than relative for tiny deviations.
 """
 
 import numpy as np
@@ -73,8 +72,8 @@ def test_fixed_sums_hand_back_out_of_range_nodes(require_gpu, oracle_mod, varian
     populations far below 2^-12.  The fast nodes take the FP64 path in both
     kernels.  The staged kernel (FP64 storage) also hands the quiescent nodes
     to the FP64 path, which keeps FP64's relative precision there; the direct
-    kernel stores them in fixed point, within the reference's own resolution
-    of the full populations (2^-54 at the rest population 1/3)."""
+    kernel stores them in fixed point, to a few units of its absolute
+    resolution 2^-58 over three steps (bound: 2^-54)."""
     from multiphase_flow_codes_gb300.engine import LBMBox
     n = 32
     cfg = capi.config_init(capi.LBM_PRESET_BOX, n, n, n, 0, 4.0, 1.0)
