@@ -547,29 +547,6 @@ bool plan_staged(lbm_ctx* c, int variant, int stages, int ctas_per_sm, StagedPla
                 : plan_fused_staged<double>(c->g, stages, ctas_per_sm, packed, groups, p, fx);
 }
 
-// the part of a fused step after stream + collide: bounce-back, the
-// particle subroutines, and the host-side state of the step
-template <typename T>
-void step_post_t(lbm_ctx* c) {
-  T* fout = fbuf<T>(c, 1 - c->cur);
-  if (c->particles_on) {
-    prof_begin(c);
-    launch_bounce_back<T>(c->g, pview(c), fout, 1, c->flags[c->fcur], c->links, c->fHIp,
-                          c->torqp, c->stream);
-    prof_end(c, LBM_PHASE_BOUNCE);
-    bounce_store_aux<T>(c, fout);
-    particle_phase<T>(c, fout);
-  } else {
-    // without particles both flag buffers say "all fluid"; flipping keeps
-    // the buffer parity the same for every box of a batch
-    c->fcur = 1 - c->fcur;
-  }
-  c->cur = 1 - c->cur;
-  c->fmacro = c->latest;
-  c->macro_pending = true;
-  c->macro_derived = true;
-}
-
 template <typename T>
 void fused_step_t(lbm_ctx* c) {
   do_forcing(c);
@@ -590,7 +567,9 @@ void fused_step_t(lbm_ctx* c) {
     bounce_store_aux<T>(c, fout);
     particle_phase<T>(c, fout);
   } else {
-    c->fcur = 1 - c->fcur;  // as step_post_t
+    // without particles both flag buffers say "all fluid"; flipping keeps
+    // the buffer parity the same for every box of a batch
+    c->fcur = 1 - c->fcur;
   }
   c->cur = 1 - c->cur;
   c->fmacro = c->latest;
@@ -614,7 +593,7 @@ void unfused_step_t(lbm_ctx* c) {
   launch_streaming<T>(c->g, fbuf<T>(c, c->cur), fbuf<T>(c, 1 - c->cur), c->stream);
   c->cur = 1 - c->cur;
   if (c->particles_on) particle_phase<T>(c, fbuf<T>(c, c->cur));
-  else c->fcur = 1 - c->fcur;  // as step_post_t
+  else c->fcur = 1 - c->fcur;  // as fused_step_t
   c->fmacro = c->latest;
   c->macro_pending = true;
   c->macro_derived = true;
@@ -2079,7 +2058,7 @@ std::string batch_step_eager(lbm_batch* b) {
   if (b->stochastic &&
       !(err = chk(cudaStreamWaitEvent(b->main, b->ev_side_all, 0), "side join", 0)).empty())
     return err;
-  for (lbm_ctx* c : b->ctx) {  // host side of the step (step_post_t without launches)
+  for (lbm_ctx* c : b->ctx) {  // host side of the step, as the end of fused_step_t
     c->fcur = 1 - c->fcur;
     c->cur = 1 - c->cur;
     c->fmacro = c->latest;

@@ -1402,6 +1402,18 @@ __global__ void __launch_bounds__(128, 8) k_fill_events(Geometry g, ParticleView
 
 }  // namespace
 
+// SMs of the current device (queried once)
+int sm_count() {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+      sms = 1;
+  }
+  return sms;
+}
+
 void launch_links(const Geometry& g, const ParticleView& pv, int32_t* isnodes, LinkSlab ls,
                   DevStatus* st, int alpha_fp32, cudaStream_t s, bool sweeps_done) {
   if (pv.npart <= 0) return;
@@ -1425,13 +1437,7 @@ void launch_bounce_scatter(const Geometry& g, const ParticleView& pv, T* f, int 
   // four blocks per SM, looping over particles: the stores run beside the
   // particle kernels of the critical path and leave half of every SM's
   // thread slots to them
-  static int sms = 0;
-  if (sms == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
-      sms = 1;
-  }
+  const int sms = sm_count();
   const int nblk = pv.npart < 4 * sms ? pv.npart : 4 * sms;
   { k_bounce_store<T><<<nblk, PB, 0, s>>>(g, pv, f, pushed, ls, st); count_launch(); }
 }
@@ -1485,13 +1491,7 @@ void launch_filling(const Geometry& g, const ParticleView& pv, const PartParams&
   { k_fill_detect<<<pv.npart, PB, 0, s>>>(g, pv, pp, ypglbp, isnodes, isnodes0, fl, st); count_launch(); }
   // eight blocks of four warps per SM: one refill event per warp for up to
   // 32 events an SM (the events' serial FP64 chains then run side by side)
-  static int sms = 0;
-  if (sms == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
-      sms = 1;
-  }
+  const int sms = sm_count();
   { k_fill_events<T><<<8 * sms, 128, 0, s>>>(g, pv, pp, ypglbp, wpp, omgpp, isnodes, isnodes0, f, fl, st); count_launch(); }
 }
 
