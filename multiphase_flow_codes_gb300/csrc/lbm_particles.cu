@@ -1086,16 +1086,20 @@ __device__ __forceinline__ void k_wrap_body(int bx, int gx, Geometry g, int npar
 __global__ void k_wrap(Geometry g, int npart, MoveState ms) {
   k_wrap_body(blockIdx.x, gridDim.x, g, npart, ms);
 }
-// beads_move, the wrap and the nearest-image sweeps of beads_links for 32
-// particles per block of 96 threads: thread t < 32 moves and wraps particle
-// 32 bx + t, then thread t sweeps axis t % 3 of particle 32 bx + t / 3 (the
-// fused time step; the sweeps need only their own particle's new centre)
-constexpr int kMoveSweepThreads = 96;
+// beads_move, the wrap and the nearest-image sweeps of beads_links for
+// kMoveSweepParts particles per block of 3 kMoveSweepParts threads: thread
+// t < kMoveSweepParts moves and wraps particle kMoveSweepParts bx + t, then
+// thread t sweeps axis t % 3 of particle kMoveSweepParts bx + t / 3 (the
+// fused time step; the sweeps need only their own particle's new centre).
+// Eight particles (one warp) per block spread the serial FP64 chains over as
+// many SMs as there are blocks.
+constexpr int kMoveSweepParts = 8;
+constexpr int kMoveSweepThreads = 3 * kMoveSweepParts;
 __global__ void __launch_bounds__(kMoveSweepThreads) k_move_wrap_sweeps(Geometry g, int npart, PartParams pp,
                                                                      MoveState ms, ParticleView pv,
                                                                      LinkSlab ls) {
-  if (threadIdx.x < 32) {
-    const int p = blockIdx.x * 32 + threadIdx.x;
+  if (threadIdx.x < kMoveSweepParts) {
+    const int p = blockIdx.x * kMoveSweepParts + threadIdx.x;
     move_particle(p, npart, pp, ms);
     wrap_particle(p, g, npart, ms);
   }
@@ -1467,7 +1471,7 @@ bool launch_move_redistribute(const Geometry& g, int npart, const PartParams& pp
                               cudaEvent_t join, const ParticleView* pv, LinkSlab* ls) {
   if (npart <= 0) return false;
   if (pv && ls)
-    { k_move_wrap_sweeps<<<(npart + 31) / 32, kMoveSweepThreads, 0, s>>>(g, npart, pp, ms, *pv, *ls); count_launch(); }
+    { k_move_wrap_sweeps<<<(npart + kMoveSweepParts - 1) / kMoveSweepParts, kMoveSweepThreads, 0, s>>>(g, npart, pp, ms, *pv, *ls); count_launch(); }
   else
     { k_move_wrap<<<(npart + kSmallBlock - 1) / kSmallBlock, kSmallBlock, 0, s>>>(g, npart, pp, ms); count_launch(); }
   cudaStream_t so = s;
