@@ -291,6 +291,75 @@ def workload(name: str):
                       name=name, ny=ny, nz=nz)
 
 
+def describe(name, c, npart, k0, urms, dtype, world):
+    """The JSON line's config block."""
+    N = c.nx * c.ny * c.nz
+    return {"workload": name, "grid": [c.nx, c.ny, c.nz], "particles": npart,
+            "radius": c.rad, "density_ratio": c.rhopart, "k0": k0, "u_rms": urms,
+            "forcing": "stochastic low-k (|k| < sqrt 8)", "mrt_type": c.mrt_type,
+            "l2": "inputs larger than L2 (populations %.2f GB)" % (2 * 19 * N * (8 if dtype == "f64" else 4) / 1e9),
+            "parallelism": f"replicas x{world}"}
+
+
+def reference_arm(args):
+    """--impl reference: the CPU restatement of the reference's time step.
+
+    Loads nothing of the engine: the parameter block comes from the
+    oracle's own restatement of the reference constants (oracle/config.py),
+    the seeded inputs from the numpy generators, the timed steps from the
+    oracle library.  Under torchrun only rank 0 runs."""
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    import re
+    import oracle
+    from oracle import config as ocfg
+    from multiphase_flow_codes_gb300 import inputs
+    name = args.workload
+    if name in ocfg.WORKLOADS:
+        c, npart, k0, urms = ocfg.workload_config(name)
+    else:
+        m = re.fullmatch(r"box(\d+)_p(\d+)_(f64|f32)", name)
+        if not m:
+            raise SystemExit(f"unknown workload {name}")
+        n, npart = int(m.group(1)), int(m.group(2))
+        k0, urms = (8.0 if n >= 256 else 4.0), 0.04
+        c = ocfg.config_init(ocfg.PRESET_BOX, n, n, n, npart, 4.0, 2.5)
+    N = c.nx * c.ny * c.nz
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    u = inputs.spectral_velocity(c.nx, k0, urms, seed=54321, ny=c.ny, nz=c.nz)
+    y = inputs.initpartpos(c.nx, c.ny, c.nz, npart, c.rad, c.mingap, seed=12345) \
+        if npart else np.zeros((0, 3))
+    o = oracle.OracleBox(c)
+    o.initpop(*u)
+    o.macrovar()
+    if npart:
+        o.release_particles(y)
+    steps = max(1, min(args.steps, args.ref_max_steps))
+    warm = max(0, min(args.warmup, args.ref_max_steps - steps))
+    if warm:
+        rc = o.step(warm)
+        if rc:
+            raise RuntimeError(f"oracle step failed with {rc}")
+    t0 = time.perf_counter()
+    rc = o.step(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    if rc:
+        raise RuntimeError(f"oracle step failed with {rc}")
+    v = N * steps / dt / 1e6
+    line = {"impl": "reference", "metric": "MLUPS", "value": v, "unit": "MLUPS",
+            "n_gpus": 0, "steps": steps, "warmup": warm, "ms_per_step": dt * 1e3 / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic seeded", "config": describe(name, c, npart, k0, urms, "f64", 1),
+            "cpu_baseline": {"value": v, "unit": "MLUPS", "cores": cores, "kind": "port",
+                             "sample": f"{steps} full steps of {name} after {warm} untimed ones (CPU "
+                                       "restatement of the reference, OpenMP over all host cores; the "
+                                       "Fortran/MPI/FFTW2 reference has no toolchain on this host)"},
+            "e2e": {"value": v, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -318,51 +387,28 @@ def main():
     ap.add_argument("--variant", default=None,
                     help="stream+collide kernel as 'variant,stages,groups,ctas_per_sm' "
                          "(default: autotuned on the workload)")
-    ap.add_argument("--ref-max-steps", type=int, default=6,
-                    help="--impl reference: at most this many full CPU steps are timed")
+    ap.add_argument("--ref-max-steps", type=int, default=200,
+                    help="--impl reference: at most this many full CPU steps (warm-up included)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
 
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+
     from multiphase_flow_codes_gb300.replicas import Replicas
-    rep = Replicas("nccl" if args.impl == "ours" else "gloo")
+    rep = Replicas("nccl")
     world, rank, local = rep.world, rep.rank, rep.local
     wl = workload(args.workload)
     c = wl.cfg
     N = c.nx * c.ny * c.nz
     from multiphase_flow_codes_gb300 import _capi as capi
     dtype = "f64" if c.precision == capi.LBM_PREC_F64 else "f32"
-    cfg_desc = {"workload": wl.name, "grid": [c.nx, c.ny, c.nz], "particles": wl.npart,
-                "radius": c.rad, "density_ratio": c.rhopart, "k0": wl.k0, "u_rms": wl.urms,
-                "forcing": "stochastic low-k (|k| < sqrt 8)", "mrt_type": c.mrt_type,
-                "l2": "inputs larger than L2 (populations %.2f GB)" % (2 * 19 * N * (8 if dtype == "f64" else 4) / 1e9),
-                "parallelism": f"replicas x{world}"}
+    cfg_desc = describe(wl.name, c, wl.npart, wl.k0, wl.urms, dtype, world)
     if dtype == "f64":
         cfg_desc["collision_sums"] = ("integer-coefficient moment sums exact in 64-bit fixed point, "
                                       "products FP64" if args.sums == "fixed" else "all FP64")
-
-    if args.impl == "reference":
-        if rank != 0:
-            return
-        import multiprocessing
-        cores = os.cpu_count() or 1
-        u, y = make_inputs(wl)
-        # a full step of the 256^3 workload takes seconds on the host cores:
-        # time a bounded number of them so the run ends within minutes
-        steps = max(1, min(args.steps, args.ref_max_steps))
-        dt = cpu_oracle(wl, u, y, steps, cores)
-        v = N * steps / dt / 1e6
-        line = {"impl": "reference", "metric": "MLUPS", "value": v, "unit": "MLUPS",
-                "n_gpus": 0, "steps": steps, "warmup": 0, "ms_per_step": dt * 1e3 / steps,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic seeded", "config": cfg_desc,
-                "cpu_baseline": {"value": v, "unit": "MLUPS", "cores": cores, "kind": "port",
-                                 "sample": f"{steps} full steps of {wl.name} (CPU restatement of the "
-                                           "reference, OpenMP; the Fortran/MPI/FFTW2 reference has no "
-                                           "toolchain on this host)"},
-                "e2e": {"value": v, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line), flush=True)
-        return
 
     import torch
     torch.cuda.set_device(local)

@@ -76,3 +76,18 @@ def test_fma_throughput_probe(engine_lib, require_gpu):
     assert 0.1 < f64.value < 200.0
     assert f32.value > f64.value
     assert engine_lib.lbm_fma_throughput(capi.LBM_PREC_F64, None) == capi.LBM_ERR_ARG
+
+
+@pytest.mark.parametrize("preset,dims,npart,rad,ratio", [
+    (capi.LBM_PRESET_BOX, (64, 64, 64), 16, 4.5, 5.0),
+    (capi.LBM_PRESET_BOX, (256, 256, 256), 1000, 4.0, 2.5),
+    (capi.LBM_PRESET_CHANNEL, (96, 64, 128), 40, 4.0, 1.0),
+])
+def test_oracle_config_equals_engine_config(engine_lib, preset, dims, npart, rad, ratio):
+    """The CPU reference leg of the benchmark builds its parameter block
+    without the engine library; every field must equal the engine's."""
+    from oracle import config as ocfg
+    a = capi.config_init(preset, *dims, npart, rad, ratio)
+    b = ocfg.config_init(preset, *dims, npart, rad, ratio)
+    assert C.sizeof(ocfg.lbm_config) == C.sizeof(capi.lbm_config)
+    assert bytes(a) == bytes(b)
