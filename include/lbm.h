@@ -426,10 +426,14 @@ int lbm_fma_throughput(int precision, double* tflops);
  * rejected with LBM_ERR_ARG.  All calls share that array and it keeps the
  * last call's partial sums: calls that overlap on one GPU (for example on
  * two streams) race on it, so the caller must order them.  No entry needs
- * clearing between calls (each call writes every entry it reads).  The first
- * call on each device looks up
- * the array's device address with that device current; make that first call
- * before any stream capture. */
+ * clearing between calls (each call writes every entry it reads).  Every
+ * call looks up the array's device address in the current context (so a
+ * caller's own driver-API context, or one recreated after cudaDeviceReset,
+ * gets its own instance); the first call in a context also loads the
+ * library's device code there, so make that first call before any stream
+ * capture.  Returns LBM_ERR_STATE without launching anything when a CUDA
+ * error is already pending from earlier work (left pending for its owner),
+ * and LBM_ERR_CUDA when one of this call's own launches fails. */
 #define LBM_NOALLOC_MAX_PLANES 4096
 int lbm_mass_momentum_noalloc(const double* f, int nx, int ny, int nz, double* out, void* stream);
 

@@ -9,20 +9,12 @@
 // alone.  Its scratch space (one partial sum per z-plane) is the file-scope
 // device array below: every GPU that loads this library holds it (128 KiB)
 // until the process exits, and every call shares it.
-#include <mutex>
-
 #include "lbm_internal.cuh"
 
 namespace {
 
-constexpr int kMaxDevices = 64;
-
 // per-plane partial sums (mass, momentum x, y, z) of the last call
 __device__ __align__(256) double g_plane_sums[LBM_NOALLOC_MAX_PLANES * 4];
-
-// device address of g_plane_sums, looked up once per device
-double* g_plane_sums_addr[kMaxDevices] = {nullptr};
-std::mutex g_addr_mutex;
 
 // Stage 1: block z sums plane z into g_plane_sums (every entry the second
 // stage reads is written first, so no clearing is needed).  Deterministic:
@@ -73,21 +65,16 @@ __global__ void __launch_bounds__(256) k_plane_total(const double* __restrict__ 
   if (threadIdx.x < 4) out[threadIdx.x] = sm[threadIdx.x][0];
 }
 
-// Device address of the scratch array on the current device, looked up
-// (cudaGetSymbolAddress) on the first call made with that device current.
-cudaError_t scratch_on_current_device(double** ptr) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+// Device address of the scratch array in the current context.  It is looked
+// up on every call (cudaGetSymbolAddress allocates nothing): a cached value
+// would go stale for a caller that runs its own driver-API context or
+// recreates the context after cudaDeviceReset, since each context holds its
+// own instance of the array.
+cudaError_t scratch_in_current_context(double** ptr) {
+  double* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void**>(&p), g_plane_sums);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lock(g_addr_mutex);
-  if (g_plane_sums_addr[dev] == nullptr) {
-    double* p = nullptr;
-    e = cudaGetSymbolAddress(reinterpret_cast<void**>(&p), g_plane_sums);
-    if (e != cudaSuccess) return e;
-    g_plane_sums_addr[dev] = p;
-  }
-  *ptr = g_plane_sums_addr[dev];
+  *ptr = p;
   return cudaSuccess;
 }
 
@@ -98,13 +85,18 @@ extern "C" int lbm_mass_momentum_noalloc(const double* f, int nx, int ny, int nz
   if (!f || !out || nx < 1 || ny < 1 || nz < 1) return LBM_ERR_ARG;
   if (nz > LBM_NOALLOC_MAX_PLANES) return LBM_ERR_ARG;  // scratch holds one sum per plane
   if ((long long)nx * ny > (1LL << 30)) return LBM_ERR_ARG;
+  // An error left pending by earlier work is not this call's: report it as
+  // such, launch nothing and leave it for its owner to read.
+  if (cudaPeekAtLastError() != cudaSuccess) return LBM_ERR_STATE;
   double* sums = nullptr;
-  if (scratch_on_current_device(&sums) != cudaSuccess) return LBM_ERR_CUDA;
+  if (scratch_in_current_context(&sums) != cudaSuccess) return LBM_ERR_CUDA;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const long long N = (long long)nx * ny * nz;
   k_plane_sums<<<nz, 256, 0, s>>>(f, nx, ny, N, sums);
   lbm::count_launch();
+  if (cudaGetLastError() != cudaSuccess) return LBM_ERR_CUDA;  // this launch's own error
   k_plane_total<<<1, 256, 0, s>>>(sums, nz, out);
   lbm::count_launch();
-  return cudaGetLastError() == cudaSuccess ? LBM_OK : LBM_ERR_CUDA;
+  if (cudaGetLastError() != cudaSuccess) return LBM_ERR_CUDA;
+  return LBM_OK;
 }

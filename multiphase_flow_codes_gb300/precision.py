@@ -16,6 +16,14 @@ and, at each checkpoint step, compares the quantities the workload names:
 The FP64 GPU path is itself held to the CPU oracle within 1e-12 by the
 parity tests, so it stands for the FP64 oracle at sizes where running the
 oracle for thousands of steps is out of reach.
+
+Beside each FP32 row the report gives the FP64 floor: a second FP64 box
+whose collision sums are done in plain FP64 instead of exact fixed point,
+so it differs from the first only by FP64 rounding.  Whatever grows between
+those two is the turbulence amplifying rounding differences, not FP32; an
+FP32 error far above the floor is FP32's own.  The population difference
+is also split into nodes whose solid flags agree in both runs and nodes
+where a sphere covers a node in one run and not in the other.
 """
 
 from __future__ import annotations
@@ -54,15 +62,37 @@ def compare(s32: dict, s64: dict, p32: dict, p64: dict, slip32: np.ndarray,
     return out
 
 
+def population_split(b_test: LBMBox, b_ref: LBMBox) -> dict:
+    """Max-norm population difference (relative to max |f_ref|) over the nodes
+    whose solid flags agree and over those whose flags differ."""
+    f_ref = b_ref.get_f()
+    scale = float(np.abs(f_ref).max()) or 1.0
+    d = np.abs(b_test.get_f() - f_ref).max(axis=0)
+    del f_ref
+    _, is_t = b_test.get_flags()
+    _, is_r = b_ref.get_flags()
+    agree = is_t == is_r
+    return {"pop_rel_flags_agree": float(d[agree].max() / scale) if agree.any() else 0.0,
+            "pop_rel_flags_differ": float(d[~agree].max() / scale) if (~agree).any() else 0.0,
+            "nodes_flags_differ": int((~agree).sum())}
+
+
 def error_report(cfg64: capi.lbm_config, u, ypglb: np.ndarray,
-                 checkpoints=(10, 100, 2000), stream_ptr: int | None = None) -> list:
-    """Step an FP64 and an FP32 copy of the same box to each checkpoint and
-    compare them there; returns one dict per checkpoint."""
+                 checkpoints=(10, 100, 2000), stream_ptr: int | None = None,
+                 floor: bool = True, split_at=(10,)) -> list:
+    """Step an FP64 and an FP32 copy of the same box (and, with `floor`, a
+    second FP64 copy with plain-FP64 collision sums) to each checkpoint and
+    compare them there; returns one dict per checkpoint with the FP32 errors
+    and, under "fp64_floor", the FP64-against-FP64 errors."""
     cfg32 = type(cfg64).from_buffer_copy(cfg64)
     cfg32.precision = capi.LBM_PREC_F32
     cfg64 = type(cfg64).from_buffer_copy(cfg64)
     cfg64.precision = capi.LBM_PREC_F64
     boxes = [LBMBox(cfg64), LBMBox(cfg32)]
+    if floor:
+        boxes.append(LBMBox(cfg64))
+        boxes[2].set_sums(capi.LBM_SUMS_FLOAT if boxes[0].sums() == capi.LBM_SUMS_FIXED
+                          else capi.LBM_SUMS_FIXED)
     r_in, r_out = cfg64.rad + 1.0, cfg64.rad + 3.0
     try:
         for b in boxes:
@@ -78,14 +108,21 @@ def error_report(cfg64: capi.lbm_config, u, ypglb: np.ndarray,
             for b in boxes:
                 b.step(cp - done)
             done = cp
-            s64, s32 = (b.statistics() for b in boxes)
-            p64, p32 = (b.get_particles() for b in boxes)
+            stats = [b.statistics() for b in boxes]
+            parts = [b.get_particles() for b in boxes]
             if len(ypglb):
-                sl64, sl32 = (b.particle_slip(r_in, r_out) for b in boxes)
+                slips = [b.particle_slip(r_in, r_out) for b in boxes]
             else:
-                sl64 = sl32 = np.zeros((0, 3))
+                slips = [np.zeros((0, 3))] * len(boxes)
             row = {"step": cp}
-            row.update(compare(s32, s64, p32, p64, sl32, sl64))
+            row.update(compare(stats[1], stats[0], parts[1], parts[0], slips[1], slips[0]))
+            if cp in split_at:
+                row.update(population_split(boxes[1], boxes[0]))
+            if floor:
+                fl = compare(stats[2], stats[0], parts[2], parts[0], slips[2], slips[0])
+                if cp in split_at:
+                    fl.update(population_split(boxes[2], boxes[0]))
+                row["fp64_floor"] = fl
             rows.append(row)
         return rows
     finally:

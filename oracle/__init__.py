@@ -63,6 +63,8 @@ def lib() -> C.CDLL:
         L.orc_step.argtypes = [P, C.c_int]
         L.orc_ran1_sequence.argtypes = [C.c_int32, C.c_int, C.POINTER(C.c_double)]
         L.orc_ran1_sequence.restype = None
+        L.orc_ran1_state.argtypes = [C.c_int32, C.c_int]
+        L.orc_ran1_state.restype = C.c_int32
         _lib = L
     return _lib
 
@@ -76,6 +78,11 @@ def ran1_sequence(seed: int, n: int) -> np.ndarray:
     out = np.empty(n)
     lib().orc_ran1_sequence(seed, n, out.ctypes.data_as(C.POINTER(C.c_double)))
     return out
+
+
+def ran1_state(seed: int, n: int) -> int:
+    """The Park-Miller state after n ran1 draws from seed (see lbm_oracle.cpp)."""
+    return int(lib().orc_ran1_state(seed, n))
 
 
 class OracleBox:

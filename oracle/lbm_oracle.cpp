@@ -1146,4 +1146,14 @@ void orc_ran1_sequence(int32_t seed, int n, double* out) {
   std::memset(iv, 0, sizeof(iv));
   for (int i = 0; i < n; ++i) out[i] = ran1(&idum, &iy, iv);
 }
+// The Park-Miller state idum after n ran1 draws from a fresh state seeded
+// with -seed: the core sequence x_{k+1} = 16807 x_k mod (2^31 - 1) from
+// x_0 = seed, advanced by NTAB + 8 = 40 steps at the first draw (the shuffle
+// table's warm-up) and one step per draw (for the known-answer tests).
+int32_t orc_ran1_state(int32_t seed, int n) {
+  int32_t idum = -seed, iy = 0, iv[32];
+  std::memset(iv, 0, sizeof(iv));
+  for (int i = 0; i < n; ++i) ran1(&idum, &iy, iv);
+  return idum;
+}
 }

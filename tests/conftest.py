@@ -85,3 +85,15 @@ def gpu_links(box):
     node, ipop, part, alpha = box.get_links()
     order = np.lexsort((ipop, node, part))
     return part[order], node[order], ipop[order], alpha[order]
+
+
+def link_term_scale(o, links):
+    """Per particle, the sum over its links of 2 |f| of the two populations a
+    link exchanges (the magnitude of the momentum-exchange terms whose sum
+    is fHIp), from the oracle's post-step populations."""
+    part, node, ipop, _ = links
+    f = o.f.reshape(19, -1)
+    mag = np.abs(f[ipop, node]) + np.abs(f[IPOPP[ipop], node])
+    s = np.zeros(o.npmax)
+    np.add.at(s, part - 1, 2.0 * mag)
+    return s

@@ -4,14 +4,18 @@ Tolerances, as the path's contract states them:
   * integer work (solid flags, link sets, refill events) must match bit for
     bit; link fractions (FP64 data) within 1e-13;
   * FP64 populations, macroscopic fields and particle state within 1e-12
-    (max-norm relative) over 10 steps;
+    (max-norm relative) over 10 steps; the hydrodynamic force and torque
+    (fHIp, torqp) within 1e-12 relative to the sum of the magnitudes of the
+    particle's link terms, because they are sums over hundreds of links that
+    cancel to a small fraction of the terms (their rounding scales with the
+    terms, whatever the order of summation);
   * FP32-shifted populations within 1e-5 of the FP64 oracle over 10 steps.
 """
 
 import numpy as np
 import pytest
 
-from conftest import gpu_links, oracle_links, relerr
+from conftest import gpu_links, link_term_scale, oracle_links, relerr
 
 from multiphase_flow_codes_gb300 import _capi as capi
 from multiphase_flow_codes_gb300 import inputs
@@ -59,6 +63,22 @@ def check_links(o, box, tol_alpha=1e-13):
     assert np.abs(ao - ag).max() <= tol_alpha, np.abs(ao - ag).max()
 
 
+def check_force_torque(o, box, tol=TOL64):
+    """fHIp and torqp against the oracle, relative to the link-term scale;
+    returns the worst errors (scaled, and in the max norm for the record)."""
+    links = oracle_links(o)
+    n = box.npart
+    p = box.get_particles()
+    scale = link_term_scale(o, links)[:n, None]
+    out = {}
+    for k in ("fHIp", "torqp"):
+        d = np.abs(p[k] - getattr(o, k)[:n])
+        out[k] = float((d / np.maximum(scale, 1e-300)).max())
+        out[k + "_maxnorm"] = relerr(p[k], getattr(o, k)[:n])
+        assert out[k] <= tol, (k, out)
+    return out
+
+
 def check_flags(o, box):
     ib, isn = box.get_flags()
     assert np.array_equal(ib, o.ibnodes)
@@ -87,6 +107,20 @@ def test_forcing_state_matches(require_gpu, oracle_mod):
     assert np.array_equal(iv, o.ivf)
     bo = np.concatenate([o.b1r, o.b2r, o.b3r])
     assert relerr(b, bo) <= 1e-14
+
+
+def test_forcing_generator_known_answer(require_gpu, oracle_mod):
+    """The device's ranff state after k FORCING calls (450 draws each, drawn
+    by jump-ahead) is the minimal-standard sequence from seed 1: after the
+    40-step warm-up and 450 k draws, 16807^(40 + 450 k) mod (2^31 - 1)
+    (Park & Miller, CACM 1988)."""
+    o, box = make_pair(oracle_mod, shape=(16, 16, 16))
+    box.set_forcing_state(-1, 0, np.zeros(32, dtype=np.int32), np.zeros(450))
+    for k in range(1, 4):
+        box.FORCING()
+        iseed, _, _, _ = box.get_forcing_state()
+        assert iseed == pow(16807, 40 + 450 * k, 2**31 - 1), k
+        assert iseed == oracle_mod.ran1_state(1, 450 * k)
 
 
 def test_unfused_subroutines_match(require_gpu, oracle_mod):
@@ -126,7 +160,8 @@ def test_particles_box64_geometry_10_steps(require_gpu, oracle_mod):
         check_flags(o, box)
         p = box.get_particles()
         assert relerr(p["ypglb"], o.ypglb) <= TOL64
-        assert relerr(p["fHIp"], o.fHIp) <= 1e-10
+        e = check_force_torque(o, box)
+    print(f"\nbox64_p16, 10 steps: {e}")
     assert relerr(box.get_f(), o.f) <= TOL64
     check_links(o, box)
 
@@ -149,7 +184,10 @@ def test_moving_particles_refill(require_gpu, oracle_mod):
     assert refilled > 0
     p = box.get_particles()
     assert relerr(p["ypglb"], o.ypglb) <= TOL64
-    assert relerr(p["omgp"], o.omgp) <= 1e-10
+    print(f"\nrefill: omgp {relerr(p['omgp'], o.omgp):.2e} wp {relerr(p['wp'], o.wp):.2e}")
+    assert relerr(p["omgp"], o.omgp) <= TOL64
+    assert relerr(p["wp"], o.wp) <= TOL64
+    check_force_torque(o, box)
     check_links(o, box)
 
 
@@ -165,7 +203,44 @@ def test_channel_particles(require_gpu, oracle_mod):
         check_flags(o, box)
     assert relerr(box.get_f(), o.f) <= TOL64
     p = box.get_particles()
-    assert relerr(p["flubp"], o.flubp) <= 1e-10 or np.abs(o.flubp).max() == 0
+    assert relerr(p["flubp"], o.flubp) <= TOL64
+
+
+def test_channel_wall_lubrication(require_gpu, oracle_mod):
+    """Spheres inside the particle-wall lubrication range of both channel
+    walls (centre closer than rad + mingap_w to x = 0 or x = nx,
+    3DChannel.../partlib.f90:2317-2356) and a pair inside the
+    particle-particle range: the lubrication forces are nonzero and match
+    the oracle every step."""
+    from multiphase_flow_codes_gb300.engine import LBMBox
+    shape = (36, 40, 32)
+    cfg = capi.config_init(capi.LBM_PRESET_CHANNEL, *shape, 4, 4.0, 1.0)
+    o = oracle_mod.OracleBox(cfg)
+    u = tuple(np.zeros((shape[2], shape[1], shape[0])) for _ in range(3))
+    o.initpop(*u)
+    o.macrovar()
+    box = LBMBox(cfg)
+    box.set_f(o.f.copy())
+    box.macrovar()
+    y = np.array([[5.1, 8.3, 7.7],               # 1.1 from the wall x = 0
+                  [shape[0] - 5.4, 30.2, 20.6],  # 1.4 from the wall x = nx
+                  [18.0, 20.0, 9.0], [18.3, 29.1, 9.4]])  # pair 1.1 apart
+    wp = np.array([[-0.01, 0.0, 0.0], [0.01, 0.0, 0.0], [0.0, 0.01, 0.0], [0.0, -0.01, 0.0]])
+    o.release_particles(y, wp)
+    box.release_particles(y, wp)
+    worst = 0.0
+    for s in range(10):
+        o.step(1)
+        box.step(1)
+        check_flags(o, box)
+        p = box.get_particles()
+        assert np.all(np.abs(o.flubp[:4]).max(axis=1) > 0), o.flubp[:4]
+        e = relerr(p["flubp"], o.flubp[:4])
+        worst = max(worst, e)
+        assert e <= TOL64, (s, e)
+        assert relerr(p["ypglb"], o.ypglb[:4]) <= TOL64
+    print(f"\nwall lubrication: flubp worst {worst:.2e}")
+    assert relerr(box.get_f(), o.f) <= TOL64
 
 
 def test_fp32_shifted_close_to_fp64(require_gpu, oracle_mod):
@@ -238,14 +313,20 @@ def test_bounce_cases_near_contact(require_gpu, oracle_mod):
     box.release_particles(y, wp, om)
     cases = _bounce_cases(o)
     assert min(cases) > 0, cases
+    worst = {}
     for s in range(10):
         o.step(1)
         box.step(1)
         check_flags(o, box)
-        if s == 0:  # the step whose bounce-back ran on the links above
-            assert relerr(box.get_particles()["fHIp"], o.fHIp) <= 1e-10
+        for k, v in check_force_torque(o, box).items():
+            worst[k] = max(worst.get(k, 0.0), v)
+        p = box.get_particles()
+        assert np.abs(o.flubp[:2]).max() > 0  # the pair is inside the lubrication range
+        worst["flubp"] = max(worst.get("flubp", 0.0), relerr(p["flubp"], o.flubp[:3]))
+        assert relerr(p["flubp"], o.flubp[:3]) <= TOL64
+    print(f"\nnear contact, worst over 10 steps: {worst}")
     assert relerr(box.get_f(), o.f) <= TOL64
     p = box.get_particles()
     assert relerr(p["ypglb"], o.ypglb) <= TOL64
-    assert relerr(p["fHIp"], o.fHIp) <= 1e-10
-    assert relerr(p["omgp"], o.omgp) <= 1e-10
+    assert relerr(p["omgp"], o.omgp) <= TOL64
+    assert relerr(p["wp"], o.wp) <= TOL64

@@ -1,0 +1,174 @@
+"""Parity of the benchmarked workloads with the oracle.
+
+* ``box256_p1000_f64`` (256^3, 1000 spheres R = 4, density ratio 2.5,
+  k0 = 8, u_rms = 0.04; the benchmark's seeded inputs) for 10 steps: solid
+  flags and link sets bit-exact every step; particle force, torque,
+  lubrication force, position, velocity and spin within the stated bounds
+  every step; populations after 10 steps in the max norm and value by value.
+* ``box64_p16_f64`` (64^3, 16 spheres R = 4.5, density ratio 5, k0 = 4,
+  u_rms = 0.03) for 1000 steps, the statistics the reference writes every
+  ``nstat`` steps (statistc: E(k) per shell and dissipation,
+  3DBox.../saveload.f90:1111-1338; ``main.f90:190-201``) and the particle
+  statistics (force RMS, mean slip) compared at steps 10, 100 and 1000.
+
+Tolerances and why:
+  populations, max norm             1e-12 relative to max |f| (10 steps)
+  populations, value by value       |df| / |f| <= 1e-12 where |f| >= 1e-5 and
+                                    <= 1e-10 where |f| >= 1e-7 (the FP64 path keeps
+                                    populations in 64-bit fixed point, absolute
+                                    resolution 2^-58 = 3.5e-18, between steps)
+  particle position / velocity      1e-12 (max norm)
+  fHIp, torqp                       1e-12 relative to the sum of the magnitudes
+                                    of the particle's link terms (a sum over ~500
+                                    links that cancels: its rounding scales with
+                                    the terms, not with the result)
+  flubp                             1e-12 (max norm; computed from positions)
+  long run, E(k) and dissipation    stated per checkpoint in LONG_RUN_TOL: two FP64
+                                    runs that differ only in rounding order drift
+                                    apart as the turbulence amplifies the
+                                    difference; the bounds hold that drift at the
+                                    level measured on GB300 with a 100x margin
+"""
+
+import numpy as np
+import pytest
+
+from conftest import gpu_links, link_term_scale, oracle_links, relerr
+
+from multiphase_flow_codes_gb300 import config, inputs
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+def seeded_pair(oracle_mod, wl):
+    """Oracle and engine from the benchmark's seeded inputs (flow seed 54321,
+    particle seed 12345), the engine initialised on the device as the
+    benchmark does."""
+    from multiphase_flow_codes_gb300.engine import LBMBox
+    c = wl.cfg
+    u = inputs.spectral_velocity(c.nx, wl.k0, wl.urms, seed=wl.flow_seed, ny=c.ny, nz=c.nz)
+    y = inputs.initpartpos(c.nx, c.ny, c.nz, wl.npart, c.rad, c.mingap, seed=wl.particle_seed)
+    o = oracle_mod.OracleBox(c)
+    o.initpop(*u)
+    o.macrovar()
+    o.release_particles(y)
+    box = LBMBox(c)
+    box.initpop(*u)
+    box.macrovar()
+    box.release_particles(y)
+    return o, box
+
+
+def check_particles(o, box, links, n, worst=None):
+    """Particle state against the oracle (bounds in the module docstring);
+    `worst` collects the largest error seen per quantity."""
+    p = box.get_particles()
+    errs = {}
+    for k in ("ypglb", "wp", "omgp", "flubp"):
+        errs[k] = relerr(p[k], getattr(o, k)[:n])
+    scale = link_term_scale(o, links)[:n, None]
+    for k in ("fHIp", "torqp"):
+        d = np.abs(p[k] - getattr(o, k)[:n])
+        errs[k] = float((d / np.maximum(scale, 1e-300)).max())
+        errs[k + "_maxnorm"] = relerr(p[k], getattr(o, k)[:n])
+    if worst is not None:
+        for k, e in errs.items():
+            worst[k] = max(worst.get(k, 0.0), e)
+    for k, e in errs.items():
+        if not k.endswith("_maxnorm"):
+            assert e <= TOL, (k, e)
+    return p
+
+
+def per_value_relerr(a, b, floor):
+    m = np.abs(b) >= floor
+    return float((np.abs(a - b)[m] / np.abs(b)[m]).max()) if m.any() else 0.0
+
+
+def test_box256_p1000_f64_ten_steps(require_gpu, oracle_mod):
+    """The benchmarked workload, 10 steps, every step against the oracle."""
+    wl = config.box256_p1000_f64()
+    o, box = seeded_pair(oracle_mod, wl)
+    n = wl.npart
+    worst = {}
+    for s in range(10):
+        assert o.step(1) == 0
+        box.step(1)
+        ib, isn = box.get_flags()
+        assert np.array_equal(ib, o.ibnodes), s
+        assert np.array_equal(isn, o.isnodes), s
+        lo = oracle_links(o)
+        lg = gpu_links(box)
+        assert len(lo[0]) == len(lg[0]), (s, len(lo[0]), len(lg[0]))
+        for a, b in zip(lo[:3], lg[:3]):
+            assert np.array_equal(a, b), s
+        assert np.abs(lo[3] - lg[3]).max() <= 1e-13, s
+        check_particles(o, box, lo, n, worst)
+    print("\nbox256_p1000_f64 particle state, worst over 10 steps: "
+          + ", ".join(f"{k} {v:.2e}" for k, v in sorted(worst.items())))
+    f = box.get_f()
+    e_max = relerr(f, o.f)
+    e5 = per_value_relerr(f, o.f, 1e-5)
+    e7 = per_value_relerr(f, o.f, 1e-7)
+    print(f"\nbox256_p1000_f64, 10 steps: populations max-norm {e_max:.2e}, "
+          f"per value (|f| >= 1e-5) {e5:.2e}, (|f| >= 1e-7) {e7:.2e}")
+    assert e_max <= TOL
+    assert e5 <= 1e-12
+    assert e7 <= 1e-10
+    box.close()
+    o.close()
+
+
+# step -> bound on (E(k) relative 2-norm, worst resolved shell, dissipation,
+# force RMS, mean slip); see the module docstring
+LONG_RUN_TOL = {
+    10: (1e-12, 1e-12, 1e-12, 1e-12, 1e-12),
+    100: (1e-11, 1e-11, 1e-11, 1e-10, 1e-11),
+    1000: (1e-9, 1e-9, 1e-9, 1e-8, 1e-9),
+}
+
+
+def test_box64_p16_long_run_statistics(require_gpu, oracle_mod):
+    """1000 steps of the 64^3, 16-sphere workload: E(k), dissipation,
+    particle force RMS and mean slip against the oracle at steps 10, 100
+    and 1000."""
+    from oracle import statistics as ost
+    wl = config.box64_p16_f64()
+    o, box = seeded_pair(oracle_mod, wl)
+    c = wl.cfg
+    n = wl.npart
+    r_in, r_out = c.rad + 1.0, c.rad + 3.0
+    done = 0
+    rows = []
+    for cp in sorted(LONG_RUN_TOL):
+        assert o.step(cp - done) == 0
+        box.step(cp - done)
+        done = cp
+        sg = box.statistics()
+        ek_o, dk_o, out_o = ost.spectrum(o.ux, o.uy, o.uz, c.visc)
+        ek_g = sg["ek"]
+        res = ek_o >= 1e-6 * ek_o.max()
+        e_l2 = float(np.linalg.norm(ek_g - ek_o) / np.linalg.norm(ek_o))
+        e_shell = float((np.abs(ek_g - ek_o)[res] / ek_o[res]).max())
+        e_diss = abs(sg["dissipation"] - out_o[2]) / out_o[2]
+        p = box.get_particles()
+        fo = o.fHIp[:n]
+        e_force = float(np.sqrt(((p["fHIp"] - fo) ** 2).sum() / (fo ** 2).sum()))
+        sl_g = box.particle_slip(r_in, r_out)
+        sl_o = ost.particle_slip(o.ux, o.uy, o.uz, o.isnodes, o.ypglb[:n], o.wp[:n], r_in, r_out)
+        m_g = np.linalg.norm(sl_g, axis=1).mean()
+        m_o = np.linalg.norm(sl_o, axis=1).mean()
+        e_slip = abs(m_g - m_o) / m_o
+        e_f = relerr(box.get_f(), o.f)
+        row = (e_l2, e_shell, e_diss, e_force, e_slip)
+        rows.append((cp, row, e_f))
+        print(f"\nbox64_p16 step {cp}: E(k) {e_l2:.2e} shell {e_shell:.2e} diss {e_diss:.2e} "
+              f"force RMS {e_force:.2e} mean slip {e_slip:.2e} populations {e_f:.2e}")
+    for cp, row, _ in rows:
+        for name, e, t in zip(("E(k)", "shell", "dissipation", "force RMS", "mean slip"), row,
+                              LONG_RUN_TOL[cp]):
+            assert e <= t, (cp, name, e, t)
+    box.close()
+    o.close()

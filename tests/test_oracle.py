@@ -39,6 +39,27 @@ def test_ran1_matches_python_restatement(oracle_mod):
         assert got.min() > 0.0 and got.max() < 1.0
 
 
+# Park & Miller, "Random number generators: good ones are hard to find",
+# CACM 31 (1988): the minimal standard x_{k+1} = 16807 x_k mod (2^31 - 1)
+# started from x_0 = 1 has x_10000 = 1043618065.
+PARK_MILLER_X10000 = 1043618065
+
+
+def test_park_miller_known_answer(oracle_mod):
+    """The core of ranff/ranpp (3DBox.../gaussian.f90:385-397) is the minimal
+    standard generator: its state after the shuffle table's 40-step warm-up
+    and 9960 draws is the published 10,000th value from seed 1, in the
+    oracle and in the Python restatement."""
+    assert oracle_mod.ran1_state(1, 9960) == PARK_MILLER_X10000
+    r = inputs.Ran1(1)
+    for _ in range(9960):
+        r()
+    assert r.idum == PARK_MILLER_X10000
+    # and every other state is the closed form 16807^k mod (2^31 - 1)
+    for n in (1, 2, 450, 4500):
+        assert oracle_mod.ran1_state(232300, n) == 232300 * pow(16807, 40 + n, 2**31 - 1) % (2**31 - 1)
+
+
 def test_ran1_golden(oracle_mod):
     g = np.load(__import__("pathlib").Path(__file__).parent / "golden" / "ran1.npz")
     for seed in (232300, 12345):
