@@ -191,11 +191,23 @@ int lbm_step(lbm_ctx* ctx, int nsteps);
 
 /* ---- initial conditions on the device (no counterpart in the reference) --- */
 /* initpop (initial.f90:3-28) from a seeded divergence-free Gaussian velocity
- * field with energy spectrum E(k) ~ k^4 exp(-2 (k/k0)^2), rescaled to a
- * per-component rms u_rms, generated on the GPU (counter-based generator,
- * cuFFT inverse transform): the role of initvel (initial.f90:55-116)
- * without host FFTs.  Same seed, same field. */
+ * field made on the GPU in the steps of initvel (initial.f90:55-116):
+ * Gaussian modes projected off k, the kx = 0 plane Hermitian, the mean, the
+ * Nyquist wavenumbers and the shells beyond nek = int(nx/2 - 1.5) zeroed,
+ * each shell int(|k| + 1/2) = ik scaled to hold exactly ik^4 exp(-2 (ik/k0)^2)
+ * (the workload's spectrum in place of initvel's), inverse FFT (cuFFT), and
+ * one factor on all components so that sqrt(<|u|^2>/3) = u_rms.  initvel
+ * draws from the Intel runtime's rand(), whose sequence is not published,
+ * so the draws come from a counter-based generator instead.  Same seed,
+ * same field. */
 int lbm_init_spectral(lbm_ctx* ctx, double k0, double u_rms, uint64_t seed);
+/* initpop from the channel's initial velocity, initvel of
+ * 3DChannel.../initial.f90:57-126: the log-law mean flow in y between the
+ * walls at x = 0 and x = nx (y+ ustar for y+ < 10.8, else
+ * (ln(y+)/0.41 + 5) ustar; ustar = 360 visc / nx, ystar = visc / ustar),
+ * u = w = 0 (the reference's perturbation amplitude is 0).  Needs a box
+ * with walls (LBM_BC_XWALLS). */
+int lbm_init_channel(lbm_ctx* ctx);
 /* initpartpos (partlib.f90:1-80) with the ranpp generator and seed `seed`,
  * then lbm_upload_particles at rest.  LBM_ERR_OVERLAP if no placement is
  * found in max_rounds rounds (0: 100000). */

@@ -120,6 +120,7 @@ SIGNATURES = {
     "lbm_statistics": (C.c_int, [_P, C.c_int, _D, _D, _D]),
     "lbm_init_spectral": (C.c_int, [_P, C.c_double, C.c_double, C.c_uint64]),
     "lbm_init_particles": (C.c_int, [_P, C.c_int, C.c_int, C.c_int]),
+    "lbm_init_channel": (C.c_int, [_P]),
     "lbm_summary": (C.c_int, [_P, _D]),
     "lbm_particle_slip": (C.c_int, [_P, C.c_double, C.c_double, _D]),
     "lbm_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]),

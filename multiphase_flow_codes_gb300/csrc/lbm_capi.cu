@@ -1138,6 +1138,20 @@ int lbm_init_spectral(lbm_ctx* ctx, double k0, double u_rms, uint64_t seed) {
   return initpop_device(ctx, dv);
 }
 
+int lbm_init_channel(lbm_ctx* ctx) {
+  if (!ctx) return LBM_ERR_ARG;
+  if (!ctx->g.channel) return fail(ctx, LBM_ERR_ARG, "init_channel: the box has no walls");
+  const long long N = ctx->g.N;
+  double* dv = nullptr;
+  CK(cudaMalloc((void**)&dv, 3 * N * sizeof(double)));
+  if (int rc = channel_loglaw_field(ctx->g, ctx->cfg.visc, dv, ctx->stream)) {
+    cudaFree(dv);
+    cudaGetLastError();
+    return fail(ctx, rc, "init_channel: launch failed");
+  }
+  return initpop_device(ctx, dv);
+}
+
 int lbm_init_particles(lbm_ctx* ctx, int npart, int seed, int max_rounds) {
   if (!ctx || npart < 0 || npart > ctx->npmax) return LBM_ERR_ARG;
   std::vector<double> y(3 * (size_t)npart), zero(3 * (size_t)npart, 0.0);

@@ -288,6 +288,7 @@ int spectrum_stats(const Geometry& g, double visc, const T* ux, const T* uy, con
 // per-component rms urms, into u[3][N] (device); synchronises s
 int spectral_field(const Geometry& g, double k0, double urms, uint64_t seed, double* u,
                    cudaStream_t s);
+int channel_loglaw_field(const Geometry& g, double visc, double* u, cudaStream_t s);
 // per-block sums: mass, momentum x/y/z, population checksum, kinetic energy
 template <typename T>
 void launch_summary(const T* f, long long N, const T* ux, const T* uy, const T* uz,

@@ -174,11 +174,15 @@ __device__ __forceinline__ double2 gauss2(uint64_t seed, long long mode, int com
   return make_double2(r * cos(t), r * sin(t));
 }
 
-// Half-spectrum coefficients (kx >= 0) of a divergence-free Gaussian field
-// with E(k) ~ k^4 exp(-2 (k/k0)^2): per mode a complex Gaussian vector,
-// projected off k, scaled by sqrt(E(k) / (4 pi k^2)).  The kx = 0 and
-// kx = nx/2 planes are made Hermitian (a mode and its mirror -k share one
-// draw, conjugated), so the inverse real transform is exact.
+// Half-spectrum coefficients (kx >= 0) of a divergence-free Gaussian field,
+// in the steps of the reference's initvel (3DBox.../initial.f90:55-116):
+// per mode a complex Gaussian vector projected off k (tmp = k.v / k^2,
+// v = v - k tmp), the kx = 0 plane made Hermitian (a mode and its mirror -k
+// share one draw, conjugated; symmetrize, gaussian.f90:80-), the mean and
+// the Nyquist wavenumbers of each axis set to zero (symmetrize), and the
+// modes of shells beyond nek = int(nx/2 - 1.5) set to zero (initial.f90:77-81).
+// The amplitude sqrt(E(k) / (4 pi k^2)) only pre-shapes the draw: the shell
+// energies are set exactly afterwards (k_shell_energy, k_shell_scale).
 __global__ void k_spectral_modes(int nx, int ny, int nz, double k0, uint64_t seed,
                                  double2* __restrict__ vx, double2* __restrict__ vy,
                                  double2* __restrict__ vz) {
@@ -191,7 +195,9 @@ __global__ void k_spectral_modes(int nx, int ny, int nz, double k0, uint64_t see
   int jy = (int)(r % ny), jz = (int)(r / ny);
   int ky = signed_k(jy, ny), kz = signed_k(jz, nz);
   const double k2 = (double)kx * kx + (double)ky * ky + (double)kz * kz;
-  if (k2 == 0.0) {
+  const int nek = (int)(nx / 2 - 1.5);
+  if (k2 == 0.0 || 2 * kx == nx || 2 * jy == ny || 2 * jz == nz ||
+      (int)(sqrt(k2) + 0.5) > nek) {
     vx[t] = vy[t] = vz[t] = make_double2(0.0, 0.0);
     return;
   }
@@ -228,15 +234,99 @@ __global__ void k_spectral_modes(int nx, int ny, int nz, double k0, uint64_t see
   vz[t] = out[2];
 }
 
+// Energy of shell ik = blockIdx.x + 1 (shells int(|k| + 1/2)) over the
+// half spectrum, the kx = 0 plane weighted 1/2 as initvel and statistc count
+// it.  One block per shell scans every mode in a fixed order and reduces with
+// a fixed tree, so the sums are the same bits on every run.
+__global__ void __launch_bounds__(256) k_shell_energy(int nx, int ny, int nz,
+                                                      const double2* __restrict__ vx,
+                                                      const double2* __restrict__ vy,
+                                                      const double2* __restrict__ vz,
+                                                      double* __restrict__ shell_e) {
+  using Red = cub::BlockReduce<double, 256>;
+  __shared__ typename Red::TempStorage tmp;
+  const int ik = blockIdx.x + 1;
+  const int nxc = nx / 2 + 1;
+  const long long total = (long long)nxc * ny * nz;
+  double s = 0.0;
+  for (long long t = threadIdx.x; t < total; t += blockDim.x) {
+    const int kx = (int)(t % nxc);
+    const long long r = t / nxc;
+    const int ky = signed_k((int)(r % ny), ny), kz = signed_k((int)(r / ny), nz);
+    const double k2 = (double)kx * kx + (double)ky * ky + (double)kz * kz;
+    if ((int)(sqrt(k2) + 0.5) != ik) continue;
+    const double2 a = vx[t], b = vy[t], c = vz[t];
+    const double e = a.x * a.x + a.y * a.y + b.x * b.x + b.y * b.y + c.x * c.x + c.y * c.y;
+    s += kx == 0 ? 0.5 * e : e;
+  }
+  const double tot = Red(tmp).Sum(s);
+  if (threadIdx.x == 0) shell_e[ik] = tot;
+}
+
+// Scale every mode of shell ik so that the shell holds ik^4 exp(-2 (ik/k0)^2)
+// (initvel's per-shell rescaling with the workload's spectrum).
+__global__ void k_shell_scale(int nx, int ny, int nz, double k0,
+                              const double* __restrict__ shell_e, double2* __restrict__ vx,
+                              double2* __restrict__ vy, double2* __restrict__ vz) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int nxc = nx / 2 + 1;
+  const long long total = (long long)nxc * ny * nz;
+  if (t >= total) return;
+  const int kx = (int)(t % nxc);
+  const long long r = t / nxc;
+  const int ky = signed_k((int)(r % ny), ny), kz = signed_k((int)(r / ny), nz);
+  const double k2 = (double)kx * kx + (double)ky * ky + (double)kz * kz;
+  const int ik = (int)(sqrt(k2) + 0.5);
+  const int nek = (int)(nx / 2 - 1.5);
+  double f = 0.0;
+  if (ik >= 1 && ik <= nek && shell_e[ik] > 0.0) {
+    const double q = (double)ik / k0;
+    const double target = (double)ik * ik * ik * ik * exp(-2.0 * q * q);
+    f = sqrt(target / shell_e[ik]);
+  }
+  vx[t] = make_double2(vx[t].x * f, vx[t].y * f);
+  vy[t] = make_double2(vy[t].x * f, vy[t].y * f);
+  vz[t] = make_double2(vz[t].x * f, vz[t].y * f);
+}
+
 __global__ void k_square(const double* __restrict__ a, double* __restrict__ b, long long n) {
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t < n) b[t] = a[t] * a[t];
 }
+// The channel's initial velocity, initvel of 3DChannel.../initial.f90:57-126:
+// walls normal to x at x = 0 and x = nx, u = w = 0, and the mean profile
+// v(x) = y+ ustar in the viscous sublayer (y+ < 10.8) and (ln(y+)/0.41 + 5)
+// ustar beyond it, y+ = (i - 1/2) / ystar for the nx/2 nodes nearest each
+// wall (a middle node of an odd nx keeps 0).  The reference's perturbation
+// terms carry the amplitude A9 = 0 and vanish.
+__global__ void k_channel_loglaw(int nx, long long N, double ustar, double ystar,
+                                 double* __restrict__ u) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= N) return;
+  const int i = (int)(t % nx) + 1;  // 1-based wall-normal index
+  const int nxh = nx / 2;
+  const int ii = i <= nxh ? i : nx + 1 - i;
+  double v = 0.0;
+  if (ii <= nxh) {
+    const double yplus = ((double)ii - 0.5) / ystar;
+    if (yplus < 10.8) {
+      v = yplus * ustar;
+    } else {
+      double u9 = log(yplus) / 0.41 + 5.0;
+      v = u9 * ustar;
+    }
+  }
+  u[t] = 0.0;
+  u[N + t] = v;
+  u[2 * N + t] = 0.0;
+}
+
+// u *= urms / sqrt(sum of squares / count): one factor for all components
 __global__ void k_scale(double* __restrict__ a, long long n, const double* __restrict__ sumsq,
-                        double urms) {
+                        double count, double urms) {
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t < n) {
-    const double ms = *sumsq / (double)n;
+    const double ms = *sumsq / count;
     a[t] = ms > 0.0 ? a[t] * (urms / sqrt(ms)) : 0.0;
   }
 }
@@ -281,15 +371,18 @@ int spectral_field(const Geometry& g, double k0, double urms, uint64_t seed, dou
                    cudaStream_t s) {
   const long long N = g.N;
   const long long nc = (long long)(g.nx / 2 + 1) * g.ny * g.nz;
+  const int nek = (int)(g.nx / 2 - 1.5);
   double2* spec = nullptr;
   double* tmp = nullptr;
+  double* shell_e = nullptr;
   void* cub_tmp = nullptr;
   size_t cub_bytes = 0;
   cufftHandle plan = 0;
   int rc = LBM_OK;
-  cub::DeviceReduce::Sum(nullptr, cub_bytes, tmp, tmp, N);
+  cub::DeviceReduce::Sum(nullptr, cub_bytes, tmp, tmp, 3 * N);
   if (cudaMalloc((void**)&spec, 3 * nc * sizeof(double2)) != cudaSuccess ||
-      cudaMalloc((void**)&tmp, (N + 1) * sizeof(double)) != cudaSuccess ||
+      cudaMalloc((void**)&tmp, (3 * N + 1) * sizeof(double)) != cudaSuccess ||
+      cudaMalloc((void**)&shell_e, (nek + 2) * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&cub_tmp, cub_bytes) != cudaSuccess) {
     rc = LBM_ERR_NOMEM;
   } else if (cufftPlan3d(&plan, g.nz, g.ny, g.nx, CUFFT_Z2D) != CUFFT_SUCCESS) {
@@ -300,17 +393,24 @@ int spectral_field(const Geometry& g, double k0, double urms, uint64_t seed, dou
     k_spectral_modes<<<blocks(nc, 256), 256, 0, s>>>(g.nx, g.ny, g.nz, k0, seed, spec,
                                                       spec + nc, spec + 2 * nc);
     count_launch();
-    for (int c = 0; c < 3 && !rc; ++c) {
-      if (cufftExecZ2D(plan, spec + c * nc, u + c * N) != CUFFT_SUCCESS) {
-        rc = LBM_ERR_CUDA;
-        break;
-      }
-      // per-component rms -> urms
-      k_square<<<blocks(N, 256), 256, 0, s>>>(u + c * N, tmp, N);
+    if (nek >= 1) {
+      k_shell_energy<<<nek, 256, 0, s>>>(g.nx, g.ny, g.nz, spec, spec + nc, spec + 2 * nc,
+                                         shell_e);
+      count_launch();
+      k_shell_scale<<<blocks(nc, 256), 256, 0, s>>>(g.nx, g.ny, g.nz, k0, shell_e, spec,
+                                                    spec + nc, spec + 2 * nc);
+      count_launch();
+    }
+    for (int c = 0; c < 3 && !rc; ++c)
+      if (cufftExecZ2D(plan, spec + c * nc, u + c * N) != CUFFT_SUCCESS) rc = LBM_ERR_CUDA;
+    if (!rc) {
+      // one factor for all three components, so the field stays solenoidal:
+      // sqrt(mean |u|^2 / 3) -> urms
+      k_square<<<blocks(3 * N, 256), 256, 0, s>>>(u, tmp, 3 * N);
       count_launch();
       size_t b = cub_bytes;
-      cub::DeviceReduce::Sum(cub_tmp, b, tmp, tmp + N, N, s);
-      k_scale<<<blocks(N, 256), 256, 0, s>>>(u + c * N, N, tmp + N, urms);
+      cub::DeviceReduce::Sum(cub_tmp, b, tmp, tmp + 3 * N, 3 * N, s);
+      k_scale<<<blocks(3 * N, 256), 256, 0, s>>>(u, 3 * N, tmp + 3 * N, (double)(3 * N), urms);
       count_launch();
     }
   }
@@ -318,8 +418,18 @@ int spectral_field(const Geometry& g, double k0, double urms, uint64_t seed, dou
   if (plan) cufftDestroy(plan);
   cudaFree(spec);
   cudaFree(tmp);
+  cudaFree(shell_e);
   cudaFree(cub_tmp);
   return rc;
+}
+
+int channel_loglaw_field(const Geometry& g, double visc, double* u, cudaStream_t s) {
+  const double rstar = 180.0;                       // 3DChannel.../para.f90:14
+  const double ustar = 2.0 * rstar * visc / (double)g.nx;
+  const double ystar = visc / ustar;
+  k_channel_loglaw<<<blocks(g.N, 256), 256, 0, s>>>(g.nx, g.N, ustar, ystar, u);
+  count_launch();
+  return cudaGetLastError() == cudaSuccess ? LBM_OK : LBM_ERR_CUDA;
 }
 
 template <typename T>

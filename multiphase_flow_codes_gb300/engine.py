@@ -143,6 +143,11 @@ class LBMBox:
         self._ck(self._L.lbm_init_spectral(self._h, float(k0), float(u_rms), int(seed)),
                  "init_spectral")
 
+    def init_channel(self):
+        """initpop from the channel's log-law initial velocity (initvel of
+        3DChannel.../initial.f90:57-126)."""
+        self._ck(self._L.lbm_init_channel(self._h), "init_channel")
+
     def init_particles(self, npart: int, seed: int = 12345, max_rounds: int = 0):
         """initpartpos with the ranpp generator, particles at rest."""
         self._ck(self._L.lbm_init_particles(self._h, int(npart), int(seed), int(max_rounds)),

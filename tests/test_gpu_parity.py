@@ -53,14 +53,22 @@ def make_pair(oracle_mod, preset=capi.LBM_PRESET_BOX, shape=(32, 32, 32), npart=
     return o, box
 
 
-def check_links(o, box, tol_alpha=1e-13):
+def check_links(o, box, tol_alpha=None):
     po, no, qo, ao = oracle_links(o)
     pg, ng, qg, ag = gpu_links(box)
     assert len(po) == len(pg), (len(po), len(pg))
     assert np.array_equal(po, pg) and np.array_equal(no, ng) and np.array_equal(qo, qg)
     # the link set is integer work (bit-exact); alpha is FP64 data computed
-    # from the same root in a better-conditioned form
+    # from the same root in a better-conditioned form, whose difference from
+    # the reference's form is the rounding of the node coordinates (up to n)
+    if tol_alpha is None:
+        tol_alpha = alpha_tolerance(o)
     assert np.abs(ao - ag).max() <= tol_alpha, np.abs(ao - ag).max()
+
+
+def alpha_tolerance(o):
+    """Link fractions: 16 ulps of the largest node coordinate."""
+    return 16.0 * np.finfo(np.float64).eps * max(o.nx, o.ny, o.nz)
 
 
 def check_force_torque(o, box, tol=TOL64):
@@ -234,7 +242,8 @@ def test_channel_wall_lubrication(require_gpu, oracle_mod):
         box.step(1)
         check_flags(o, box)
         p = box.get_particles()
-        assert np.all(np.abs(o.flubp[:4]).max(axis=1) > 0), o.flubp[:4]
+        if s == 0:  # every sphere starts inside a lubrication range
+            assert np.all(np.abs(o.flubp[:4]).max(axis=1) > 0), o.flubp[:4]
         e = relerr(p["flubp"], o.flubp[:4])
         worst = max(worst, e)
         assert e <= TOL64, (s, e)
@@ -321,7 +330,8 @@ def test_bounce_cases_near_contact(require_gpu, oracle_mod):
         for k, v in check_force_torque(o, box).items():
             worst[k] = max(worst.get(k, 0.0), v)
         p = box.get_particles()
-        assert np.abs(o.flubp[:2]).max() > 0  # the pair is inside the lubrication range
+        if s == 0:  # the pair starts inside the lubrication range (it is pushed apart)
+            assert np.abs(o.flubp[:2]).max() > 0
         worst["flubp"] = max(worst.get("flubp", 0.0), relerr(p["flubp"], o.flubp[:3]))
         assert relerr(p["flubp"], o.flubp[:3]) <= TOL64
     print(f"\nnear contact, worst over 10 steps: {worst}")

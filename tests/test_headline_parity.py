@@ -23,7 +23,8 @@ Tolerances and why:
                                     links that cancels: its rounding scales with
                                     the terms, not with the result)
   flubp                             1e-12 (max norm; computed from positions)
-  long run, E(k) and dissipation    stated per checkpoint in LONG_RUN_TOL: two FP64
+  link fractions alpha              16 ulps of the largest node coordinate (256)
+  long run, statistics              stated per checkpoint in LONG_RUN_TOL: two FP64
                                     runs that differ only in rounding order drift
                                     apart as the turbulence amplifies the
                                     difference; the bounds hold that drift at the
@@ -104,7 +105,8 @@ def test_box256_p1000_f64_ten_steps(require_gpu, oracle_mod):
         assert len(lo[0]) == len(lg[0]), (s, len(lo[0]), len(lg[0]))
         for a, b in zip(lo[:3], lg[:3]):
             assert np.array_equal(a, b), s
-        assert np.abs(lo[3] - lg[3]).max() <= 1e-13, s
+        worst["alpha"] = max(worst.get("alpha", 0.0), float(np.abs(lo[3] - lg[3]).max()))
+        assert worst["alpha"] <= 16.0 * np.finfo(np.float64).eps * 256, s
         check_particles(o, box, lo, n, worst)
     print("\nbox256_p1000_f64 particle state, worst over 10 steps: "
           + ", ".join(f"{k} {v:.2e}" for k, v in sorted(worst.items())))
@@ -122,11 +124,15 @@ def test_box256_p1000_f64_ten_steps(require_gpu, oracle_mod):
 
 
 # step -> bound on (E(k) relative 2-norm, worst resolved shell, dissipation,
-# force RMS, mean slip); see the module docstring
+# force RMS, mean slip, populations in the max norm).  Measured on GB300:
+#   step 10:   7.7e-16 1.0e-15 6.7e-16 2.5e-15 3.2e-16 2.5e-15
+#   step 100:  6.5e-15 1.3e-14 8.2e-15 7.1e-14 3.8e-15 2.8e-14
+#   step 1000: 1.5e-14 8.2e-14 4.2e-14 1.2e-13 3.5e-15 4.0e-13
+# the bounds are 100x those, rounded up to a power of ten
 LONG_RUN_TOL = {
-    10: (1e-12, 1e-12, 1e-12, 1e-12, 1e-12),
-    100: (1e-11, 1e-11, 1e-11, 1e-10, 1e-11),
-    1000: (1e-9, 1e-9, 1e-9, 1e-8, 1e-9),
+    10: (1e-13, 1e-13, 1e-13, 1e-12, 1e-13, 1e-12),
+    100: (1e-12, 1e-11, 1e-12, 1e-11, 1e-12, 1e-11),
+    1000: (1e-11, 1e-11, 1e-11, 1e-10, 1e-12, 1e-10),
 }
 
 
@@ -166,9 +172,9 @@ def test_box64_p16_long_run_statistics(require_gpu, oracle_mod):
         rows.append((cp, row, e_f))
         print(f"\nbox64_p16 step {cp}: E(k) {e_l2:.2e} shell {e_shell:.2e} diss {e_diss:.2e} "
               f"force RMS {e_force:.2e} mean slip {e_slip:.2e} populations {e_f:.2e}")
-    for cp, row, _ in rows:
-        for name, e, t in zip(("E(k)", "shell", "dissipation", "force RMS", "mean slip"), row,
-                              LONG_RUN_TOL[cp]):
+    for cp, row, e_f in rows:
+        for name, e, t in zip(("E(k)", "shell", "dissipation", "force RMS", "mean slip",
+                               "populations"), row + (e_f,), LONG_RUN_TOL[cp]):
             assert e <= t, (cp, name, e, t)
     box.close()
     o.close()

@@ -5,9 +5,12 @@
   spheres bit for bit where the Python restatement ``inputs.initpartpos``
   and the oracle place them.
 * ``lbm_init_spectral``: the seeded solenoidal Gaussian field behind
-  initpop: the same seed gives the same bits, another seed another field;
-  zero mean, per-component rms u_rms, divergence-free, and the energy in
-  the spectrum's peak shells well above the far tail.
+  initpop, made in initvel's steps (3DBox.../initial.f90:55-116): the same
+  seed gives the same bits, another seed another field; zero mean, rms
+  u_rms, divergence-free, no Nyquist or beyond-nek modes, and every shell's
+  energy exactly on the workload's spectrum k^4 exp(-2 (k/k0)^2).
+* ``lbm_init_channel``: initvel of the channel program (the log-law mean
+  flow, 3DChannel.../initial.f90:57-126) against its numpy restatement.
 """
 
 import numpy as np
@@ -49,11 +52,14 @@ def _field(box):
 
 def test_init_spectral_properties(require_gpu):
     from multiphase_flow_codes_gb300.engine import LBMBox
+    from oracle import statistics as ost
     n, k0, urms = 48, 4.0, 0.03
     cfg = capi.config_init(capi.LBM_PRESET_BOX, n, n, n, 0, 4.0, 2.5)
+    cfg.forcing = capi.LBM_FORCING_NONE  # macrovar's u is then sum c f, no F/2
     box = LBMBox(cfg)
     box.init_spectral(k0, urms, 54321)
     u1 = _field(box)
+    stats = box.statistics()
     box.init_spectral(k0, urms, 54321)
     u2 = _field(box)
     box.init_spectral(k0, urms, 54322)
@@ -61,23 +67,41 @@ def test_init_spectral_properties(require_gpu):
     box.close()
     assert np.array_equal(u1, u2)                      # same seed, same bits
     assert np.abs(u1 - u3).max() > 0.1 * urms          # another seed, another field
-    assert np.abs(u1.mean(axis=(1, 2, 3))).max() <= 1e-13
-    rms = np.sqrt((u1 ** 2).mean(axis=(1, 2, 3)))
-    assert np.abs(rms / urms - 1.0).max() <= 1e-12, rms
-    # divergence in spectral space, relative to |k| |u^|
+    assert np.abs(u1.mean(axis=(1, 2, 3))).max() <= 1e-15
+    rms = np.sqrt((u1 ** 2).sum(axis=0).mean() / 3.0)
+    assert abs(rms / urms - 1.0) <= 1e-12, rms
     uh = np.fft.rfftn(u1, axes=(1, 2, 3))
     kz = np.fft.fftfreq(n, 1.0 / n)[:, None, None]
     ky = np.fft.fftfreq(n, 1.0 / n)[None, :, None]
     kx = np.arange(n // 2 + 1)[None, None, :]
-    ny_ok = (np.abs(kz) < n // 2) & (np.abs(ky) < n // 2) & (kx < n // 2)
-    div = kx * uh[0] + ky * uh[1] + kz * uh[2]
     kk = np.sqrt(kx * kx + ky * ky + kz * kz + 0.0)
-    mag = kk * np.sqrt((np.abs(uh) ** 2).sum(axis=0))
-    assert (np.abs(div)[ny_ok]).max() <= 1e-10 * mag.max()
-    # spectrum shape E(k) ~ k^4 exp(-2 (k/k0)^2): the peak shells (k near k0)
-    # hold far more energy than shells at 3 k0
-    e = (np.abs(uh) ** 2).sum(axis=0)
-    shell = (kk + 0.5).astype(int)
-    ek = np.bincount(shell.ravel(), weights=e.ravel(), minlength=n)
-    assert ek[int(k0)] > 1e3 * ek[int(3 * k0)]
-    assert ek[0] <= 1e-20 * ek.max()
+    amp = np.sqrt((np.abs(uh) ** 2).sum(axis=0))
+    # divergence-free, relative to |k| |u^|
+    div = kx * uh[0] + ky * uh[1] + kz * uh[2]
+    assert np.abs(div).max() <= 1e-12 * (kk * amp).max()
+    # no Nyquist modes and nothing beyond shell nek
+    nek = int(n / 2 - 1.5)
+    nyq = (kx == n // 2) | (np.abs(ky) == n // 2) | (np.abs(kz) == n // 2) | ((kk + 0.5).astype(int) > nek)
+    assert np.broadcast_to(amp, nyq.shape)[nyq].max() <= 1e-12 * amp.max()
+    # every shell on the spectrum: E(ik) / (ik^4 exp(-2 (ik/k0)^2)) is one constant
+    ek, _, _ = ost.spectrum(*u1, cfg.visc)
+    ik = np.arange(1, nek + 1, dtype=np.float64)
+    ratio = ek / (ik ** 4 * np.exp(-2.0 * (ik / k0) ** 2))
+    assert np.abs(ratio / ratio[0] - 1.0).max() <= 1e-10, ratio
+    # and the engine's own statistc agrees with the numpy spectrum
+    assert np.abs(stats["ek"] - ek).max() <= 1e-12 * ek.max()
+
+
+def test_init_channel_loglaw(require_gpu):
+    from multiphase_flow_codes_gb300.engine import LBMBox
+    from oracle import initial
+    for shape in ((64, 24, 16), (45, 20, 12)):
+        cfg = capi.config_init(capi.LBM_PRESET_CHANNEL, *shape, 0, 4.0, 1.0)
+        cfg.forcing = capi.LBM_FORCING_NONE  # macrovar's u is then sum c f, no F/2
+        box = LBMBox(cfg)
+        box.init_channel()
+        u = _field(box)
+        box.close()
+        ref = np.stack(initial.channel_loglaw(*shape, cfg.visc))
+        assert np.abs(u - ref).max() <= 1e-15 * np.abs(ref).max() + 1e-18, shape
+        assert ref[1].max() > 0.0
