@@ -4,10 +4,10 @@ TEST INFRASTRUCTURE ONLY.  The parity tests, ``__graft_entry__.smoke()`` and
 the CPU-baseline leg of ``bench.py`` compare the engine with it; the engine
 never calls it.
 
-Parity unpinned: the reference (Fortran + MPI + FFTW 2) cannot be compiled
-or run in this environment and ships no golden vectors, so this restatement
-is validated by invariants, independent restatements and hand-derived cases
-(see tests/), not against the reference's own output.
+Parity pinned against the reference itself: the reference (Fortran + MPI +
+FFTW 2, no Fortran compiler here) is translated to C++ by ``oracle/fortran``
+and run on one process (``oracle.refrun``); tests/test_reference_pin.py and
+tests/test_reference_golden.py hold this restatement to that run.
 """
 
 from __future__ import annotations
@@ -31,6 +31,13 @@ def build(force: bool = False) -> Path:
     if force or not LIB.exists() or LIB.stat().st_mtime < max(src.stat().st_mtime, hdr.stat().st_mtime):
         subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
     return LIB
+
+
+def build_reference() -> dict:
+    """The reference's own programs, translated and compiled into
+    oracle/_ref/ (where its sources or the generated translation exist)."""
+    from .fortran import build as rbuild
+    return rbuild.build_all()
 
 
 def lib() -> C.CDLL:

@@ -72,7 +72,7 @@ ELEMENTAL = {"abs", "sqrt", "dsqrt", "exp", "dexp", "log", "alog", "dlog", "sin"
              "float", "int", "nint", "mod", "max", "min", "amax1", "amin1", "max0", "min0",
              "dmax1", "dmin1", "sign", "cmplx", "dcmplx", "aimag", "conjg", "floor", "idint",
              "ifix"}
-REDUCTIONS = {"sum", "maxval", "minval"}
+REDUCTIONS = {"sum", "maxval", "minval", "count"}
 OTHER_INTRINSICS = {"cshift", "size", "trim", "mpi_wtime", "lbound", "ubound", "rand", "irand"}
 
 CPP_KEYWORDS = set()
@@ -239,6 +239,8 @@ class Gen:
             return (b, r)
         if n in ("cmplx", "dcmplx", "conjg"):
             return ("complex", r)
+        if n == "count":
+            return ("int", 0)
         if n in REDUCTIONS:
             return (self.etype(args[0])[0], 0)
         if n == "cshift":
@@ -478,17 +480,20 @@ class Gen:
         base, rank = self.etype(arr)
         if rank == 0:
             raise FortranError(f"{self.where}: {n} of a scalar")
+        if n == "count":
+            mask, base = arr, "int"
         ct = CTYPE[base]
         ext = self.extents(arr)
         iv = [f"_r{self.new_tmp()}" for _ in range(rank)]
         init = {"sum": f"{ct}(0)", "maxval": f"-std::numeric_limits<{ct}>::max()",
-                "minval": f"std::numeric_limits<{ct}>::max()"}[n]
+                "minval": f"std::numeric_limits<{ct}>::max()", "count": "0"}[n]
         loops = ""
         for d in reversed(range(rank)):
             loops += f"for (int64_t {iv[d]} = 0; {iv[d]} < {ext[d]}; ++{iv[d]}) "
-        el = self.cexpr(arr, iv)
+        el = self.cexpr(arr, iv) if n != "count" else "1"
         upd = {"sum": f"_s = _s + {el};", "maxval": f"{{ {ct} _v = {el}; if (_v > _s) _s = _v; }}",
-               "minval": f"{{ {ct} _v = {el}; if (_v < _s) _s = _v; }}"}[n]
+               "minval": f"{{ {ct} _v = {el}; if (_v < _s) _s = _v; }}",
+               "count": "_s = _s + 1;"}[n]
         if mask is not None:
             upd = f"if ({self.cexpr(mask, iv)}) {upd}"
         return f"([&]() {{ {ct} _s = {init}; {loops}{{ {upd} }} return _s; }})()"
@@ -868,3 +873,230 @@ class Gen:
                     raise FortranError(f"{st.where}: only assignments inside WHERE")
                 self.where = a.where
                 self.assign(a, ind, mask=m)
+
+    # ------------------------------------------------------------------
+    # program units
+    def bounds_c(self, dims) -> str:
+        bs = []
+        for d in dims:
+            if d in (":", "*"):
+                raise FortranError(f"{self.where}: deferred bounds here")
+            lo, hi = d
+            bs.append(f"{{{self.cexpr(lo) if lo is not None else '1'}, {self.cexpr(hi)}}}")
+        return "{" + ", ".join(bs) + "}"
+
+    def signature(self, u: Unit) -> str:
+        sc = self.scope_of_cached(u)
+        parts = []
+        for a, (k, base) in zip(u.args, self.dummy_kinds(u)):
+            ct = CTYPE[base]
+            if k == "ref":
+                parts.append(f"{ct}& F_{a}")
+            elif k == "ptr":
+                parts.append(f"{ct}* F_{a}_p")
+            else:
+                parts.append(f"frt::Arr<{ct}> F_{a}")
+        if u.kind == "function":
+            ret = CTYPE[sc[u.result].base]
+        else:
+            ret = "void"
+        return f"{ret} F_{u.name}({', '.join(parts)})"
+
+    def emit_unit(self, u: Unit):
+        self.sc = dict(self.scope_of_cached(u))
+        self._implicit_none = u.implicit_none
+        self.implicit_locals = []
+        self.where = f"{u.file}:{u.name}"
+        self.result_c = self.sc[u.result].cname if u.kind == "function" else ""
+        head = len(self.out)
+        self.emit(self.signature(u) + " {", 0)
+        # dummy array views, parameters, locals (in declaration order)
+        body_start = len(self.out)
+        for a, (k, base) in zip(u.args, self.dummy_kinds(u)):
+            if k == "ptr":
+                s = self.sc[a]
+                dims = [d if d != "*" else (None, Num("2147483647", "int")) for d in s.decl.dims]
+                if any(d == ":" for d in dims):
+                    raise FortranError(f"{u.file}: {u.name}: mixed dummy shape")
+                self.emit(f"frt::Arr<{CTYPE[base]}> F_{a} = frt::Arr<{CTYPE[base]}>::view("
+                          f"F_{a}_p, {self.bounds_c(dims)});", 1)
+        for name, d in u.decls.items():
+            s = self.sc.get(name)
+            if s is None or s.kind in ("dummy",):
+                continue
+            ct = CTYPE[d.base]
+            if s.kind == "param":
+                self.emit(f"const {ct} {s.cname} = {self.convert(self.cexpr(d.init), self.etype(d.init)[0], d.base)};", 1)
+            elif s.kind == "result":
+                self.emit(f"{ct} {s.cname} = {ct}();", 1)
+            elif d.dims is None:
+                static = "static " if ("save" in d.attrs or d.init is not None) else ""
+                init = self.cexpr(d.init) if d.init is not None else f"{ct}()"
+                self.emit(f"{static}{ct} {s.cname} = {init};", 1)
+            elif "allocatable" in d.attrs:
+                self.emit(f"frt::Arr<{ct}> {s.cname};", 1)
+            else:
+                static = "static " if "save" in d.attrs else ""
+                self.emit(f"{static}frt::Arr<{ct}> {s.cname}({self.bounds_c(d.dims)});", 1)
+        if u.kind == "function" and self.sc[u.result].kind == "result" and u.result not in u.decls:
+            s = self.sc[u.result]
+            self.emit(f"{CTYPE[s.base]} {s.cname} = {CTYPE[s.base]}();", 1)
+        decl_end = len(self.out)
+        self.stmts(u.body, 1)
+        if u.kind == "function":
+            self.emit(f"return {self.result_c};", 1)
+        self.emit("}", 0)
+        # implicitly typed locals discovered while emitting the body
+        for s in self.implicit_locals:
+            self.out.insert(decl_end, f"  {CTYPE[s.base]} {s.cname} = {CTYPE[s.base]}();")
+
+    def module_code(self, m: Unit, ns_init: str) -> tuple:
+        """(globals, init function body) of a module."""
+        self.sc = {}
+        for name, d in m.decls.items():
+            kind = "mparam" if "parameter" in d.attrs else "module"
+            self.sc[name] = Sym(d, kind, f"F_{name}")
+        self._implicit_none = True
+        self.implicit_locals = []
+        glob, init = [], []
+        for name, d in m.decls.items():
+            ct = CTYPE[d.base]
+            self.where = d.where
+            if d.dims is None:
+                glob.append(f"{ct} F_{name} = {ct}();")
+                if "parameter" in d.attrs:
+                    v = self.convert(self.cexpr(d.init), self.etype(d.init)[0], d.base)
+                    if d.base in ("int", "int8", "real"):
+                        init.append(f'F_{name} = frt::param<{ct}>("{name}", {v});')
+                    else:
+                        init.append(f"F_{name} = {v};")
+                elif d.init is not None:
+                    init.append(f"F_{name} = {self.cexpr(d.init)};")
+            else:
+                glob.append(f"frt::Arr<{ct}> F_{name};")
+                if "allocatable" not in d.attrs:
+                    init.append(f"F_{name}.allocate({self.bounds_c(d.dims)});")
+                else:
+                    init.append(f"F_{name}.deallocate();")
+        return glob, init
+
+    def reachable(self, roots) -> list:
+        seen, order, stack = set(), [], list(roots)
+
+        def calls_in(body, acc):
+            for st in body:
+                if isinstance(st, Call):
+                    acc.add(st.name)
+                for attr in ("body",):
+                    if hasattr(st, attr) and isinstance(getattr(st, attr), list):
+                        calls_in(getattr(st, attr), acc)
+                if isinstance(st, If):
+                    for _, b in st.branches:
+                        calls_in(b, acc)
+                if isinstance(st, Select):
+                    for _, b in st.cases:
+                        calls_in(b, acc)
+                if isinstance(st, Where):
+                    for _, b in st.branches:
+                        calls_in(b, acc)
+                for e in self._exprs_of(st):
+                    for n in self.names_in(e):
+                        if n in self.units and self.units[n].kind == "function":
+                            acc.add(n)
+        while stack:
+            n = stack.pop()
+            if n in seen or n not in self.units:
+                continue
+            seen.add(n)
+            order.append(n)
+            acc = set()
+            calls_in(self.units[n].body, acc)
+            stack.extend(sorted(acc))
+        return order
+
+    @staticmethod
+    def _exprs_of(st):
+        if isinstance(st, Assign):
+            return [st.lhs, st.rhs]
+        if isinstance(st, Call):
+            return [a.value if isinstance(a, Kw) else a for a in st.args]
+        if isinstance(st, If):
+            return [c for c, _ in st.branches if c is not None]
+        if isinstance(st, Do):
+            return [x for x in (st.lo, st.hi, st.step) if x is not None]
+        if isinstance(st, DoWhile):
+            return [st.cond] if st.cond is not None else []
+        if isinstance(st, Where):
+            return [c for c, _ in st.branches if c is not None]
+        return []
+
+    def generate(self, roots, header="frt.h") -> str:
+        names = self.reachable(roots)
+        missing = [r for r in roots if r not in self.units]
+        if missing:
+            raise FortranError(f"roots not found: {missing}")
+        ns = self.program
+        self.out = []
+        self.called = set()
+        glob_all, init_all = [], []
+        for mname, m in self.modules.items():
+            g, i = self.module_code(m, mname)
+            glob_all += g
+            init_all += i
+        # procedures
+        protos = [self.signature(self.units[n]) + ";" for n in names]
+        bodies_start = len(self.out)
+        for n in names:
+            self.emit_unit(self.units[n])
+            self.emit("", 0)
+        bodies = self.out[bodies_start:]
+        src = [f"// Generated from the reference's Fortran by oracle/fortran (test infrastructure).",
+               f'#include "{header}"', "#include <limits>", "#include <algorithm>", "",
+               f"namespace {ns} {{", ""]
+        src += glob_all + [""]
+        src += ["void init_modules() {"] + ["  " + x for x in init_all] + ["}", ""]
+        src += protos + [""] + bodies
+        # variable table and entry points
+        src += ["struct VarEntry { const char* name; int type; void* addr; int is_array; };",
+                "static VarEntry vars[] = {"]
+        tcode = {"int": 0, "int8": 1, "real": 2, "complex": 3, "logical": 4, "char": 5}
+        for m in self.modules.values():
+            for name, d in m.decls.items():
+                src.append(f'  {{"{name}", {tcode[d.base]}, (void*)&F_{name}, {1 if d.dims else 0}}},')
+        src += ["  {nullptr, 0, nullptr, 0}};", ""]
+        noarg = [n for n in names if self.units[n].kind == "subroutine" and not self.units[n].args]
+        src += ["static std::string last_error;",
+                "}  // namespace " + ns, "",
+                'extern "C" {',
+                f"const char* {ns}_error() {{ return {ns}::last_error.c_str(); }}",
+                f"void {ns}_override(const char* name, double v) {{ frt::overrides()[name] = v; }}",
+                f"void {ns}_clear_overrides() {{ frt::overrides().clear(); }}",
+                f"int {ns}_init() {{ try {{ {ns}::init_modules(); }} catch (std::exception& e) "
+                f"{{ {ns}::last_error = e.what(); return -1; }} return 0; }}",
+                f"int {ns}_call(const char* name) {{",
+                "  try {"]
+        for n in noarg:
+            src.append(f'    if (std::string(name) == "{n}") {{ {ns}::F_{n}(); return 0; }}')
+        src += [f'    {ns}::last_error = std::string("no such subroutine: ") + name; return -2;',
+                f"  }} catch (std::exception& e) {{ {ns}::last_error = e.what(); return -1; }}",
+                "}",
+                f"int {ns}_var(const char* name, int* type, int* rank, int64_t* lb, int64_t* ub, void** data) {{",
+                f"  for ({ns}::VarEntry* v = {ns}::vars; v->name; ++v) {{",
+                "    if (std::string(name) != v->name) continue;",
+                "    *type = v->type;",
+                "    if (!v->is_array) { *rank = 0; *data = v->addr; return 0; }",
+                "    void* d = nullptr; int r = 0;",
+                "    switch (v->type) {",
+                "      case 0: { auto* a = (frt::Arr<int32_t>*)v->addr; r = a->rank; d = a->p; for (int k = 0; k < r; ++k) { lb[k] = a->lb[k]; ub[k] = a->ub[k]; } break; }",
+                "      case 1: { auto* a = (frt::Arr<int64_t>*)v->addr; r = a->rank; d = a->p; for (int k = 0; k < r; ++k) { lb[k] = a->lb[k]; ub[k] = a->ub[k]; } break; }",
+                "      case 2: { auto* a = (frt::Arr<double>*)v->addr; r = a->rank; d = a->p; for (int k = 0; k < r; ++k) { lb[k] = a->lb[k]; ub[k] = a->ub[k]; } break; }",
+                "      case 3: { auto* a = (frt::Arr<frt::cplx>*)v->addr; r = a->rank; d = a->p; for (int k = 0; k < r; ++k) { lb[k] = a->lb[k]; ub[k] = a->ub[k]; } break; }",
+                "      case 4: { auto* a = (frt::Arr<bool>*)v->addr; r = a->rank; d = a->p; for (int k = 0; k < r; ++k) { lb[k] = a->lb[k]; ub[k] = a->ub[k]; } break; }",
+                "      default: return -1;",
+                "    }",
+                "    *rank = r; *data = d; return d ? 0 : -3;",
+                "  }",
+                "  return -2;",
+                "}",
+                '}  // extern "C"', ""]
+        return "\n".join(src)

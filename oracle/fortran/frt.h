@@ -144,14 +144,14 @@ template <class A, class B>
 inline auto fmax2(A a, B b) -> decltype(a + b) { return a > b ? a : b; }
 template <class A, class B>
 inline auto fmin2(A a, B b) -> decltype(a + b) { return a < b ? a : b; }
-template <class A, class B, class... R>
-inline auto fmaxn(A a, B b, R... r) { return fmaxn(fmax2(a, b), r...); }
 template <class A>
 inline A fmaxn(A a) { return a; }
-template <class A, class B, class... R>
-inline auto fminn(A a, B b, R... r) { return fminn(fmin2(a, b), r...); }
 template <class A>
 inline A fminn(A a) { return a; }
+template <class A, class B, class... R>
+inline auto fmaxn(A a, B b, R... r) { return fmaxn(fmax2(a, b), r...); }
+template <class A, class B, class... R>
+inline auto fminn(A a, B b, R... r) { return fminn(fmin2(a, b), r...); }
 inline int32_t ipow(int32_t b, int32_t e) {
   int32_t r = 1;
   for (int32_t i = 0; i < e; ++i) r *= b;

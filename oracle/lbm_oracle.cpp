@@ -3,11 +3,14 @@
 // parity tests, the smoke check and the CPU-baseline leg of bench.py compare
 // the engine with it.  Nothing in the product library links or calls this file.
 //
-// Parity status: the reference is Fortran 90 + MPI + FFTW 2 and cannot be
-// compiled in this environment (no Fortran compiler, no MPI), and it ships
-// no tests or golden vectors.  This restatement is therefore "parity
-// unpinned" against the reference's own run; it is pinned instead against
-// invariants, independent restatements and hand-derived cases (tests/).
+// Parity status: pinned against the reference's own run.  The reference is
+// Fortran 90 + MPI + FFTW 2 with no Fortran compiler on either machine, so
+// its hot-path sources are translated to C++ by oracle/fortran and run on one
+// process (oracle/refrun.py); tests/test_reference_pin.py holds this
+// restatement to that run (the channel program bit for bit, the box program
+// bit for bit up to its FFT-synthesised stochastic force, 1e-13), and
+// tests/test_reference_golden.py to fixtures recorded from it.  The
+// reference ships no tests or golden vectors of its own.
 //
 // Each routine follows one reference subroutine line by line, for a single
 // periodic domain: the MPI halo exchanges become periodic index wraps and the

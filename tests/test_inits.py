@@ -87,7 +87,9 @@ def test_init_spectral_properties(require_gpu):
     ek, _, _ = ost.spectrum(*u1, cfg.visc)
     ik = np.arange(1, nek + 1, dtype=np.float64)
     ratio = ek / (ik ** 4 * np.exp(-2.0 * (ik / k0) ** 2))
-    assert np.abs(ratio / ratio[0] - 1.0).max() <= 1e-10, ratio
+    resolved = ek >= 1e-6 * ek.max()  # shells far below the peak carry FFT rounding
+    assert resolved.sum() >= 8
+    assert np.abs(ratio[resolved] / ratio[0] - 1.0).max() <= 1e-10, ratio
     # and the engine's own statistc agrees with the numpy spectrum
     assert np.abs(stats["ek"] - ek).max() <= 1e-12 * ek.max()
 
