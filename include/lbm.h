@@ -102,6 +102,9 @@ int lbm_config_init(lbm_config* cfg, int preset, int nx, int ny, int nz,
 typedef struct lbm_ctx lbm_ctx;
 
 int lbm_create(const lbm_config* cfg, lbm_ctx** out);  /* allocates all device state */
+/* The configuration a context was created with, and its particle count. */
+int lbm_get_config(const lbm_ctx* ctx, lbm_config* cfg);
+int lbm_particle_count(const lbm_ctx* ctx, int* npart);
 int lbm_destroy(lbm_ctx* ctx);
 const char* lbm_last_error(const lbm_ctx* ctx);         /* never NULL */
 int lbm_version(void);                                  /* ABI version (1) */
@@ -364,6 +367,9 @@ typedef struct lbm_request {
   int32_t nsteps;
   int32_t precision;
   int32_t mrt_type;      /* 0: the preset's MRT rates; 1..3: MRTtype of para.f90 */
+  int32_t keep_state;    /* 1: keep the finished solve's context for
+                            lbm_server_take instead of destroying it       */
+  int32_t reserved;
   double rad, rhopart;
   double k0, u_rms;
   uint64_t seed;
@@ -389,7 +395,15 @@ int lbm_server_wait(lbm_server* server, int64_t id, double timeout_s);
  * batch regroupings, chunks advanced, seconds spent advancing, seconds since
  * creation */
 int lbm_server_stats(lbm_server* server, double* out);
-/* stop the loop; resident solves end as LBM_REQ_FAILED (LBM_ERR_STATE) */
+/* The context of a finished request submitted with keep_state = 1: its
+ * final populations, flags and particles, in the engine's axes (walls normal
+ * to x; lbm_get_config gives the relabelled grid).  The caller owns it from
+ * here and destroys it with lbm_destroy; until it is taken it stays resident
+ * and counts against the server's HBM budget.  LBM_ERR_STATE if the request
+ * is not done or kept nothing. */
+int lbm_server_take(lbm_server* server, int64_t id, lbm_ctx** out);
+/* stop the loop; resident solves end as LBM_REQ_FAILED (LBM_ERR_STATE);
+ * kept contexts not taken are destroyed */
 int lbm_server_destroy(lbm_server* server);
 
 /* ---- diagnostics --------------------------------------------------------- */

@@ -141,6 +141,9 @@ SIGNATURES = {
     "lbm_server_wait": (C.c_int, [_P, C.c_int64, C.c_double]),
     "lbm_server_stats": (C.c_int, [_P, _D]),
     "lbm_server_destroy": (C.c_int, [_P]),
+    "lbm_server_take": (C.c_int, [_P, C.c_int64, C.POINTER(C.c_void_p)]),
+    "lbm_get_config": (C.c_int, [_P, C.POINTER(lbm_config)]),
+    "lbm_particle_count": (C.c_int, [_P, C.POINTER(C.c_int)]),
 }
 
 PHASES = ("stream_collide", "bounce", "particles", "links", "filling", "forcing")

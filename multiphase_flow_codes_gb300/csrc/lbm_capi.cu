@@ -637,11 +637,27 @@ uint64_t footprint(const lbm_config& c, int64_t* cap_out) {
   return b;
 }
 
+// Device address of a host buffer the GPU can read and write directly:
+// page-locked memory (cudaHostAlloc, cudaHostRegister).  Pageable memory
+// gives nullptr and takes the staged path.
+const void* mapped_host(const void* h) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 template <typename T>
 int upload_soa_t(lbm_ctx* ctx, const double* h, bool aos) {
   const long long N = ctx->g.N;
   T* f = fbuf<T>(ctx, ctx->cur);
-  if (aos) {
+  const double* hm = aos ? static_cast<const double*>(mapped_host(h)) : nullptr;
+  if (hm) {
+    // one pass over the link: the kernel reads the host array in place
+    launch_aos_host_to_soa<T>(hm, f, N, sm_count(), ctx->stream);
+  } else if (aos) {
     long long chunk = kStagingDoubles / 19;
     for (long long n0 = 0; n0 < N; n0 += chunk) {
       long long nn = std::min(chunk, N - n0);
@@ -669,7 +685,10 @@ template <typename T>
 int download_soa_t(lbm_ctx* ctx, double* h, bool aos) {
   const long long N = ctx->g.N;
   T* f = fbuf<T>(ctx, ctx->cur);
-  if (aos) {
+  double* hm = aos ? static_cast<double*>(const_cast<void*>(mapped_host(h))) : nullptr;
+  if (hm) {
+    launch_soa_to_aos_host<T>(f, hm, N, sm_count(), ctx->stream);
+  } else if (aos) {
     long long chunk = kStagingDoubles / 19;
     for (long long n0 = 0; n0 < N; n0 += chunk) {
       long long nn = std::min(chunk, N - n0);
@@ -769,6 +788,18 @@ int lbm_config_init(lbm_config* cfg, int preset, int nx, int ny, int nz, int npa
   } else {
     return LBM_ERR_ARG;
   }
+  return LBM_OK;
+}
+
+int lbm_get_config(const lbm_ctx* ctx, lbm_config* cfg) {
+  if (!ctx || !cfg) return LBM_ERR_ARG;
+  *cfg = ctx->cfg;
+  return LBM_OK;
+}
+
+int lbm_particle_count(const lbm_ctx* ctx, int* npart) {
+  if (!ctx || !npart) return LBM_ERR_ARG;
+  *npart = ctx->npart;
   return LBM_OK;
 }
 

@@ -568,6 +568,68 @@ __global__ void k_soa_to_aos(Geometry g, const T* __restrict__ soa, double* __re
   int q = (int)(t - nl * NPOP);
   aos[t] = (double)soa[q * g.N + node0 + nl];
 }
+// Host transfers of the reference-layout populations f(0:18, x, y, z) that
+// read or write page-locked host memory directly over the CPU-GPU link (no
+// staging copy): a block moves tiles of kXTile nodes, the AoS side as one
+// contiguous run with 16-byte accesses, transposed in shared memory, the SoA
+// side as coalesced rows.
+constexpr int kXTile = 256;
+template <typename T>
+__global__ void __launch_bounds__(256) k_aos_host_to_soa(const double* __restrict__ aos,
+                                                         T* __restrict__ soa, long long N) {
+  extern __shared__ double tile[];
+  const long long ntiles = (N + kXTile - 1) / kXTile;
+  for (long long ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
+    const long long a0 = ti * kXTile;
+    const int nn = (int)min((long long)kXTile, N - a0);
+    const double* src = aos + a0 * NPOP;
+    const int total = nn * NPOP;
+    if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+      const double2* s2 = reinterpret_cast<const double2*>(src);
+      for (int i = threadIdx.x; i < (total >> 1); i += blockDim.x) {
+        const double2 v = s2[i];
+        tile[2 * i] = v.x;
+        tile[2 * i + 1] = v.y;
+      }
+      if ((total & 1) && threadIdx.x == 0) tile[total - 1] = src[total - 1];
+    } else {
+      for (int i = threadIdx.x; i < total; i += blockDim.x) tile[i] = src[i];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < total; i += blockDim.x) {
+      const int q = i / nn, n = i - q * nn;
+      soa[(long long)q * N + a0 + n] = T(tile[n * NPOP + q]);
+    }
+    __syncthreads();
+  }
+}
+template <typename T>
+__global__ void __launch_bounds__(256) k_soa_to_aos_host(const T* __restrict__ soa,
+                                                         double* __restrict__ aos, long long N) {
+  extern __shared__ double tile[];
+  const long long ntiles = (N + kXTile - 1) / kXTile;
+  for (long long ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
+    const long long a0 = ti * kXTile;
+    const int nn = (int)min((long long)kXTile, N - a0);
+    double* dst = aos + a0 * NPOP;
+    const int total = nn * NPOP;
+    for (int i = threadIdx.x; i < total; i += blockDim.x) {
+      const int q = i / nn, n = i - q * nn;
+      tile[n * NPOP + q] = (double)soa[(long long)q * N + a0 + n];
+    }
+    __syncthreads();
+    if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+      double2* d2 = reinterpret_cast<double2*>(dst);
+      for (int i = threadIdx.x; i < (total >> 1); i += blockDim.x)
+        d2[i] = make_double2(tile[2 * i], tile[2 * i + 1]);
+      if ((total & 1) && threadIdx.x == 0) dst[total - 1] = tile[total - 1];
+    } else {
+      for (int i = threadIdx.x; i < total; i += blockDim.x) dst[i] = tile[i];
+    }
+    __syncthreads();
+  }
+}
+
 template <typename T>
 __global__ void k_convert(const double* __restrict__ in, T* __restrict__ out, long long n) {
   long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -819,6 +881,22 @@ void launch_soa_to_aos(const Geometry& g, const T* soa, double* aos, long long n
   { k_soa_to_aos<T><<<blocks_for(nnodes * NPOP, 256), 256, 0, s>>>(g, soa, aos, node0, nnodes); count_launch(); }
 }
 template <typename T>
+void launch_aos_host_to_soa(const double* aos_mapped, T* soa, long long N, int sms,
+                            cudaStream_t s) {
+  const size_t smem = (size_t)kXTile * NPOP * sizeof(double);
+  const long long ntiles = (N + kXTile - 1) / kXTile;
+  const unsigned grid = (unsigned)std::min<long long>(ntiles, 5LL * sms);
+  { k_aos_host_to_soa<T><<<grid, 256, smem, s>>>(aos_mapped, soa, N); count_launch(); }
+}
+template <typename T>
+void launch_soa_to_aos_host(const T* soa, double* aos_mapped, long long N, int sms,
+                            cudaStream_t s) {
+  const size_t smem = (size_t)kXTile * NPOP * sizeof(double);
+  const long long ntiles = (N + kXTile - 1) / kXTile;
+  const unsigned grid = (unsigned)std::min<long long>(ntiles, 5LL * sms);
+  { k_soa_to_aos_host<T><<<grid, 256, smem, s>>>(soa, aos_mapped, N); count_launch(); }
+}
+template <typename T>
 void launch_convert(const double* in, T* out, long long n, cudaStream_t s) {
   { k_convert<T><<<blocks_for(n, 256), 256, 0, s>>>(in, out, n); count_launch(); }
 }
@@ -894,6 +972,8 @@ void launch_forcing_tables(const Geometry& g, const ForcingDev* st, const T* ytw
                                      long long, cudaStream_t);                              \
   template void launch_soa_to_aos<T>(const Geometry&, const T*, double*, long long,         \
                                      long long, cudaStream_t);                              \
+  template void launch_aos_host_to_soa<T>(const double*, T*, long long, int, cudaStream_t);  \
+  template void launch_soa_to_aos_host<T>(const T*, double*, long long, int, cudaStream_t);  \
   template void launch_convert<T>(const double*, T*, long long, cudaStream_t);              \
   template void launch_convert_back<T>(const T*, double*, long long, cudaStream_t);         \
   template void launch_force_field<T>(const Geometry&, const ForceView<T>&, double*,        \

@@ -228,6 +228,17 @@ void launch_aos_to_soa(const Geometry& g, const double* aos, T* soa, long long n
 template <typename T>
 void launch_soa_to_aos(const Geometry& g, const T* soa, double* aos, long long node0,
                        long long nnodes, cudaStream_t s);
+// SMs of the current device (queried once)
+int sm_count();
+
+// direct transfers between page-locked host memory (reference layout) and
+// the SoA populations; `sms`: the device's SM count
+template <typename T>
+void launch_aos_host_to_soa(const double* aos_mapped, T* soa, long long N, int sms,
+                            cudaStream_t s);
+template <typename T>
+void launch_soa_to_aos_host(const T* soa, double* aos_mapped, long long N, int sms,
+                            cudaStream_t s);
 template <typename T>
 void launch_convert(const double* in, T* out, long long n, cudaStream_t s);
 template <typename T>

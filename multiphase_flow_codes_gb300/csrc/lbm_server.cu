@@ -55,6 +55,7 @@ struct Job {
   int remaining = 0;
   bool batchable = false;
   int internal_axis[3] = {0, 1, 2};  // external axis of internal x, y, z
+  lbm_ctx* kept = nullptr;           // finished context held for lbm_server_take
 };
 
 }  // namespace
@@ -112,10 +113,14 @@ void finish(lbm_server* s, Job* j, int err) {
       j->res.summary[5] = out[5];
     }
   }
-  lbm_destroy(j->ctx);
+  const bool keep = err == LBM_OK && j->req.keep_state;
+  if (keep)
+    j->kept = j->ctx;  // stays resident (and counted) until taken
+  else
+    lbm_destroy(j->ctx);
   j->ctx = nullptr;
   std::lock_guard<std::mutex> lk(s->mu);
-  s->used -= j->bytes;
+  if (!keep) s->used -= j->bytes;
   j->res.t_done = now_s(s);
   j->res.state = err == LBM_OK ? LBM_REQ_DONE : LBM_REQ_FAILED;
   j->res.error = err;
@@ -400,6 +405,21 @@ int lbm_server_stats(lbm_server* s, double* out) {
   return LBM_OK;
 }
 
+int lbm_server_take(lbm_server* s, int64_t id, lbm_ctx** out) {
+  if (!s || !out) return LBM_ERR_ARG;
+  *out = nullptr;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->jobs.find(id);
+  if (it == s->jobs.end()) return LBM_ERR_ARG;
+  Job* j = it->second.get();
+  if (j->res.state != LBM_REQ_DONE || !j->kept) return LBM_ERR_STATE;
+  *out = j->kept;
+  j->kept = nullptr;
+  s->used -= j->bytes;
+  s->cv_work.notify_all();
+  return LBM_OK;
+}
+
 int lbm_server_destroy(lbm_server* s) {
   if (!s) return LBM_OK;
   {
@@ -408,6 +428,8 @@ int lbm_server_destroy(lbm_server* s) {
     s->cv_work.notify_all();
   }
   if (s->loop.joinable()) s->loop.join();
+  for (auto& kv : s->jobs)
+    if (kv.second->kept) lbm_destroy(kv.second->kept);
   delete s;
   return LBM_OK;
 }

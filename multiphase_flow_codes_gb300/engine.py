@@ -43,6 +43,25 @@ class LBMBox:
         self._h = h
         self.npart = 0
 
+    @classmethod
+    def adopt(cls, handle) -> "LBMBox":
+        """An LBMBox around an existing context (e.g. one taken from the
+        server), which it now owns."""
+        box = cls.__new__(cls)
+        box._L = capi.lib()
+        cfg = capi.lbm_config()
+        rc = box._L.lbm_get_config(handle, C.byref(cfg))
+        if rc != capi.LBM_OK:
+            raise LBMError(rc, "lbm_get_config")
+        n = C.c_int(0)
+        box._L.lbm_particle_count(handle, C.byref(n))
+        box.cfg = cfg
+        box.nx, box.ny, box.nz = cfg.nx, cfg.ny, cfg.nz
+        box.N = box.nx * box.ny * box.nz
+        box._h = handle
+        box.npart = int(n.value)
+        return box
+
     # ---- lifetime ------------------------------------------------------
     def close(self):
         if getattr(self, "_h", None):

@@ -23,7 +23,11 @@ so it differs from the first only by FP64 rounding.  Whatever grows between
 those two is the turbulence amplifying rounding differences, not FP32; an
 FP32 error far above the floor is FP32's own.  The population difference
 is also split into nodes whose solid flags agree in both runs and nodes
-where a sphere covers a node in one run and not in the other.
+where a sphere covers a node in one run and not in the other, and
+``storage_rounding`` measures what rounding the stored populations to FP32
+does by itself to one FP64 step (the force sum over a sphere's links
+cancels to about 1 % of its terms, so the populations' FP32 rounding shows
+in the force amplified about 100 times).
 """
 
 from __future__ import annotations
@@ -77,6 +81,39 @@ def population_split(b_test: LBMBox, b_ref: LBMBox) -> dict:
             "nodes_flags_differ": int((~agree).sum())}
 
 
+def storage_rounding(cfg64: capi.lbm_config, box64: LBMBox, steps: int = 1) -> dict:
+    """The part of the FP32 error that FP32 storage alone causes: two FP64
+    copies of `box64`'s current state, one with its populations rounded to
+    single precision, stepped `steps` steps in FP64 and compared (particle
+    force RMS, populations).  Both copies are set up the same way (state,
+    particle vectors, forcing generator), so their difference is the
+    rounding of the stored populations and nothing else."""
+    f = box64.get_f()
+    part = box64.get_particle_state()
+    first = part.pop("first_move")
+    forcing = box64.get_forcing_state()
+    copies = []
+    try:
+        for rounded in (False, True):
+            b = LBMBox(cfg64)
+            copies.append(b)
+            b.set_f(f.astype(np.float32).astype(np.float64) if rounded else f)
+            b.macrovar()
+            if box64.npart:
+                b.set_particle_state(part, first)
+            b.set_forcing_state(*forcing)
+            b.step(steps)
+        pa, pb = (b.get_particles() for b in copies)
+        out = {"steps": steps, "pop_rel": float(np.abs(copies[1].get_f() - copies[0].get_f()).max()
+                                                / np.abs(f).max())}
+        if box64.npart:
+            out["force_rms_rel"] = _rel(pb["fHIp"], pa["fHIp"])
+        return out
+    finally:
+        for b in copies:
+            b.close()
+
+
 def error_report(cfg64: capi.lbm_config, u, ypglb: np.ndarray,
                  checkpoints=(10, 100, 2000), stream_ptr: int | None = None,
                  floor: bool = True, split_at=(10,)) -> list:
@@ -118,6 +155,7 @@ def error_report(cfg64: capi.lbm_config, u, ypglb: np.ndarray,
             row.update(compare(stats[1], stats[0], parts[1], parts[0], slips[1], slips[0]))
             if cp in split_at:
                 row.update(population_split(boxes[1], boxes[0]))
+                row["fp32_storage_only"] = storage_rounding(cfg64, boxes[0])
             if floor:
                 fl = compare(stats[2], stats[0], parts[2], parts[0], slips[2], slips[0])
                 if cp in split_at:

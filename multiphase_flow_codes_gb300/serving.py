@@ -36,6 +36,7 @@ class lbm_request(C.Structure):
     _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
                 ("wall_axis", C.c_int32), ("npart", C.c_int32), ("nsteps", C.c_int32),
                 ("precision", C.c_int32), ("mrt_type", C.c_int32),
+                ("keep_state", C.c_int32), ("reserved", C.c_int32),
                 ("rad", C.c_double), ("rhopart", C.c_double), ("k0", C.c_double),
                 ("u_rms", C.c_double), ("seed", C.c_uint64)]
 
@@ -51,9 +52,10 @@ REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 
 
 def request(nx, ny, nz, nsteps, wall_axis=1, npart=0, rad=4.0, rhopart=1.0, k0=4.0,
-            u_rms=0.03, seed=1, precision=capi.LBM_PREC_F32, mrt_type=0) -> lbm_request:
-    return lbm_request(nx, ny, nz, wall_axis, npart, nsteps, precision, mrt_type, rad, rhopart,
-                       k0, u_rms, seed)
+            u_rms=0.03, seed=1, precision=capi.LBM_PREC_F32, mrt_type=0,
+            keep_state=False) -> lbm_request:
+    return lbm_request(nx, ny, nz, wall_axis, npart, nsteps, precision, mrt_type,
+                       int(bool(keep_state)), 0, rad, rhopart, k0, u_rms, seed)
 
 
 class LBMServer:
@@ -102,6 +104,16 @@ class LBMServer:
         if rc != capi.LBM_OK:
             raise LBMError(rc, f"lbm_server_wait({rid})")
         return self.result(rid)
+
+    def take(self, rid: int):
+        """The finished solve of a request submitted with keep_state, as an
+        LBMBox (engine axes: walls normal to x) that the caller now owns."""
+        from .engine import LBMBox
+        h = C.c_void_p()
+        rc = self._L.lbm_server_take(self._h, C.c_int64(rid), C.byref(h))
+        if rc != capi.LBM_OK:
+            raise LBMError(rc, f"lbm_server_take({rid})")
+        return LBMBox.adopt(h)
 
     def stats(self) -> dict:
         out = (C.c_double * 10)()

@@ -271,6 +271,29 @@ def test_fortran_layout_roundtrip(require_gpu, oracle_mod):
     assert np.array_equal(box.get_f(), o.f * 0.5)
 
 
+@pytest.mark.parametrize("precision", [capi.LBM_PREC_F64, capi.LBM_PREC_F32])
+def test_fortran_layout_page_locked(require_gpu, oracle_mod, precision):
+    """Upload and download of the reference-layout populations from
+    page-locked host memory (read and written by the GPU in place) give the
+    same bits as the staged path from pageable memory."""
+    import torch
+    from multiphase_flow_codes_gb300._capi import dptr
+    o, box = make_pair(oracle_mod, shape=(40, 20, 12), precision=precision)
+    ff = box.get_f_fortran()                       # pageable: staged path
+    n = ff.size
+    pin = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+    hp = np.ndarray(ff.shape, dtype=np.float64, buffer=pin, order="F")
+    box._ck(box._L.lbm_download_f(box.handle, dptr(hp)), "download_f")
+    assert np.array_equal(hp, ff)
+    rng = np.random.default_rng(5)
+    hp[...] = ff * (1.0 + 1e-3 * rng.standard_normal(ff.shape))
+    box._ck(box._L.lbm_upload_f(box.handle, dptr(hp)), "upload_f")
+    back = box.get_f_fortran()
+    ref = hp.astype(np.float32).astype(np.float64) if precision == capi.LBM_PREC_F32 else hp
+    assert np.array_equal(back, ref)
+    box.close()
+
+
 def test_mass_momentum(require_gpu, oracle_mod):
     o, box = make_pair(oracle_mod, shape=(16, 16, 16))
     box.step(3)

@@ -61,3 +61,49 @@ def test_oversized_request_rejected(require_gpu):
     with serving.LBMServer(1 << 20, 4, 8) as srv:
         with pytest.raises(capi.LBMError):
             srv.submit(serving.request(64, 64, 64, 10))
+
+
+def test_served_fields_match_standalone_and_oracle(require_gpu, oracle_mod):
+    """A request served in a mix, its context kept and taken afterwards:
+    its final populations and particles equal a standalone LBMBox run of the
+    same request bit for bit, and agree with the FP64 oracle started from
+    the same initial state within the FP32 tolerance."""
+    from conftest import relerr
+    from multiphase_flow_codes_gb300.engine import LBMBox
+    steps, seed, npart = 12, 21, 3
+    target = serving.request(24, 32, 20, steps, wall_axis=1, npart=npart, seed=seed, u_rms=0.03,
+                             keep_state=True)
+    others = [serving.request(32, 24, 28, 9, wall_axis=1, npart=2, seed=8),
+              serving.request(24, 24, 24, 17, wall_axis=-1, npart=2, seed=11)]
+    with serving.LBMServer(8 << 30, 16, 4) as srv:
+        ids = [srv.submit(r) for r in others[:1] + [target] + others[1:]]
+        res = [srv.wait(i, timeout=300.0) for i in ids]
+        assert all(r.state == serving.REQ_DONE for r in res)
+        served = srv.take(ids[1])
+    assert (served.nx, served.ny, served.nz) == (32, 24, 20)  # walls normal to engine x
+    f_served = served.get_f()
+    p_served = served.get_particles()
+    served.close()
+
+    cfg = capi.config_init(capi.LBM_PRESET_CHANNEL, 32, 24, 20, npart, 4.0, 1.0)
+    cfg.precision = capi.LBM_PREC_F32
+    box = LBMBox(cfg)
+    box.init_spectral(4.0, 0.03, seed)
+    box.macrovar()
+    box.init_particles(npart, seed=seed % 2147483646 + 1)
+    f0 = box.get_f()
+    y0 = box.get_particles()["ypglb"]
+    box.step(steps)
+    assert np.array_equal(box.get_f(), f_served)
+    for k in ("ypglb", "wp", "omgp", "fHIp"):
+        assert np.array_equal(box.get_particles()[k], p_served[k]), k
+    box.close()
+
+    ocfg = capi.config_init(capi.LBM_PRESET_CHANNEL, 32, 24, 20, npart, 4.0, 1.0)
+    o = oracle_mod.OracleBox(ocfg)
+    o.f[...] = f0
+    o.macrovar()
+    o.release_particles(y0)
+    assert o.step(steps) == 0
+    assert relerr(f_served, o.f) <= 1e-5
+    assert relerr(p_served["ypglb"], o.ypglb[:npart]) <= 1e-9
