@@ -381,9 +381,10 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=20.0,
                     help="window of the Poisson serving run (0: skip it)")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="requests per second")
-    ap.add_argument("--sums", choices=["fixed", "float"], default="fixed",
+    ap.add_argument("--sums", choices=["fixed", "float", "integer"], default="fixed",
                     help="FP64 collision arithmetic: integer-coefficient moment sums exact in "
-                         "64-bit fixed point (default) or all in FP64")
+                         "64-bit fixed point (fixed, the default), all in FP64 (float), or the "
+                         "velocity and force products as integer products too (integer)")
     ap.add_argument("--variant", default=None,
                     help="stream+collide kernel as 'variant,stages,groups,ctas_per_sm' "
                          "(default: autotuned on the workload)")
@@ -407,8 +408,11 @@ def main():
     dtype = "f64" if c.precision == capi.LBM_PREC_F64 else "f32"
     cfg_desc = describe(wl.name, c, wl.npart, wl.k0, wl.urms, dtype, world)
     if dtype == "f64":
-        cfg_desc["collision_sums"] = ("integer-coefficient moment sums exact in 64-bit fixed point, "
-                                      "products FP64" if args.sums == "fixed" else "all FP64")
+        cfg_desc["collision_sums"] = {
+            "fixed": "integer-coefficient moment sums exact in 64-bit fixed point, products FP64",
+            "integer": "moment sums exact in 64-bit fixed point, velocity and force products as "
+                       "exact 128-bit integer products (no FP64 instruction per in-range node)",
+            "float": "all FP64"}[args.sums]
 
     import torch
     torch.cuda.set_device(local)
@@ -421,7 +425,8 @@ def main():
     torch.cuda.synchronize()
     sampler.start()
     fixed = tuple(int(v) for v in args.variant.split(",")) if args.variant else None
-    sums = capi.LBM_SUMS_FIXED if args.sums == "fixed" else capi.LBM_SUMS_FLOAT
+    sums = {"fixed": capi.LBM_SUMS_FIXED, "float": capi.LBM_SUMS_FLOAT,
+            "integer": capi.LBM_SUMS_INTEGER}[args.sums]
     ms, launches, phases, f64, p64, variant = run_device(wl, u, y, args.steps, args.warmup, local,
                                                          want_f=not args.no_fp32, variant=fixed,
                                                          sums=sums)
@@ -438,13 +443,13 @@ def main():
     alg_bytes = 2 * 19 * esz * N
     achieved = alg_bytes / (sc_ms / sc_n / 1e3) / 1e9 if sc_n else None
     figs = profile_figures()
-    key = f"fused_{dtype}_{c.nx}" + ("_fx" if dtype == "f64" and args.sums == "fixed" else "")
+    key = f"fused_{dtype}_{c.nx}" + ("_fx" if dtype == "f64" and args.sums != "float" else "")
     traffic = None
     if key in figs and figs[key].get("dram_bytes_per_node"):
         traffic = figs[key]["dram_bytes_per_node"] * N
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
-            "kernel": kernel_name(variant, dtype == "f64" and args.sums == "fixed"),
+            "kernel": kernel_name(variant, dtype == "f64" and args.sums != "float"),
             "alg_bytes_per_launch": alg_bytes, "peak_source": peak_src}
     fp64 = {}
     if dtype == "f64" and key in figs and figs[key].get("fp64_flop_per_node") and sc_n:

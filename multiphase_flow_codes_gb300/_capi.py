@@ -31,7 +31,7 @@ LBM_BC_PERIODIC, LBM_BC_XWALLS = 0, 1
 LBM_FORCING_NONE, LBM_FORCING_STOCHASTIC, LBM_FORCING_CONSTANT = 0, 1, 2
 LBM_PRESET_BOX, LBM_PRESET_CHANNEL = 0, 1
 LBM_VARIANT_DIRECT, LBM_VARIANT_STAGED, LBM_VARIANT_STAGED_X2 = 1, 2, 3
-LBM_SUMS_FLOAT, LBM_SUMS_FIXED = 0, 1
+LBM_SUMS_FLOAT, LBM_SUMS_FIXED, LBM_SUMS_INTEGER = 0, 1, 2
 
 
 class lbm_config(C.Structure):

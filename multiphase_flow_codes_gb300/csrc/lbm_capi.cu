@@ -214,7 +214,7 @@ void pop_format(lbm_ctx* c, bool fixed) {
 // sums, the direct stream + collide kernel
 bool fixed_path(const lbm_ctx* c) {
   // (a constant body force must fit the fixed-point force range, |F| < 2^-7)
-  return !c->f32 && c->sums == LBM_SUMS_FIXED && c->variant == LBM_VARIANT_DIRECT &&
+  return !c->f32 && c->sums != LBM_SUMS_FLOAT && c->variant == LBM_VARIANT_DIRECT &&
          std::fabs(c->cfg.force_y) < 0.0078125;
 }
 template <typename T>
@@ -498,7 +498,7 @@ void launch_stream_collide(lbm_ctx* c, const T* fin, T* fout, bool use_cache = f
     return;
   }
   int mode = 0;
-  const bool fx = !c->f32 && c->sums == LBM_SUMS_FIXED;
+  const bool fx = !c->f32 && c->sums != LBM_SUMS_FLOAT;
   if (use_cache && fx && c->fcache && c->latest.mode == FM_TABLE) {
     const bool hit = c->fmacro.mode == FM_TABLE && c->fmacro.slot == c->fcache_slot &&
                      c->slot_version[c->fcache_slot] == c->fcache_version;
@@ -507,7 +507,8 @@ void launch_stream_collide(lbm_ctx* c, const T* fin, T* fout, bool use_cache = f
   bool done = false;
   if constexpr (sizeof(T) == 8) {
     if (c->g.pop_fixed) {  // fin and fout in fixed point (fixed_path)
-      launch_fused_fixed(c->g, c->r, fin, fout, c->flags[c->fcur], fview<T>(c, c->fmacro),
+      launch_fused_fixed(c->g, c->r, c->sums == LBM_SUMS_INTEGER, fin, fout, c->flags[c->fcur],
+                         fview<T>(c, c->fmacro),
                          fview<T>(c, c->latest), reinterpret_cast<T*>(c->fcache), mode,
                          c->status, c->stream);
       done = true;
@@ -532,7 +533,7 @@ void launch_stream_collide(lbm_ctx* c, const T* fin, T* fout, bool use_cache = f
 bool plan_staged(lbm_ctx* c, int variant, int stages, int ctas_per_sm, StagedPlan* p,
                  int groups = 1) {
   const bool packed = variant == LBM_VARIANT_STAGED_X2;
-  const bool fx = !c->f32 && c->sums == LBM_SUMS_FIXED;
+  const bool fx = !c->f32 && c->sums != LBM_SUMS_FLOAT;
   if (variant != LBM_VARIANT_STAGED && !packed) return false;
   if (stages == 0) {
     for (int S = 4; S >= 2 && stages == 0; --S) {
@@ -1815,7 +1816,7 @@ int lbm_set_variant(lbm_ctx* ctx, int variant, int stages, int groups, int ctas_
 
 int lbm_set_sums(lbm_ctx* ctx, int mode) {
   if (!ctx) return LBM_ERR_ARG;
-  if (mode != LBM_SUMS_FLOAT && mode != LBM_SUMS_FIXED)
+  if (mode != LBM_SUMS_FLOAT && mode != LBM_SUMS_FIXED && mode != LBM_SUMS_INTEGER)
     return fail(ctx, LBM_ERR_ARG, "unknown collision arithmetic");
   if (ctx->f32 && mode != LBM_SUMS_FLOAT)
     return fail(ctx, LBM_ERR_ARG, "fixed-point sums apply to FP64 contexts only");

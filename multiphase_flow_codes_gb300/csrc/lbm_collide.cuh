@@ -37,6 +37,10 @@ struct RatesT {
   // [1..15] A_k, [16] B1r, [17] B2r, [18] 1/19
   long long Li[19];
   int Lsh[19];
+  // the factors of the velocity and force terms, for the all-integer core
+  // (fx_core_int): B1t H1 B2t H2 B3 H3 B6 H6 B7 H7 B8 H8 B9 H9 B10 H10 0.1 0.05
+  long long Ni[18];
+  int Nsh[18];
 };
 
 // c as (integer m, shift sh) with c = m * 2^-sh exactly and |m| in
@@ -72,6 +76,11 @@ RatesT<T> rates_t(const Rates& r) {
   fixed_factor(-11.0 * Bk(1), &o.Li[16], &o.Lsh[16]);
   fixed_factor(r.omegepsl * Bk(2), &o.Li[17], &o.Lsh[17]);
   fixed_factor(1.0 / 19.0, &o.Li[18], &o.Lsh[18]);
+  const double nf[18] = {19.0 * Bk(1), 38.0 * Hk(1), r.omegepslj * Bk(2), -11.0 * Hk(2),
+                         -2.0 / 3.0 * Bk(3), -2.0 / 3.0 * Hk(3), Bk(6), 2.0 * Hk(6),
+                         r.omegxx * Bk(7), -Hk(7), Bk(8), 2.0 * Hk(8), r.omegxx * Bk(9), -Hk(9),
+                         Bk(10), Hk(10), 0.1, 0.05};
+  for (int k = 0; k < 18; ++k) fixed_factor(nf[k], &o.Ni[k], &o.Nsh[k]);
   return o;
 }
 
@@ -458,6 +467,167 @@ __host__ __device__ __forceinline__ bool fx_core(const long long (&g)[NPOP], FP 
   return true;
 }
 
+// round(a * b * 2^-s), s >= 1: one exact 128-bit product, one rounding
+__host__ __device__ __forceinline__ long long mul_round(long long a, long long b, int s) {
+  const __int128 p = (__int128)a * (__int128)b + ((__int128)1 << (s - 1));
+  return (long long)(p >> s);
+}
+
+// fx_core with the velocity and force terms as integer products too, so the
+// collision issues no FP64 instruction: the velocity u (scale 2^-kFxIn) and
+// this step's body force F (2^-kFxF) enter as integers; the products
+// u_a u_b are rounded once to 2^-64 and F_a u_b to 2^-kFxF; each term of a
+// moment is one exact 128-bit product of such a value and a fixed-point
+// factor (RatesT::Ni), rounded once to 2^-kFxOut.  Ranges, so that nothing
+// overflows: |u| < 2^-2 and |F| < 2^-9 (a node beyond them is declined, as
+// is one whose moments leave their ranges).  The roundings (2^-62 per term)
+// are those of fx_core's conversions from FP64.
+constexpr int kFxUU = 64;  // u_a u_b
+__host__ __device__ __forceinline__ bool fx_core_int(const long long (&g)[NPOP], long long fpx,
+                                                     long long fpy, long long fpz, long long Fx,
+                                                     long long Fy, long long Fz,
+                                                     const RatesT<double>& r,
+                                                     long long (&h)[NPOP]) {
+  typedef long long I;
+  const I a1 = g[1] + g[2], d1 = g[1] - g[2];
+  const I a3 = g[3] + g[4], d3 = g[3] - g[4];
+  const I a5 = g[5] + g[6], d5 = g[5] - g[6];
+  const I s78 = g[7] + g[8], d78 = g[7] - g[8], s910 = g[9] + g[10], d910 = g[9] - g[10];
+  const I s1112 = g[11] + g[12], d1112 = g[11] - g[12];
+  const I s1314 = g[13] + g[14], d1314 = g[13] - g[14];
+  const I s1516 = g[15] + g[16], d1516 = g[15] - g[16];
+  const I s1718 = g[17] + g[18], d1718 = g[17] - g[18];
+  const I sum1 = a1 + a3 + a5;
+  const I Sxy = s78 + s910, Sxz = s1112 + s1314, Syz = s1516 + s1718;
+  const I sum2 = Sxy + Sxz + Syz;
+  const I D1 = d78 + d910, D2 = d1112 + d1314;
+  const I sum3 = D1 + D2;
+  const I A = s78 - s910, Bv = d1516 + d1718;
+  const I sum4 = A + Bv;
+  const I C = s1112 - s1314, Dd = s1516 - s1718;
+  const I sum5 = C + Dd;
+  const I sum7 = a3 + a5, sum8 = Sxy + Sxz, sum10 = a3 - a5, sum11 = Sxy - Sxz;
+  const I rho = g[0] + sum1 + sum2;
+  const I ev1 = -30 * g[0] - 11 * sum1 + 8 * sum2;
+  const I ev2 = 12 * g[0] - 4 * sum1 + sum2;
+  const I ev3 = -4 * d1 + sum3;
+  const I ev4 = -4 * d3 + sum4;
+  const I ev5 = -4 * d5 + sum5;
+  const I ev6 = 2 * (a1 - Syz) - sum7 + sum8;
+  const I ev7 = -4 * a1 + 2 * (sum7 - Syz) + sum8;
+  const I ev8 = sum10 + sum11;
+  const I ev9 = -2 * sum10 + sum11;
+  // macrovar: u = sum c f + F_prev / 2, exact at 2^-kFxIn
+  constexpr int sh = kFxF - kFxIn + 1;
+  auto half = [](long long v) { return (v + (1LL << (sh - 1))) >> sh; };
+  const I ux = d1 + sum3 + half(fpx);
+  const I uy = d3 + sum4 + half(fpy);
+  const I uz = d5 + sum5 + half(fpz);
+  {
+    constexpr unsigned long long ulim = 1ULL << (kFxIn - 2);  // |u| < 2^-2
+    constexpr unsigned long long flim = 1ULL << (kFxF - 9);   // |F| < 2^-9
+    const unsigned long long bad =
+        (((unsigned long long)ux + ulim) | ((unsigned long long)uy + ulim) |
+         ((unsigned long long)uz + ulim)) & ~(2 * ulim - 1);
+    const unsigned long long badf =
+        (((unsigned long long)Fx + flim) | ((unsigned long long)Fy + flim) |
+         ((unsigned long long)Fz + flim)) & ~(2 * flim - 1);
+    if (bad | badf) return false;
+  }
+  // products (collision.f90:66-81): u_a u_b at 2^-64, F_a u_b at 2^-kFxF
+  constexpr int suu = 2 * kFxIn - kFxUU, sfu = kFxIn;
+  const I qxx = mul_round(ux, ux, suu), qyy = mul_round(uy, uy, suu), qzz = mul_round(uz, uz, suu);
+  const I qxy = mul_round(ux, uy, suu), qyz = mul_round(uy, uz, suu), qxz = mul_round(ux, uz, suu);
+  const I pa = mul_round(Fx, ux, sfu), pb = mul_round(Fy, uy, sfu), pc = mul_round(Fz, uz, sfu);
+  const I t1 = qxx + qyy + qzz;
+  const I eq6 = 2 * qxx - qyy - qzz, eq8 = qyy - qzz;
+  const I G3 = pa + pb + pc, e6 = 2 * pa - pb - pc, e8 = pb - pc;
+  const I m10 = mul_round(Fx, uy, sfu) + mul_round(Fy, ux, sfu);
+  const I m11 = mul_round(Fy, uz, sfu) + mul_round(Fz, uy, sfu);
+  const I m12 = mul_round(Fx, uz, sfu) + mul_round(Fz, ux, sfu);
+  // factor k times a value at scale 2^-sv, at 2^-kFxOut
+  auto N = [&](int k, I v, int sv) { return mul_round(v, r.Ni[k], r.Nsh[k] + sv - kFxOut); };
+  auto L = [&](int k, I v) { return fx_mul(v, r.Li[k], r.Lsh[k]); };
+  I M[16];
+  M[1] = L(1, ev1) + L(16, rho) + N(0, t1, kFxUU) + N(1, G3, kFxF);
+  M[2] = L(2, ev2) + L(17, rho) + N(2, t1, kFxUU) + N(3, G3, kFxF);
+  M[3] = L(3, ev3) + N(4, ux, kFxIn) + N(5, Fx, kFxF);
+  M[4] = L(4, ev4) + N(4, uy, kFxIn) + N(5, Fy, kFxF);
+  M[5] = L(5, ev5) + N(4, uz, kFxIn) + N(5, Fz, kFxF);
+  M[6] = L(6, ev6) + N(6, eq6, kFxUU) + N(7, e6, kFxF);
+  M[7] = L(7, ev7) + N(8, eq6, kFxUU) + N(9, e6, kFxF);
+  M[8] = L(8, ev8) + N(10, eq8, kFxUU) + N(11, e8, kFxF);
+  M[9] = L(9, ev9) + N(12, eq8, kFxUU) + N(13, e8, kFxF);
+  M[10] = L(10, d78 - d910) + N(14, qxy, kFxUU) + N(15, m10, kFxF);
+  M[11] = L(11, d1516 - d1718) + N(14, qyz, kFxUU) + N(15, m11, kFxF);
+  M[12] = L(12, d1112 - d1314) + N(14, qxz, kFxUU) + N(15, m12, kFxF);
+  M[13] = L(13, D1 - D2);
+  M[14] = L(14, Bv - A);
+  M[15] = L(15, C - Dd);
+  const I tl1 = L(18, rho);
+  const I tl6 = N(16, ux, kFxIn) + N(17, Fx, kFxF);
+  const I tl8 = N(16, uy, kFxIn) + N(17, Fy, kFxF);
+  const I tl10 = N(16, uz, kFxIn) + N(17, Fz, kFxF);
+  unsigned out = 0;
+#pragma unroll
+  for (int k = 1; k < 16; ++k) out |= fx_out_of_range(M[k]);
+  out |= fx_out_of_range(tl1) | fx_out_of_range(tl6) | fx_out_of_range(tl8) |
+         fx_out_of_range(tl10);
+  if (out) return false;
+
+  // inverse transform, exact (collision.f90:160-200)
+  h[0] = tl1 - 30 * M[1] + 12 * M[2];
+  const I suma = tl1 - 11 * M[1] - 4 * M[2];
+  const I sumb = tl1 + 8 * M[1] + M[2];
+  const I sumc = tl6 - 4 * M[3];
+  const I sumd = 2 * M[6] - 4 * M[7];
+  const I sume = tl8 - 4 * M[4];
+  const I q67 = 2 * M[7] - M[6], r89 = M[8] - 2 * M[9];
+  const I sumf = q67 + r89;
+  const I sumg = tl10 - 4 * M[5];
+  const I sumh = q67 - r89;
+  const I p67 = M[6] + M[7], p89 = M[8] + M[9];
+  const I sumi = p67 + p89;
+  const I sumk = p67 - p89;
+  const I sump = -2 * p67;
+  const I sum67 = tl6 + M[3], sum89 = tl8 + M[4], sum1011 = tl10 + M[5];
+  const I ad = suma + sumd, af = suma + sumf, ah = suma + sumh;
+  h[1] = ad + sumc;
+  h[2] = ad - sumc;
+  h[3] = af + sume;
+  h[4] = af - sume;
+  h[5] = ah + sumg;
+  h[6] = ah - sumg;
+  {
+    const I base = sumb + sumi, p = sum67 + sum89, m = sum67 - sum89;
+    const I bp = base + M[10], bm = base - M[10];
+    const I P = p + (M[13] - M[14]), Q = m + (M[13] + M[14]);
+    h[7] = bp + P;
+    h[10] = bp - P;
+    h[8] = bm - Q;
+    h[9] = bm + Q;
+  }
+  {
+    const I base = sumb + sumk, p = sum67 + sum1011, m = sum67 - sum1011;
+    const I bp = base + M[12], bm = base - M[12];
+    const I P = p + (M[15] - M[13]), Q = m - (M[13] + M[15]);
+    h[11] = bp + P;
+    h[14] = bp - P;
+    h[12] = bm - Q;
+    h[13] = bm + Q;
+  }
+  {
+    const I base = sumb + sump, p = sum89 + sum1011, m = sum89 - sum1011;
+    const I bp = base + M[11], bm = base - M[11];
+    const I P = p + (M[14] - M[15]), Q = m + (M[14] + M[15]);
+    h[15] = bp + P;
+    h[18] = bp - P;
+    h[16] = bm - Q;
+    h[17] = bm + Q;
+  }
+  return true;
+}
+
 __host__ __device__ __forceinline__ bool collide_fx(double (&f)[NPOP], double fpx, double fpy,
                                                     double fpz, double fx, double fy, double fz,
                                                     const RatesT<double>& r) {
@@ -499,6 +669,26 @@ __host__ __device__ __forceinline__ bool collide_fx_fixed(long long (&g)[NPOP], 
   if (out) return false;
   long long h[NPOP];
   if (!fx_core<FP>(g, fpx, fpy, fpz, fx, fy, fz, r, h)) return false;
+  constexpr int sh = kFxOut - kFxIn;
+#pragma unroll
+  for (int q = 0; q < NPOP; ++q) g[q] = (h[q] + (1LL << (sh - 1))) >> sh;
+  return true;
+}
+
+// collide_fx_fixed with the all-integer core (fx_core_int): the forces of
+// this step (Fx, Fy, Fz) at 2^-kFxF.
+__host__ __device__ __forceinline__ bool collide_fx_fixed_int(long long (&g)[NPOP], long long fpx,
+                                                              long long fpy, long long fpz,
+                                                              long long Fx, long long Fy,
+                                                              long long Fz,
+                                                              const RatesT<double>& r) {
+  constexpr unsigned long long lim = 1ULL << (kFxIn + kFxInMax);
+  unsigned long long out = 0;
+#pragma unroll
+  for (int q = 0; q < NPOP; ++q) out |= ((unsigned long long)g[q] + lim) & ~(2 * lim - 1);
+  if (out) return false;
+  long long h[NPOP];
+  if (!fx_core_int(g, fpx, fpy, fpz, Fx, Fy, Fz, r, h)) return false;
   constexpr int sh = kFxOut - kFxIn;
 #pragma unroll
   for (int q = 0; q < NPOP; ++q) g[q] = (h[q] + (1LL << (sh - 1))) >> sh;

@@ -327,7 +327,7 @@ __device__ __forceinline__ void body_force_fx(const ForceView<double>& fv, const
 // as in k_fused) holds them as 64-bit integers at 2^-kFxF.
 // Five CTAs of 128 threads per SM (96 registers; the 19 populations spill to
 // L1) measured 3 % faster than four without spills, six slower.
-template <bool CHANNEL>
+template <bool CHANNEL, bool INTCORE>
 __global__ void __launch_bounds__(128, 5) k_fused_fixed(Geometry g, RatesT<double> r,
                                                          const long long* __restrict__ fin,
                                                          long long* __restrict__ fout,
@@ -360,8 +360,15 @@ __global__ void __launch_bounds__(128, 5) k_fused_fixed(Geometry g, RatesT<doubl
     body_force_fx(fnew, g, x, y, z, fc);
   }
   if (!solid) {
-    const double fx = fx_to<kFxF>(fc[0]), fy = fx_to<kFxF>(fc[1]), fz = fx_to<kFxF>(fc[2]);
-    if (!collide_fx_fixed<long long>(f, fp[0], fp[1], fp[2], fx, fy, fz, r)) {
+    bool done;
+    if constexpr (INTCORE) {
+      done = collide_fx_fixed_int(f, fp[0], fp[1], fp[2], fc[0], fc[1], fc[2], r);
+    } else {
+      done = collide_fx_fixed<long long>(f, fp[0], fp[1], fp[2], fx_to<kFxF>(fc[0]),
+                                         fx_to<kFxF>(fc[1]), fx_to<kFxF>(fc[2]), r);
+    }
+    if (!done) {
+      const double fx = fx_to<kFxF>(fc[0]), fy = fx_to<kFxF>(fc[1]), fz = fx_to<kFxF>(fc[2]);
       double d[NPOP];
 #pragma unroll
       for (int q = 0; q < NPOP; ++q) d[q] = pop_from_fixed(fin[(size_t)q * N + n]);
@@ -802,8 +809,8 @@ void launch_fused_step(const Geometry& g, const Rates& r, const T* fin, T* fout,
     { k_fused<T, false><<<row_grid(g, B), B, 0, s>>>(g, rt, fin, fout, isnodes, fprev, fnew, nullptr, 0); count_launch(); }
 }
 
-void launch_fused_fixed(const Geometry& g, const Rates& r, const double* fin, double* fout,
-                        const int32_t* isnodes, const ForceView<double>& fprev,
+void launch_fused_fixed(const Geometry& g, const Rates& r, bool int_core, const double* fin,
+                        double* fout, const int32_t* isnodes, const ForceView<double>& fprev,
                         const ForceView<double>& fnew, double* fcache, int fcache_mode,
                         DevStatus* st, cudaStream_t s) {
   const int B = 128;
@@ -812,12 +819,13 @@ void launch_fused_fixed(const Geometry& g, const Rates& r, const double* fin, do
   const long long* gi = reinterpret_cast<const long long*>(fin);
   long long* go = reinterpret_cast<long long*>(fout);
   long long* fci = reinterpret_cast<long long*>(fcache);
-  if (g.channel)
-    k_fused_fixed<true><<<row_grid(g, B), B, 0, s>>>(g, rt, gi, go, isnodes, fprev, fnew, fci,
-                                                     fcache_mode, st);
+  auto launch = [&](auto kern) {
+    kern<<<row_grid(g, B), B, 0, s>>>(g, rt, gi, go, isnodes, fprev, fnew, fci, fcache_mode, st);
+  };
+  if (int_core)
+    g.channel ? launch(k_fused_fixed<true, true>) : launch(k_fused_fixed<false, true>);
   else
-    k_fused_fixed<false><<<row_grid(g, B), B, 0, s>>>(g, rt, gi, go, isnodes, fprev, fnew, fci,
-                                                      fcache_mode, st);
+    g.channel ? launch(k_fused_fixed<true, false>) : launch(k_fused_fixed<false, false>);
   count_launch();
 }
 

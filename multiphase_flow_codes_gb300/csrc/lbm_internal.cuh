@@ -152,7 +152,8 @@ void launch_fused_step(const Geometry& g, const Rates& r, const T* fin, T* fout,
                        cudaStream_t s);
 // the FP64 fixed-point step on populations stored in fixed point (fin and
 // fout hold 64-bit integers at 2^-58; g.pop_fixed)
-void launch_fused_fixed(const Geometry& g, const Rates& r, const double* fin, double* fout,
+void launch_fused_fixed(const Geometry& g, const Rates& r, bool int_core, const double* fin,
+                        double* fout,
                         const int32_t* isnodes, const ForceView<double>& fprev,
                         const ForceView<double>& fnew, double* fcache, int fcache_mode,
                         DevStatus* st, cudaStream_t s);

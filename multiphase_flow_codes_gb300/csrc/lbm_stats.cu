@@ -234,40 +234,59 @@ __global__ void k_spectral_modes(int nx, int ny, int nz, double k0, uint64_t see
   vz[t] = out[2];
 }
 
-// Energy of shell ik = blockIdx.x + 1 (shells int(|k| + 1/2)) over the
-// half spectrum, the kx = 0 plane weighted 1/2 as initvel and statistc count
-// it.  One block per shell scans every mode in a fixed order and reduces with
-// a fixed tree, so the sums are the same bits on every run.
-__global__ void __launch_bounds__(256) k_shell_energy(int nx, int ny, int nz,
+// Target energy of shell ik: the workload's spectrum ik^4 exp(-2 (ik/k0)^2)
+__device__ __forceinline__ double shell_target(int ik, double k0) {
+  const double q = (double)ik / k0;
+  return (double)ik * ik * ik * ik * exp(-2.0 * q * q);
+}
+
+// Energy of every shell int(|k| + 1/2) = 1..nek over the half spectrum, the
+// kx = 0 plane weighted 1/2 as initvel and statistc count it, relative to the
+// shell's target energy.  Each mode's share is converted to 64-bit fixed
+// point at 2^-kShellFx and added with integer atomics, per block in shared
+// memory and then per shell in global memory: integer addition does not
+// depend on the order, so the sums are the same bits on every run.  (The
+// modes are pre-shaped to the target spectrum, so a shell sums to a few
+// units whatever its energy.)
+constexpr int kShellFx = 50;
+__global__ void __launch_bounds__(256) k_shell_energy(int nx, int ny, int nz, double k0,
                                                       const double2* __restrict__ vx,
                                                       const double2* __restrict__ vy,
                                                       const double2* __restrict__ vz,
-                                                      double* __restrict__ shell_e) {
-  using Red = cub::BlockReduce<double, 256>;
-  __shared__ typename Red::TempStorage tmp;
-  const int ik = blockIdx.x + 1;
+                                                      unsigned long long* __restrict__ acc) {
+  extern __shared__ unsigned long long sacc[];
+  const int nek = (int)(nx / 2 - 1.5);
+  for (int i = threadIdx.x; i <= nek; i += blockDim.x) sacc[i] = 0ull;
+  __syncthreads();
   const int nxc = nx / 2 + 1;
   const long long total = (long long)nxc * ny * nz;
-  double s = 0.0;
-  for (long long t = threadIdx.x; t < total; t += blockDim.x) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
     const int kx = (int)(t % nxc);
     const long long r = t / nxc;
     const int ky = signed_k((int)(r % ny), ny), kz = signed_k((int)(r / ny), nz);
     const double k2 = (double)kx * kx + (double)ky * ky + (double)kz * kz;
-    if ((int)(sqrt(k2) + 0.5) != ik) continue;
+    const int ik = (int)(sqrt(k2) + 0.5);
+    if (ik < 1 || ik > nek) continue;
+    const double target = shell_target(ik, k0);
+    if (!(target > 0.0)) continue;
     const double2 a = vx[t], b = vy[t], c = vz[t];
-    const double e = a.x * a.x + a.y * a.y + b.x * b.x + b.y * b.y + c.x * c.x + c.y * c.y;
-    s += kx == 0 ? 0.5 * e : e;
+    double e = a.x * a.x + a.y * a.y + b.x * b.x + b.y * b.y + c.x * c.x + c.y * c.y;
+    if (kx == 0) e *= 0.5;
+    const double q = ldexp(e / target, kShellFx);
+    atomicAdd(&sacc[ik], (unsigned long long)llrint(fmin(q, 9.0e18)));
   }
-  const double tot = Red(tmp).Sum(s);
-  if (threadIdx.x == 0) shell_e[ik] = tot;
+  __syncthreads();
+  for (int i = threadIdx.x; i <= nek; i += blockDim.x)
+    if (sacc[i]) atomicAdd(&acc[i], sacc[i]);
 }
 
-// Scale every mode of shell ik so that the shell holds ik^4 exp(-2 (ik/k0)^2)
+// Scale every mode of shell ik so that the shell holds its target energy
 // (initvel's per-shell rescaling with the workload's spectrum).
-__global__ void k_shell_scale(int nx, int ny, int nz, double k0,
-                              const double* __restrict__ shell_e, double2* __restrict__ vx,
-                              double2* __restrict__ vy, double2* __restrict__ vz) {
+__global__ void k_shell_scale(int nx, int ny, int nz,
+                              const unsigned long long* __restrict__ acc,
+                              double2* __restrict__ vx, double2* __restrict__ vy,
+                              double2* __restrict__ vz) {
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const int nxc = nx / 2 + 1;
   const long long total = (long long)nxc * ny * nz;
@@ -279,11 +298,8 @@ __global__ void k_shell_scale(int nx, int ny, int nz, double k0,
   const int ik = (int)(sqrt(k2) + 0.5);
   const int nek = (int)(nx / 2 - 1.5);
   double f = 0.0;
-  if (ik >= 1 && ik <= nek && shell_e[ik] > 0.0) {
-    const double q = (double)ik / k0;
-    const double target = (double)ik * ik * ik * ik * exp(-2.0 * q * q);
-    f = sqrt(target / shell_e[ik]);
-  }
+  if (ik >= 1 && ik <= nek && acc[ik] > 0ull)
+    f = sqrt(1.0 / ldexp((double)acc[ik], -kShellFx));  // sqrt(target / shell energy)
   vx[t] = make_double2(vx[t].x * f, vx[t].y * f);
   vy[t] = make_double2(vy[t].x * f, vy[t].y * f);
   vz[t] = make_double2(vz[t].x * f, vz[t].y * f);
@@ -374,7 +390,7 @@ int spectral_field(const Geometry& g, double k0, double urms, uint64_t seed, dou
   const int nek = (int)(g.nx / 2 - 1.5);
   double2* spec = nullptr;
   double* tmp = nullptr;
-  double* shell_e = nullptr;
+  unsigned long long* shell_acc = nullptr;
   void* cub_tmp = nullptr;
   size_t cub_bytes = 0;
   cufftHandle plan = 0;
@@ -382,7 +398,7 @@ int spectral_field(const Geometry& g, double k0, double urms, uint64_t seed, dou
   cub::DeviceReduce::Sum(nullptr, cub_bytes, tmp, tmp, 3 * N);
   if (cudaMalloc((void**)&spec, 3 * nc * sizeof(double2)) != cudaSuccess ||
       cudaMalloc((void**)&tmp, (3 * N + 1) * sizeof(double)) != cudaSuccess ||
-      cudaMalloc((void**)&shell_e, (nek + 2) * sizeof(double)) != cudaSuccess ||
+      cudaMalloc((void**)&shell_acc, (nek + 2) * sizeof(unsigned long long)) != cudaSuccess ||
       cudaMalloc(&cub_tmp, cub_bytes) != cudaSuccess) {
     rc = LBM_ERR_NOMEM;
   } else if (cufftPlan3d(&plan, g.nz, g.ny, g.nx, CUFFT_Z2D) != CUFFT_SUCCESS) {
@@ -394,11 +410,13 @@ int spectral_field(const Geometry& g, double k0, double urms, uint64_t seed, dou
                                                       spec + nc, spec + 2 * nc);
     count_launch();
     if (nek >= 1) {
-      k_shell_energy<<<nek, 256, 0, s>>>(g.nx, g.ny, g.nz, spec, spec + nc, spec + 2 * nc,
-                                         shell_e);
+      cudaMemsetAsync(shell_acc, 0, (nek + 2) * sizeof(unsigned long long), s);
+      const unsigned grid = (unsigned)std::min<long long>(blocks(nc, 256), 8LL * sm_count());
+      k_shell_energy<<<grid, 256, (nek + 1) * sizeof(unsigned long long), s>>>(
+          g.nx, g.ny, g.nz, k0, spec, spec + nc, spec + 2 * nc, shell_acc);
       count_launch();
-      k_shell_scale<<<blocks(nc, 256), 256, 0, s>>>(g.nx, g.ny, g.nz, k0, shell_e, spec,
-                                                    spec + nc, spec + 2 * nc);
+      k_shell_scale<<<blocks(nc, 256), 256, 0, s>>>(g.nx, g.ny, g.nz, shell_acc, spec, spec + nc,
+                                                    spec + 2 * nc);
       count_launch();
     }
     for (int c = 0; c < 3 && !rc; ++c)
@@ -418,7 +436,7 @@ int spectral_field(const Geometry& g, double k0, double urms, uint64_t seed, dou
   if (plan) cufftDestroy(plan);
   cudaFree(spec);
   cudaFree(tmp);
-  cudaFree(shell_e);
+  cudaFree(shell_acc);
   cudaFree(cub_tmp);
   return rc;
 }

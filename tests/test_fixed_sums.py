@@ -40,12 +40,13 @@ def test_fp64_contexts_default_to_fixed_sums(require_gpu):
         b32.set_sums(capi.LBM_SUMS_FIXED)
 
 
+@pytest.mark.parametrize("mode", [capi.LBM_SUMS_FIXED, capi.LBM_SUMS_INTEGER])
 @pytest.mark.parametrize("variant", [capi.LBM_VARIANT_DIRECT, capi.LBM_VARIANT_STAGED])
 @pytest.mark.parametrize("preset,shape", [
     (capi.LBM_PRESET_BOX, (48, 40, 32)),
     (capi.LBM_PRESET_CHANNEL, (32, 40, 24)),
 ])
-def test_fixed_sums_match_oracle_and_fp64(require_gpu, oracle_mod, variant, preset, shape):
+def test_fixed_sums_match_oracle_and_fp64(require_gpu, oracle_mod, variant, preset, shape, mode):
     if preset == capi.LBM_PRESET_CHANNEL and variant == capi.LBM_VARIANT_STAGED:
         pytest.skip("the staged kernel serves periodic boxes")
     o, fx = make_pair(oracle_mod, preset=preset, shape=shape, npart=3, rad=4.0, rhopart=2.5)
@@ -53,7 +54,8 @@ def test_fixed_sums_match_oracle_and_fp64(require_gpu, oracle_mod, variant, pres
     for b in (fx, fl):
         b.set_variant(variant)
     fl.set_sums(capi.LBM_SUMS_FLOAT)
-    assert fx.sums() == capi.LBM_SUMS_FIXED
+    fx.set_sums(mode)
+    assert fx.sums() == mode
     for _ in range(10):
         o.step(1)
         fx.step(1)
@@ -65,8 +67,10 @@ def test_fixed_sums_match_oracle_and_fp64(require_gpu, oracle_mod, variant, pres
     assert relerr(px["fHIp"], pl["fHIp"]) <= 1e-11
 
 
-@pytest.mark.parametrize("variant", [capi.LBM_VARIANT_DIRECT, capi.LBM_VARIANT_STAGED])
-def test_fixed_sums_hand_back_out_of_range_nodes(require_gpu, oracle_mod, variant):
+@pytest.mark.parametrize("variant,mode", [(capi.LBM_VARIANT_DIRECT, capi.LBM_SUMS_FIXED),
+                                          (capi.LBM_VARIANT_STAGED, capi.LBM_SUMS_FIXED),
+                                          (capi.LBM_VARIANT_DIRECT, capi.LBM_SUMS_INTEGER)])
+def test_fixed_sums_hand_back_out_of_range_nodes(require_gpu, oracle_mod, variant, mode):
     """One half of the box moves fast enough for populations of 1/8 and
     more; the other half is at rest with a 1e-9 density ripple, all its
     populations far below 2^-12.  The fast nodes take the FP64 path in both
@@ -91,12 +95,12 @@ def test_fixed_sums_hand_back_out_of_range_nodes(require_gpu, oracle_mod, varian
     f0 = f0 + w[:, None, None, None] * ripple[None]
     assert np.abs(f0).max() >= 0.125
     boxes = []
-    for mode in (capi.LBM_SUMS_FIXED, capi.LBM_SUMS_FLOAT):
+    for m in (mode, capi.LBM_SUMS_FLOAT):
         b = LBMBox(cfg)
         b.set_f(f0.copy())
         b.macrovar()
         b.set_variant(variant)
-        b.set_sums(mode)
+        b.set_sums(m)
         b.step(3)
         boxes.append(b.get_f())
     fxd, fld = boxes
