@@ -476,7 +476,7 @@ void particle_phase(lbm_ctx* c, T* f_plain) {
     cudaStreamWaitEvent(c->stream, c->ev_store, 0);
     c->store_pending = false;
   }
-  launch_links(c->g, pview(c), c->flags[nf], c->links, c->status, c->f32, c->stream, true);
+  launch_links(c->g, pview(c), c->flags[nf], c->links, c->status, c->f32 ? 1 : 0, c->stream, true);
   prof_end(c, LBM_PHASE_LINKS);
   prof_begin(c);
   launch_filling<T>(c->g, pview(c), c->pp, c->ypglbp, c->wpp, c->omgpp, c->flags[nf],
@@ -1463,7 +1463,7 @@ int lbm_upload_particles(lbm_ctx* ctx, int npart, const double* ypglb, const dou
   CK(reset_flags(ctx, 0));
   CK(reset_flags(ctx, 1));
   ctx->particles_on = npart > 0;
-  if (npart > 0) launch_links(ctx->g, pview(ctx), ctx->flags[ctx->fcur], ctx->links, ctx->status, ctx->f32, ctx->stream);
+  if (npart > 0) launch_links(ctx->g, pview(ctx), ctx->flags[ctx->fcur], ctx->links, ctx->status, ctx->f32 ? 1 : 0, ctx->stream);
   CK(cudaGetLastError());
   return check_status(ctx);
 }
@@ -1505,7 +1505,7 @@ int lbm_particle_state(lbm_ctx* ctx, int dir, int npart, double* state, int32_t*
   CK(reset_flags(ctx, 1));
   ctx->particles_on = npart > 0;
   if (npart > 0)
-    launch_links(ctx->g, pview(ctx), ctx->flags[ctx->fcur], ctx->links, ctx->status, ctx->f32,
+    launch_links(ctx->g, pview(ctx), ctx->flags[ctx->fcur], ctx->links, ctx->status, ctx->f32 ? 1 : 0,
                  ctx->stream);
   CK(cudaGetLastError());
   return check_status(ctx);
@@ -1690,7 +1690,7 @@ int lbm_beads_links(lbm_ctx* ctx) {
   if (!ctx->particles_on) return LBM_OK;
   int nf = 1 - ctx->fcur;
   CK(reset_flags(ctx, nf));
-  launch_links(ctx->g, pview(ctx), ctx->flags[nf], ctx->links, ctx->status, ctx->f32, ctx->stream);
+  launch_links(ctx->g, pview(ctx), ctx->flags[nf], ctx->links, ctx->status, ctx->f32 ? 1 : 0, ctx->stream);
   ctx->fcur = nf;
   CK(cudaGetLastError());
   return check_status(ctx);

@@ -41,6 +41,10 @@ struct RatesT {
   // (fx_core_int): B1t H1 B2t H2 B3 H3 B6 H6 B7 H7 B8 H8 B9 H9 B10 H10 0.1 0.05
   long long Ni[18];
   int Nsh[18];
+  // the same factors at the one scale 2^62 (|c| < 2), so that every product
+  // of the integer core shifts by a compile-time amount: [0..18] as Li,
+  // [19..36] as Ni
+  long long Ci[37];
 };
 
 // c as (integer m, shift sh) with c = m * 2^-sh exactly and |m| in
@@ -81,6 +85,12 @@ RatesT<T> rates_t(const Rates& r) {
                          r.omegxx * Bk(7), -Hk(7), Bk(8), 2.0 * Hk(8), r.omegxx * Bk(9), -Hk(9),
                          Bk(10), Hk(10), 0.1, 0.05};
   for (int k = 0; k < 18; ++k) fixed_factor(nf[k], &o.Ni[k], &o.Nsh[k]);
+  auto c62 = [](double c) { return (long long)std::llround(std::ldexp(c, 62)); };
+  for (int k = 0; k < 16; ++k) o.Ci[k] = c62(ck[k] * (1.0 - sk[k]));
+  o.Ci[16] = c62(-11.0 * Bk(1));
+  o.Ci[17] = c62(r.omegepsl * Bk(2));
+  o.Ci[18] = c62(1.0 / 19.0);
+  for (int k = 0; k < 18; ++k) o.Ci[19 + k] = c62(nf[k]);
   return o;
 }
 
@@ -545,9 +555,10 @@ __host__ __device__ __forceinline__ bool fx_core_int(const long long (&g)[NPOP],
   const I m10 = mul_round(Fx, uy, sfu) + mul_round(Fy, ux, sfu);
   const I m11 = mul_round(Fy, uz, sfu) + mul_round(Fz, uy, sfu);
   const I m12 = mul_round(Fx, uz, sfu) + mul_round(Fz, ux, sfu);
-  // factor k times a value at scale 2^-sv, at 2^-kFxOut
-  auto N = [&](int k, I v, int sv) { return mul_round(v, r.Ni[k], r.Nsh[k] + sv - kFxOut); };
-  auto L = [&](int k, I v) { return fx_mul(v, r.Li[k], r.Lsh[k]); };
+  // factor k (at 2^-62) times a value at scale 2^-sv, at 2^-kFxOut: the
+  // shifts are compile-time constants
+  auto N = [&](int k, I v, int sv) { return mul_round(v, r.Ci[19 + k], 62 + sv - kFxOut); };
+  auto L = [&](int k, I v) { return mul_round(v, r.Ci[k], 62 + kFxIn - kFxOut); };
   I M[16];
   M[1] = L(1, ev1) + L(16, rho) + N(0, t1, kFxUU) + N(1, G3, kFxF);
   M[2] = L(2, ev2) + L(17, rho) + N(2, t1, kFxUU) + N(3, G3, kFxF);

@@ -190,7 +190,12 @@ constexpr float kDecide = 4e-3f;
 
 // beads_links for one particle per block.  Integer outcomes (solid flags,
 // link sets) are exactly those of the reference's FP64 loop nest; the link
-// fraction alpha is FP64 (the reference formula) unless alpha_fp32 is set.
+// fraction alpha is computed in FP64 (alpha_fp32 0: stored FP64; 2: stored
+// FP32) or in FP32 (1, the FP32 population path).  The FP32 arithmetic starts
+// from offsets node - centre formed in FP64 and rounded once (a difference of
+// FP32 coordinates near x = 256 would be off by up to 1.5e-5 lattice units,
+// which the bounced populations would inherit), so alpha is good to the FP32
+// rounding of the quadratic's terms, about 1e-6.
 // The nearest-image history of the in-place sweeps of beads_links
 // (partlib.f90:959-985) for every particle: one thread per (particle, axis).
 // The y and x sweeps are taken from three start states (the centre, the end
@@ -241,7 +246,7 @@ __device__ __forceinline__ void k_links_body(int bx, int gx, Geometry g, Particl
   __shared__ double plane_z[MAXPLANES];
   __shared__ double yval[3][MAXC];
   __shared__ double xval[3][MAXC];
-  __shared__ float xvalf[3][MAXC];
+  __shared__ float xofff[3][MAXC];  // (i - 1/2) - x centre per x candidate, FP64 then rounded
   __shared__ int nplanes;
   __shared__ int row_k[MAXROWS], row_j[MAXROWS];
   __shared__ double row_z[MAXROWS], row_y[MAXROWS];
@@ -302,7 +307,7 @@ __device__ __forceinline__ void k_links_body(int bx, int gx, Geometry g, Particl
     if (c < tx) {
       double v = channel ? x0 : sweep_value(sev[3 + s], cx.at(c));
       xval[s][c] = v;
-      xvalf[s][c] = (float)v;
+      xofff[s][c] = (float)(((double)cx.at(c) - 0.5) - v);
     }
   }
   if (tid == 0 && (cy.total() > MAXC || cx.total() > MAXC)) fixed_ok = 0;
@@ -370,7 +375,7 @@ __device__ __forceinline__ void k_links_body(int bx, int gx, Geometry g, Particl
   // class of node (row r, x candidate ci): 0 out of reach, 1 solid, 2 fluid
   auto node_class = [&](int r, int ci) -> int {
     const int i = cx.at(ci);
-    const float xxf = ((float)i - 0.5f) - xvalf[min(r, 2)][ci];
+    const float xxf = xofff[min(r, 2)][ci];
     const float yyf = row_yy[r], zzf = row_zz[r];
     const float rr0f = xxf * xxf + yyf * yyf + zzf * zzf;
     if (!(rr0f <= reachf)) return 0;
@@ -449,7 +454,7 @@ __device__ __forceinline__ void k_links_body(int bx, int gx, Geometry g, Particl
       r = rc >> 8;
       ci = rc & 255;
       i = cx.at(ci);
-      xxf = ((float)i - 0.5f) - xvalf[min(r, 2)][ci];
+      xxf = xofff[min(r, 2)][ci];
       yyf = row_yy[r];
       zzf = row_zz[r];
 #pragma unroll
@@ -532,8 +537,8 @@ __device__ __forceinline__ void k_links_body(int bx, int gx, Geometry g, Particl
       // partlib.f90:1016-1023 with aa = |x0 - x1|^2 = |c|^2 (1 or 2) and
       // bb = x1.(x0 - x1) = -x1.c taken exactly: the same root without the
       // cancellation in the reference's aa and without divisions
-      if (alpha_fp32) {
-        const float xf = ((float)li - 0.5f) - xvalf[min(lr, 2)][lci] + (float)ix;
+      if (alpha_fp32 == 1) {
+        const float xf = xofff[min(lr, 2)][lci] + (float)ix;
         const float yf = row_yy[lr] + (float)iy, zf = row_zz[lr] + (float)iz;
         const float cc = xf * xf + yf * yf + zf * zf - rad2f;
         const float bb = -(xf * (float)ix + yf * (float)iy + zf * (float)iz);
@@ -559,7 +564,9 @@ __device__ __forceinline__ void k_links_body(int bx, int gx, Geometry g, Particl
         // max(disc, 0) by the sign bit (an integer select)
         const double disc = fma(a0, a0, -ca);
         const double a1 = sqrt(__double_as_longlong(disc) < 0 ? 0.0 : disc);
-        alph[w] = 1.0 - (-a0 + a1);
+        const double a = 1.0 - (-a0 + a1);
+        if (alpha_fp32 == 2) alph32[w] = (float)a;  // FP32 slab, FP64 arithmetic
+        else alph[w] = a;
       }
     }
     __syncthreads();
@@ -706,13 +713,14 @@ __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, Partic
     for (int t = threadIdx.x; t < 3 * kBounceSpan; t += NT) {
       const int a = t / kBounceSpan, d = t - a * kBounceSpan;
       const bool periodic = !(channel && a == 0);
-      const R cen = a == 0 ? xc0 : (a == 1 ? yc0 : zc0);
+      // in FP64 whatever R: an FP32 centre near x = 256 is off by 1.5e-5
+      const double cen = pv.ypglb[3 * p + a];
       const int n = a == 0 ? g.nx : (a == 1 ? g.ny : g.nz);
       const int nh = a == 0 ? g.nxh : (a == 1 ? g.nyh : g.nzh);
       int i = (a == 0 ? lo[0] : (a == 1 ? lo[1] : lo[2])) + d;
       if (periodic) i = ((i % n) + n) % n;
-      const R pnt = R(i + 1) - R(0.5);
-      tdel[a][d] = pnt - (periodic ? near_img_t<R>(cen, pnt, n, nh) : cen);
+      const double pnt = (double)(i + 1) - 0.5;
+      tdel[a][d] = R(pnt - (periodic ? near_img_t<double>(cen, pnt, n, nh) : cen));
     }
     if (threadIdx.x < NPOP) {
       const int q = threadIdx.x;
@@ -720,12 +728,13 @@ __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, Partic
     }
     __syncthreads();
   }
-  auto delta = [&](int a, int i, R cen, int n, int nhalf, bool periodic) -> R {
+  auto delta = [&](int a, int i, R, int n, int nhalf, bool periodic) -> R {
     int d = i - lo[a];
     if (periodic) d = d < 0 ? d + n : (d >= n ? d - n : d);
     if (d >= 0 && d < kBounceSpan) return tdel[a][d];
-    const R pnt = R(i + 1) - R(0.5);
-    return pnt - (periodic ? near_img_t<R>(cen, pnt, n, nhalf) : cen);
+    const double cen = pv.ypglb[3 * p + a];
+    const double pnt = (double)(i + 1) - 0.5;
+    return R(pnt - (periodic ? near_img_t<double>(cen, pnt, n, nhalf) : cen));
   };
   // cb db - cc dc for cb, cc in {-1, 0, 1}: one add at most
   auto cross = [](int cb, R db, int cc, R dc) -> R {

@@ -20,12 +20,14 @@ from . import config, inputs
 from .engine import LBMBatch, LBMBox
 
 
-def main(n: int = 128, npart: int = 150, steps: int = 3):
+def main(n: int = 128, npart: int = 150, steps: int = 3, sums: int = capi.LBM_SUMS_FIXED):
     u = inputs.spectral_velocity(n, 4.0, 0.03)
     y = inputs.initpartpos(n, n, n, npart, 4.0)
     for prec in (capi.LBM_PREC_F64, capi.LBM_PREC_F32):
         wl = config.box(n, npart, 4.0, 2.5, 4.0, 0.03, steps, precision=prec)
         box = LBMBox(wl.cfg)
+        if prec == capi.LBM_PREC_F64:
+            box.set_sums(sums)
         box.initpop(*u)
         box.macrovar()
         box.release_particles(y)
@@ -65,4 +67,7 @@ def main(n: int = 128, npart: int = 150, steps: int = 3):
 
 
 if __name__ == "__main__":
-    main()
+    import sys
+    modes = {"fixed": capi.LBM_SUMS_FIXED, "integer": capi.LBM_SUMS_INTEGER,
+             "float": capi.LBM_SUMS_FLOAT}
+    main(sums=modes[sys.argv[1]] if len(sys.argv) > 1 else capi.LBM_SUMS_FIXED)

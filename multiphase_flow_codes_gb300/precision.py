@@ -116,7 +116,7 @@ def storage_rounding(cfg64: capi.lbm_config, box64: LBMBox, steps: int = 1) -> d
 
 def error_report(cfg64: capi.lbm_config, u, ypglb: np.ndarray,
                  checkpoints=(10, 100, 2000), stream_ptr: int | None = None,
-                 floor: bool = True, split_at=(10,)) -> list:
+                 floor: bool = True, split_at=(10, 100)) -> list:
     """Step an FP64 and an FP32 copy of the same box (and, with `floor`, a
     second FP64 copy with plain-FP64 collision sums) to each checkpoint and
     compare them there; returns one dict per checkpoint with the FP32 errors

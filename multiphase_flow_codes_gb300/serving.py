@@ -7,16 +7,20 @@ drives it with a Poisson stream of channel solves (walls normal to y) and
 reports throughput and latency percentiles.
 
 The channel workload: grid X x Y x Z with X, Z uniform in 64..192 and the
-wall-normal Y uniform in 64..128 (multiples of 8), 0..400 spheres of radius 4
-(capped at a 5 % solid fraction), density ratio 1 (the channel's var_inc.f90:29),
-FP32 populations, 200..2000 steps, started from stagnant flow and driven by
-the channel preset's constant force as the reference channel is
-(C/para.f90:20-22).  The collision uses MRTtype 1 (para.f90's rates "for
-stability"): with the channel's default LBGK rates (MRTtype 2) at
-tau = 0.5108 these small channels accelerate to velocities at which the
-flow diverges within ~500 steps, in the CPU oracle as on the GPU.  A request
-whose spheres come to overlap fails with LBM_ERR_OVERLAP, as the reference
-stops (partlib.f90:2634-2646); such failures are counted apart.
+wall-normal Y uniform in 64..128 (multiples of 8), a decaying turbulent
+initial field (lbm_init_spectral: E(k) ~ k^4 exp(-2 (k/4)^2), u_rms 0.03),
+0..400 spheres of radius 4 (drawn as stated, capped at a 25 % solid
+fraction: random placement with the reference's 2-unit gap cannot seat more
+in the smallest grids), density ratio 1 (the channel's var_inc.f90:29),
+FP32 populations, 200..2000 steps, driven by the channel preset's constant
+force (C/para.f90:20-22).  The collision uses MRTtype 1: with the channel's
+own LBGK rates (MRTtype 2) at tau = 0.5108 the solves with spheres diverge
+(measured on GB300: by step 500 at 64^3 with 100 spheres and at
+128 x 96 x 128 with 400, by step 700 at 192 x 128 x 192 with 400), while
+without spheres MRTtype 2 stays stable for 3000 steps and MRTtype 1 is
+stable with spheres for 3000 steps on all three grids.  A request whose
+spheres come to overlap fails with LBM_ERR_OVERLAP, as the reference stops
+(partlib.f90:2634-2646); such failures are counted apart.
 """
 
 from __future__ import annotations
