@@ -194,13 +194,16 @@ def run_device(wl, u, y, steps, warmup, device, want_f=False, variant=None, sums
     return ms, launches, phases, f, parts, variant
 
 
-def kernel_name(variant, fixed=False):
+def kernel_name(variant, fixed=False, integer=False):
     v, st, groups, per_sm = variant
     if v == 3:
         return (f"k_fused_staged_x2 (stream + MRT collide + forcing, FP32 pairs on f32x2; "
                 f"{st} stages, {groups} consumer groups, {per_sm} CTAs/SM)")
     if v == 2:
         return f"k_fused_staged (stream + MRT collide + forcing; {st} stages, {per_sm} CTAs/SM)"
+    if fixed and integer:
+        return ("k_fused_fixed (stream + MRT collide + forcing; direct, populations and forces in "
+                "64-bit fixed point, all-integer collision core)")
     if fixed:
         return ("k_fused_fixed (stream + MRT collide + forcing; direct, populations and forces in "
                 "64-bit fixed point)")
@@ -381,10 +384,11 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=20.0,
                     help="window of the Poisson serving run (0: skip it)")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="requests per second")
-    ap.add_argument("--sums", choices=["fixed", "float", "integer"], default="fixed",
+    ap.add_argument("--sums", choices=["fixed", "float", "integer"], default="integer",
                     help="FP64 collision arithmetic: integer-coefficient moment sums exact in "
-                         "64-bit fixed point (fixed, the default), all in FP64 (float), or the "
-                         "velocity and force products as integer products too (integer)")
+                         "64-bit fixed point with FP64 products (fixed), all in FP64 (float), or "
+                         "the velocity and force products as integer products too (integer, the "
+                         "default)")
     ap.add_argument("--variant", default=None,
                     help="stream+collide kernel as 'variant,stages,groups,ctas_per_sm' "
                          "(default: autotuned on the workload)")
@@ -443,16 +447,25 @@ def main():
     alg_bytes = 2 * 19 * esz * N
     achieved = alg_bytes / (sc_ms / sc_n / 1e3) / 1e9 if sc_n else None
     figs = profile_figures()
-    key = f"fused_{dtype}_{c.nx}" + ("_fx" if dtype == "f64" and args.sums != "float" else "")
+    key = f"fused_{dtype}_{c.nx}" + ({"fixed": "_fx", "integer": "_int"}.get(args.sums, "")
+                                      if dtype == "f64" else "")
     traffic = None
     if key in figs and figs[key].get("dram_bytes_per_node"):
         traffic = figs[key]["dram_bytes_per_node"] * N
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
-            "kernel": kernel_name(variant, dtype == "f64" and args.sums != "float"),
+            "kernel": kernel_name(variant, dtype == "f64" and args.sums != "float",
+                                  args.sums == "integer"),
             "alg_bytes_per_launch": alg_bytes, "peak_source": peak_src}
     fp64 = {}
-    if dtype == "f64" and key in figs and figs[key].get("fp64_flop_per_node") and sc_n:
+    if dtype == "f64" and key in figs and figs[key].get("pipes"):
+        # the all-integer core issues no FP64 instruction: its compute roofline
+        # is the integer pipes, from the ncu capture
+        fp64 = {"fp64_inst_per_node": 0.0, "pipes_pct_of_peak": figs[key]["pipes"],
+                "capture": figs[key].get("capture"),
+                "note": "all-integer collision core: bound by the ALU pipe (fixed-point sums, "
+                        "128-bit products, range tests), not by FP64 or HBM"}
+    elif dtype == "f64" and key in figs and figs[key].get("fp64_flop_per_node") and sc_n:
         import ctypes as C
         peak = C.c_double(0.0)
         rc = capi.lib().lbm_fma_throughput(capi.LBM_PREC_F64, C.byref(peak))

@@ -286,23 +286,22 @@ int lbm_set_variant(lbm_ctx* ctx, int variant, int stages, int groups, int ctas_
 int lbm_get_variant(lbm_ctx* ctx, int* variant, int* stages, int* groups, int* ctas_per_sm);
 /* Arithmetic of the collision in the fused stream + collide kernels.
  * LBM_SUMS_FLOAT: every operation in the populations' precision.
- * LBM_SUMS_FIXED (FP64 contexts, their default): the sums with small integer
- * coefficients of the forward and inverse moment transforms are computed
- * exactly in 64-bit fixed point (2^-58 and 2^-61 resolution), and every
- * product with a rate, velocity or force stays FP64, so results agree with
- * LBM_SUMS_FLOAT to FP64 rounding.  A node whose populations or moments
- * leave the fixed point's range (|f| >= 1/8, scaled moments >= 1/32, not
- * finite) or whose populations are all below 2^-12 takes the FP64 path.
- * GB300 issues FP64 at about 1/32 of its 32-bit integer rate, and these
- * sums are most of the FP64 kernel's instructions.  FP32 contexts accept
- * LBM_SUMS_FLOAT only.  The unfused per-subroutine entries always use
- * LBM_SUMS_FLOAT.
- * LBM_SUMS_INTEGER (FP64 contexts): LBM_SUMS_FIXED with the velocity and
- * force terms as exact 128-bit integer products of fixed-point values too
- * (products rounded once to 2^-64 or 2^-70, each term of a moment once to
- * 2^-61), so the direct kernel issues no FP64 instruction on a node that
- * stays in range (|u| < 1/4, |F| < 2^-9; others take the FP64 path).
- * No counterpart in the reference. */
+ * LBM_SUMS_FIXED (FP64 contexts): the sums with small integer coefficients
+ * of the forward and inverse moment transforms are computed exactly in
+ * 64-bit fixed point (2^-58 and 2^-61 resolution), and every product with a
+ * rate, velocity or force stays FP64, so results agree with LBM_SUMS_FLOAT
+ * to FP64 rounding.  A node whose populations or moments leave the fixed
+ * point's range (|f| >= 1/8, scaled moments >= 1/32, not finite) or whose
+ * populations are all below 2^-12 takes the FP64 path.  GB300 issues FP64 at
+ * about 1/32 of its 32-bit integer rate, and these sums are most of the FP64
+ * kernel's instructions.
+ * LBM_SUMS_INTEGER (FP64 contexts, their default): LBM_SUMS_FIXED with the
+ * velocity and force terms as exact 128-bit integer products of fixed-point
+ * values too (products rounded once to 2^-64 or 2^-70, each term of a moment
+ * once to 2^-61), so the direct kernel issues no FP64 instruction on a node
+ * that stays in range (|u| < 1/4, |F| < 2^-9; others take the FP64 path).
+ * FP32 contexts accept LBM_SUMS_FLOAT only.  The unfused per-subroutine
+ * entries always use LBM_SUMS_FLOAT.  No counterpart in the reference. */
 enum { LBM_SUMS_FLOAT = 0, LBM_SUMS_FIXED = 1, LBM_SUMS_INTEGER = 2 };
 int lbm_set_sums(lbm_ctx* ctx, int mode);
 int lbm_get_sums(lbm_ctx* ctx, int* mode);

@@ -834,7 +834,7 @@ int lbm_create(const lbm_config* cfg, lbm_ctx** out) {
   g.channel = cfg->boundary == LBM_BC_XWALLS;
   g.sw = 4 * ((g.nx + 127) / 128);
   ctx->f32 = cfg->precision == LBM_PREC_F32;
-  ctx->sums = ctx->f32 ? LBM_SUMS_FLOAT : LBM_SUMS_FIXED;
+  ctx->sums = ctx->f32 ? LBM_SUMS_FLOAT : LBM_SUMS_INTEGER;
   ctx->esz = ctx->f32 ? 4 : 8;
   // MRT rates, B/para.f90:91-135
   const double tau = 3.0 * cfg->visc + 0.5;

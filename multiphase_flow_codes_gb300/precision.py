@@ -128,7 +128,7 @@ def error_report(cfg64: capi.lbm_config, u, ypglb: np.ndarray,
     boxes = [LBMBox(cfg64), LBMBox(cfg32)]
     if floor:
         boxes.append(LBMBox(cfg64))
-        boxes[2].set_sums(capi.LBM_SUMS_FLOAT if boxes[0].sums() == capi.LBM_SUMS_FIXED
+        boxes[2].set_sums(capi.LBM_SUMS_FLOAT if boxes[0].sums() != capi.LBM_SUMS_FLOAT
                           else capi.LBM_SUMS_FIXED)
     r_in, r_out = cfg64.rad + 1.0, cfg64.rad + 3.0
     try:

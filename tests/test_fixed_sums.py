@@ -23,11 +23,13 @@ from multiphase_flow_codes_gb300 import inputs
 pytestmark = pytest.mark.gpu
 
 
-def test_fp64_contexts_default_to_fixed_sums(require_gpu):
+def test_fp64_contexts_default_to_integer_sums(require_gpu):
     from multiphase_flow_codes_gb300 import LBMError
     from multiphase_flow_codes_gb300.engine import LBMBox
     cfg = capi.config_init(capi.LBM_PRESET_BOX, 16, 16, 16, 0, 4.0, 1.0)
     box = LBMBox(cfg)
+    assert box.sums() == capi.LBM_SUMS_INTEGER
+    box.set_sums(capi.LBM_SUMS_FIXED)
     assert box.sums() == capi.LBM_SUMS_FIXED
     box.set_sums(capi.LBM_SUMS_FLOAT)
     assert box.sums() == capi.LBM_SUMS_FLOAT
