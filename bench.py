@@ -381,7 +381,7 @@ def main():
                          "('' to skip)")
     ap.add_argument("--batch-steps", type=int, default=500,
                     help="steps of the 48-box batched ensemble (0: skip it)")
-    ap.add_argument("--serve-seconds", type=float, default=20.0,
+    ap.add_argument("--serve-seconds", type=float, default=10.0,
                     help="window of the Poisson serving run (0: skip it)")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="requests per second")
     ap.add_argument("--sums", choices=["fixed", "float", "integer"], default="integer",

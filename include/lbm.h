@@ -396,9 +396,10 @@ int lbm_server_result(lbm_server* server, int64_t id, lbm_result* out);
 /* block until request id is done or failed, at most timeout_s seconds
  * (LBM_ERR_TIMEOUT otherwise) */
 int lbm_server_wait(lbm_server* server, int64_t id, double timeout_s);
-/* out[10]: submitted, done, failed, resident, queued, HBM bytes in use,
+/* out[13]: submitted, done, failed, resident, queued, HBM bytes in use,
  * batch regroupings, chunks advanced, seconds spent advancing, seconds since
- * creation */
+ * creation, and the loop's seconds spent admitting (context set-up),
+ * regrouping and retiring (summaries, context destruction) */
 int lbm_server_stats(lbm_server* server, double* out);
 /* The context of a finished request submitted with keep_state = 1: its
  * final populations, flags and particles, in the engine's axes (walls normal

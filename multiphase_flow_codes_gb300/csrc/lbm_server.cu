@@ -78,6 +78,9 @@ struct lbm_server {
   bool membership_changed = true;
   int64_t rebuilds = 0, chunks = 0, done = 0, failed = 0;
   double busy_s = 0.0;
+  // loop-thread seconds spent admitting (context set-up), regrouping and
+  // retiring (summary and context destruction)
+  double admit_s = 0.0, regroup_s = 0.0, retire_s = 0.0;
 };
 
 namespace {
@@ -151,7 +154,17 @@ int start_job(lbm_server* s, Job* j) {
   return LBM_OK;
 }
 
+double secs_since(Clock::time_point t) {
+  return std::chrono::duration<double>(Clock::now() - t).count();
+}
+
 void admit(lbm_server* s) {
+  const auto t0 = Clock::now();
+  struct Tally {
+    lbm_server* s;
+    Clock::time_point t0;
+    ~Tally() { s->admit_s += secs_since(t0); }
+  } tally{s, t0};
   std::vector<Job*> take;
   {
     std::lock_guard<std::mutex> lk(s->mu);
@@ -184,6 +197,7 @@ void admit(lbm_server* s) {
 
 // batches of phase-compatible FP32 boxes; everything else steps alone
 void regroup(lbm_server* s) {
+  const auto t0 = Clock::now();
   for (lbm_batch* b : s->batches) lbm_batch_destroy(b);
   s->batches.clear();
   s->batch_members.clear();
@@ -228,6 +242,7 @@ void regroup(lbm_server* s) {
   }
   ++s->rebuilds;
   s->membership_changed = false;
+  s->regroup_s += secs_since(t0);
 }
 
 void advance(lbm_server* s) {
@@ -286,6 +301,7 @@ void advance(lbm_server* s) {
   std::vector<Job*> done;
   for (size_t i = 0; i < resident_before && i < s->active.size(); ++i)
     if (s->active[i]->remaining <= 0) done.push_back(s->active[i]);
+  const auto t_retire = Clock::now();
   if (!done.empty() || !finished.empty()) {
     // a finished box leaves its batch before its context goes away
     for (lbm_batch* b : s->batches) lbm_batch_destroy(b);
@@ -300,6 +316,7 @@ void advance(lbm_server* s) {
     for (auto& f : finished) failed |= f.first == j;
     if (!failed) finish(s, j, LBM_OK);
   }
+  s->retire_s += secs_since(t_retire);
 }
 
 void run_loop(lbm_server* s) {
@@ -401,6 +418,9 @@ int lbm_server_stats(lbm_server* s, double* out) {
   out[6] = (double)s->rebuilds;
   out[7] = (double)s->chunks;
   out[8] = s->busy_s;
+  out[10] = s->admit_s;
+  out[11] = s->regroup_s;
+  out[12] = s->retire_s;
   out[9] = now_s(s);
   return LBM_OK;
 }

@@ -128,10 +128,10 @@ class LBMServer:
         return LBMBox.adopt(h)
 
     def stats(self) -> dict:
-        out = (C.c_double * 10)()
+        out = (C.c_double * 13)()
         self._L.lbm_server_stats(self._h, out)
         keys = ("submitted", "done", "failed", "resident", "queued", "hbm_bytes", "regroupings",
-                "chunks", "advance_s", "uptime_s")
+                "chunks", "advance_s", "uptime_s", "admit_s", "regroup_s", "retire_s")
         return dict(zip(keys, list(out)))
 
 
