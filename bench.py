@@ -384,6 +384,8 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=10.0,
                     help="window of the Poisson serving run (0: skip it)")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="requests per second")
+    ap.add_argument("--no-fp64-float", action="store_true",
+                    help="skip the all-FP64 (--sums float) comparison run of the FP64 workload")
     ap.add_argument("--sums", choices=["fixed", "float", "integer"], default="integer",
                     help="FP64 collision arithmetic: integer-coefficient moment sums exact in "
                          "64-bit fixed point with FP64 products (fixed), all in FP64 (float), or "
@@ -505,6 +507,23 @@ def main():
                        "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                        "how": "C ABI: lbm_upload_f (Fortran layout, pinned host) + particles, "
                               f"{args.steps} x (lbm_step + particle read-back), lbm_download_f"}
+
+    # the same FP64 steps with every collision operation and the stored
+    # populations in plain FP64 (no fixed point anywhere), for comparison
+    if dtype == "f64" and args.sums != "float" and not args.no_fp64_float:
+        msf, lf, phf, _, _, vf = run_device(wl, u, y, args.steps, args.warmup, local,
+                                            variant=variant, sums=capi.LBM_SUMS_FLOAT)
+        scf, nf = phf["stream_collide"]
+        achf = alg_bytes / (scf / nf / 1e3) / 1e9 if nf else None
+        ratef, _ = rep.rate(N * args.steps, msf / 1e3)
+        line["fp64_all_float"] = {
+            "value": ratef / 1e6, "unit": "MLUPS", "ms_per_step": msf / args.steps,
+            "roofline": {"bound": "hbm", "achieved": achf, "peak": hbm, "unit": "GB/s",
+                         "frac": (achf / hbm) if achf else None,
+                         "kernel": kernel_name(vf, False, False)},
+            "phase_ms_per_step": {k: (v[0] / args.steps) for k, v in phf.items()},
+            "how": "the workload's steps with LBM_SUMS_FLOAT: FP64 collision arithmetic and FP64 "
+                   "population storage throughout (the reference's own arithmetic)"}
 
     if not args.no_fp32 and dtype == "f64":
         from multiphase_flow_codes_gb300 import config

@@ -215,6 +215,14 @@ int lbm_init_channel(lbm_ctx* ctx);
  * then lbm_upload_particles at rest.  LBM_ERR_OVERLAP if no placement is
  * found in max_rounds rounds (0: 100000). */
 int lbm_init_particles(lbm_ctx* ctx, int npart, int seed, int max_rounds);
+/* The placement of lbm_init_particles without a context or a GPU: initpartpos
+ * (3DBox.../partlib.f90:1-80, 3DChannel.../partlib.f90:10-24) for the grid,
+ * boundary, rad, mingap and mingap_w of cfg; centres into ypglb (3, npart),
+ * the reference's var_inc layout.  LBM_ERR_OVERLAP if no placement is found in
+ * max_rounds rounds (0: 100000).  Host code only: it may be called from any
+ * thread while the GPU runs. */
+int lbm_place_particles(const lbm_config* cfg, int npart, int seed, int max_rounds,
+                        double* ypglb);
 /* Deterministic summary of the current state: out[0] mass (sum f), out[1..3]
  * momentum, out[4] checksum sum_q,n (1 + q/19 + (n mod 97)/97) f, out[5]
  * kinetic energy sum (u.u)/2 of the last macrovar.  Bitwise equal for

@@ -120,6 +120,7 @@ SIGNATURES = {
     "lbm_statistics": (C.c_int, [_P, C.c_int, _D, _D, _D]),
     "lbm_init_spectral": (C.c_int, [_P, C.c_double, C.c_double, C.c_uint64]),
     "lbm_init_particles": (C.c_int, [_P, C.c_int, C.c_int, C.c_int]),
+    "lbm_place_particles": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P]),
     "lbm_init_channel": (C.c_int, [_P]),
     "lbm_summary": (C.c_int, [_P, _D]),
     "lbm_particle_slip": (C.c_int, [_P, C.c_double, C.c_double, _D]),
@@ -183,6 +184,16 @@ def config_init(preset: int, nx: int, ny: int, nz: int, npart: int, rad: float,
     if rc != LBM_OK:
         raise LBMError(rc, "lbm_config_init rejected the arguments")
     return cfg
+
+
+def place_particles(cfg: lbm_config, npart: int, seed: int, max_rounds: int = 0) -> np.ndarray:
+    """initpartpos on the host (lbm_place_particles): centres ``(npart, 3)``."""
+    y = np.zeros((npart, 3), dtype=np.float64)
+    rc = lib().lbm_place_particles(C.byref(cfg), npart, seed, max_rounds,
+                                   y.ctypes.data_as(C.c_void_p))
+    if rc != LBM_OK:
+        raise LBMError(rc, "lbm_place_particles")
+    return y
 
 
 def footprint(cfg: lbm_config) -> int:

@@ -271,42 +271,109 @@ struct Ran1 {
 
 // initpartpos (B/partlib.f90:1-80, C/partlib.f90:10-24): uniform centres,
 // every particle that comes within mingap of a later one drawn again
-// (ovlpchk with istep00 = 0, B/partlib.f90:118-171); y is (3, npart)
+// (ovlpchk with istep00 = 0, B/partlib.f90:118-171); y is (3, npart).
+// Same draws and same overlap flags as the reference's all-pairs test, which
+// this restricts, per round, to the pairs that can have changed: a pair of
+// particles that both kept their place tested clear in the round before, so
+// only a particle drawn again is tested, against the particles in its own
+// and the neighbouring cells of a grid whose cells are at least the overlap
+// distance 2 rad + mingap wide.  Each candidate pair is tested with the
+// reference's own expression (nearest image, distance minus 2 rad + mingap).
+// The cost of a round falls from npart^2 / 2 tests to (particles drawn
+// again) x (neighbours); near the densest packings the algorithm reaches,
+// placements take thousands of rounds with a handful of particles each.
 bool init_particle_positions(const Geometry& g, int npart, double rad, double mingap,
                              double mingap_w, int seed, int max_rounds, double* y) {
   Ran1 rng(seed);
-  std::vector<int> flag(npart, 1);
   const double radpgap = rad + mingap_w;
   auto near = [](double c, double p, int n, int nh) {
     if (c - p > nh) c -= n;
     if (c - p < -nh) c += n;
     return c;
   };
+  // the reference's test of particle a against a later particle b
+  auto overlap = [&](int a, int b) {
+    const double xc = y[3 * a], yc = y[3 * a + 1], zc = y[3 * a + 2];
+    double xb = y[3 * b], yb = y[3 * b + 1], zb = y[3 * b + 2];
+    if (!g.channel) xb = near(xb, xc, g.nx, g.nxh);
+    yb = near(yb, yc, g.ny, g.nyh);
+    zb = near(zb, zc, g.nz, g.nzh);
+    const double dx = xc - xb, dy = yc - yb, dz = zc - zb;
+    return std::sqrt(dx * dx + dy * dy + dz * dz) - 2.0 * rad - mingap < 0.0;
+  };
+  const int ext[3] = {g.nx, g.ny, g.nz};
+  const bool periodic[3] = {!g.channel, true, true};
+  const double cut = 2.0 * rad + mingap;
+  int nc[3];
+  double inv[3];
+  for (int a = 0; a < 3; ++a) {
+    // cells of at least the overlap distance (with a margin for its
+    // rounding); with fewer than three cells on an axis the neighbours
+    // would coincide, so that axis has one cell
+    int c = cut > 0.0 ? (int)std::floor((double)ext[a] / (cut * 1.0001)) : 1;
+    if (c < 3) c = 1;
+    nc[a] = c;
+    inv[a] = (double)c / (double)ext[a];
+  }
+  auto coord = [&](int i, int a) {
+    const int k = (int)(y[3 * i + a] * inv[a]);
+    return k < 0 ? 0 : (k >= nc[a] ? nc[a] - 1 : k);
+  };
+  auto cell_of = [&](int i) { return coord(i, 0) + nc[0] * (coord(i, 1) + nc[1] * coord(i, 2)); };
+  std::vector<std::vector<int>> members((size_t)nc[0] * nc[1] * nc[2]);
+  std::vector<int> cell(npart, -1), moved, flagged;
+  std::vector<char> is_moved(npart, 0), flag(npart, 0);
+  for (int i = 0; i < npart; ++i) moved.push_back(i);
   for (int round = 0; round < max_rounds; ++round) {
-    for (int ip = 0; ip < npart; ++ip) {
-      if (!flag[ip]) continue;
+    for (int ip : moved) {  // in index order, as the reference draws
       y[3 * ip] = g.channel ? radpgap + ((double)g.nx - 2.0 * radpgap) * rng() : (double)g.nx * rng();
       y[3 * ip + 1] = (double)g.ny * rng();
       y[3 * ip + 2] = (double)g.nz * rng();
+      const int c = cell_of(ip);
+      if (c != cell[ip]) {
+        if (cell[ip] >= 0) {
+          std::vector<int>& v = members[cell[ip]];
+          v.erase(std::find(v.begin(), v.end(), ip));
+        }
+        members[c].push_back(ip);
+        cell[ip] = c;
+      }
+      is_moved[ip] = 1;
     }
-    std::fill(flag.begin(), flag.end(), 0);
-    bool any = false;
-    for (int a = 0; a + 1 < npart; ++a) {
-      const double xc = y[3 * a], yc = y[3 * a + 1], zc = y[3 * a + 2];
-      for (int b = a + 1; b < npart; ++b) {
-        double xb = y[3 * b], yb = y[3 * b + 1], zb = y[3 * b + 2];
-        if (!g.channel) xb = near(xb, xc, g.nx, g.nxh);
-        yb = near(yb, yc, g.ny, g.nyh);
-        zb = near(zb, zc, g.nz, g.nzh);
-        const double dx = xc - xb, dy = yc - yb, dz = zc - zb;
-        if (std::sqrt(dx * dx + dy * dy + dz * dz) - 2.0 * rad - mingap < 0.0) {
-          flag[a] = 1;
-          any = true;
-          break;
+    flagged.clear();
+    for (int r : moved) {
+      int nb[3][3], nn[3];
+      for (int a = 0; a < 3; ++a) {
+        nn[a] = 0;
+        const int cr = coord(r, a);
+        if (nc[a] == 1) {
+          nb[a][nn[a]++] = 0;
+          continue;
+        }
+        for (int d = -1; d <= 1; ++d) {
+          int c = cr + d;
+          if (periodic[a]) c = (c + nc[a]) % nc[a];
+          else if (c < 0 || c >= nc[a]) continue;
+          nb[a][nn[a]++] = c;
         }
       }
+      for (int iz = 0; iz < nn[2]; ++iz)
+        for (int iy = 0; iy < nn[1]; ++iy)
+          for (int ix = 0; ix < nn[0]; ++ix)
+            for (int q : members[nb[0][ix] + nc[0] * (nb[1][iy] + nc[1] * nb[2][iz])]) {
+              if (q == r || (is_moved[q] && q < r)) continue;  // each pair once
+              const int a = q < r ? q : r, b = q < r ? r : q;
+              if (!flag[a] && overlap(a, b)) {
+                flag[a] = 1;
+                flagged.push_back(a);
+              }
+            }
     }
-    if (!any) return true;
+    for (int r : moved) is_moved[r] = 0;
+    std::sort(flagged.begin(), flagged.end());
+    for (int a : flagged) flag[a] = 0;
+    moved.swap(flagged);
+    if (moved.empty()) return true;
   }
   return false;
 }
@@ -1182,6 +1249,22 @@ int lbm_init_channel(lbm_ctx* ctx) {
     return fail(ctx, rc, "init_channel: launch failed");
   }
   return initpop_device(ctx, dv);
+}
+
+int lbm_place_particles(const lbm_config* cfg, int npart, int seed, int max_rounds,
+                        double* ypglb) {
+  if (!cfg || npart < 0 || (npart > 0 && !ypglb)) return LBM_ERR_ARG;
+  if (cfg->nx < 1 || cfg->ny < 1 || cfg->nz < 1 || (npart > 0 && !(cfg->rad > 0.0)))
+    return LBM_ERR_ARG;
+  Geometry g{};
+  g.nx = cfg->nx; g.ny = cfg->ny; g.nz = cfg->nz;
+  g.nxh = g.nx / 2; g.nyh = g.ny / 2; g.nzh = g.nz / 2;
+  g.channel = cfg->boundary == LBM_BC_XWALLS;
+  if (npart > 0 &&
+      !init_particle_positions(g, npart, cfg->rad, cfg->mingap, cfg->mingap_w, seed,
+                               max_rounds > 0 ? max_rounds : 100000, ypglb))
+    return LBM_ERR_OVERLAP;
+  return LBM_OK;
 }
 
 int lbm_init_particles(lbm_ctx* ctx, int npart, int seed, int max_rounds) {

@@ -9,9 +9,9 @@ reports throughput and latency percentiles.
 The channel workload: grid X x Y x Z with X, Z uniform in 64..192 and the
 wall-normal Y uniform in 64..128 (multiples of 8), a decaying turbulent
 initial field (lbm_init_spectral: E(k) ~ k^4 exp(-2 (k/4)^2), u_rms 0.03),
-0..400 spheres of radius 4 (drawn as stated, capped at a 25 % solid
-fraction: random placement with the reference's 2-unit gap cannot seat more
-in the smallest grids), density ratio 1 (the channel's var_inc.f90:29),
+0..400 spheres of radius 4 (drawn as stated, capped at a 15 % solid
+fraction: the reference's random placement with its 2-unit gap cannot seat
+more in the smaller grids), density ratio 1 (the channel's var_inc.f90:29),
 FP32 populations, 200..2000 steps, driven by the channel preset's constant
 force (C/para.f90:20-22).  The collision uses MRTtype 1: with the channel's
 own LBGK rates (MRTtype 2) at tau = 0.5108 the solves with spheres diverge
@@ -55,10 +55,13 @@ class lbm_result(C.Structure):
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
 
 # The workload's "0 to 400 spheres of radius 4" is drawn as stated and capped
-# at this solid fraction: random sequential placement with the reference's
-# 2-unit gap (initpartpos) cannot seat 400 spheres in the smallest grids
-# (64 x 64 x 64 holds about 160 at 25 %).
-MAX_SOLID_FRACTION = 0.25
+# at this solid fraction.  initpartpos draws every sphere that overlaps a
+# later one again until none does; with the 2-unit gap that process stops
+# finding placements near 15 % solid in these grids (of 400 requests capped
+# at 25 %, 9 still had no placement after the reference's 100000 rounds,
+# e.g. 64 x 80 x 72 with 226 spheres, 16.4 %; capped at 15 % all 400 place,
+# the slowest in 24000 rounds).
+MAX_SOLID_FRACTION = 0.15
 # MRT rates of the served channels (0: the channel preset's MRTtype 2, LBGK)
 SERVING_MRT = 1
 
