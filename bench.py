@@ -151,12 +151,14 @@ def initial_f(u):
     return f
 
 
-def run_device(wl, u, y, steps, warmup, device, want_f=False, variant=None, sums=None):
+def run_device(wl, u, y, steps, warmup, device, want_f=False, variant=None, sums=None,
+               overlap=True):
     """Device-resident timing of `steps` C-ABI step calls."""
     import torch
     from multiphase_flow_codes_gb300 import _capi as capi
     from multiphase_flow_codes_gb300.engine import LBMBox
     box = LBMBox(wl.cfg)
+    box.set_overlap(overlap)
     if sums is not None and wl.cfg.precision == capi.LBM_PREC_F64:
         box.set_sums(sums)
     stream = torch.cuda.Stream(device=device)
@@ -194,6 +196,19 @@ def run_device(wl, u, y, steps, warmup, device, want_f=False, variant=None, sums
     return ms, launches, phases, f, parts, variant
 
 
+def sc_achieved(phases, alg_bytes):
+    """Algorithmic GB/s of the stream + collide kernel from the per-phase
+    CUDA-event times.  With the overlap of the particle phases, a step's
+    stream + collide is two launches (the far nodes, beside the previous
+    step's particle kernels on their own stream, then the near segments): the
+    step's bytes over the sum of the two launches' durations."""
+    sc_ms, sc_n = phases["stream_collide"]
+    far_ms, _ = phases.get("stream_collide_far", (0.0, 0))
+    if not sc_n:
+        return None
+    return alg_bytes * sc_n / ((sc_ms + far_ms) / 1e3) / 1e9
+
+
 def kernel_name(variant, fixed=False, integer=False):
     v, st, groups, per_sm = variant
     if v == 3:
@@ -210,12 +225,13 @@ def kernel_name(variant, fixed=False, integer=False):
     return "k_fused (stream + MRT collide + forcing; direct)"
 
 
-def run_e2e(wl, f0_fortran, y, steps, device, variant=None, sums=None):
+def run_e2e(wl, f0_fortran, y, steps, device, variant=None, sums=None, overlap=True):
     """End to end through the C ABI with host buffers (see module doc)."""
     import torch
     from multiphase_flow_codes_gb300 import _capi as capi
     from multiphase_flow_codes_gb300.engine import LBMBox
     box = LBMBox(wl.cfg)
+    box.set_overlap(overlap)
     if sums is not None and wl.cfg.precision == capi.LBM_PREC_F64:
         box.set_sums(sums)
     if variant is not None:
@@ -381,9 +397,16 @@ def main():
                          "('' to skip)")
     ap.add_argument("--batch-steps", type=int, default=500,
                     help="steps of the 48-box batched ensemble (0: skip it)")
-    ap.add_argument("--serve-seconds", type=float, default=10.0,
+    ap.add_argument("--serve-seconds", type=float, default=30.0,
                     help="window of the Poisson serving run (0: skip it)")
-    ap.add_argument("--serve-rate", type=float, default=20.0, help="requests per second")
+    ap.add_argument("--serve-rate", type=float, default=6.0,
+                    help="requests per second (6: the highest rate measured with a flat p99 "
+                         "over 600 s; 20: the overload case)")
+    ap.add_argument("--serve-window", type=float, default=10.0,
+                    help="seconds per latency window of the serving run")
+    ap.add_argument("--no-overlap", action="store_true",
+                    help="FP64: run each step's stream + collide whole, after the previous "
+                         "step's particle phases (lbm_set_overlap 0)")
     ap.add_argument("--no-fp64-float", action="store_true",
                     help="skip the all-FP64 (--sums float) comparison run of the FP64 workload")
     ap.add_argument("--sums", choices=["fixed", "float", "integer"], default="integer",
@@ -435,7 +458,7 @@ def main():
             "integer": capi.LBM_SUMS_INTEGER}[args.sums]
     ms, launches, phases, f64, p64, variant = run_device(wl, u, y, args.steps, args.warmup, local,
                                                          want_f=not args.no_fp32, variant=fixed,
-                                                         sums=sums)
+                                                         sums=sums, overlap=not args.no_overlap)
     clocks = sampler.stop()
     rate, t_s = rep.rate(N * args.steps, ms / 1e3)
     t_ms = t_s * 1e3
@@ -445,9 +468,8 @@ def main():
     hbm = float(peaks.get("hbm_gbs", HBM_FALLBACK))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     esz = 8 if dtype == "f64" else 4
-    sc_ms, sc_n = phases["stream_collide"]
     alg_bytes = 2 * 19 * esz * N
-    achieved = alg_bytes / (sc_ms / sc_n / 1e3) / 1e9 if sc_n else None
+    achieved = sc_achieved(phases, alg_bytes)
     figs = profile_figures()
     key = f"fused_{dtype}_{c.nx}" + ({"fixed": "_fx", "integer": "_int"}.get(args.sums, "")
                                       if dtype == "f64" else "")
@@ -501,7 +523,8 @@ def main():
         f0 = initial_f(u)
         f0_fortran = np.asfortranarray(np.transpose(f0, (0, 3, 2, 1)))
         del f0
-        e_ms, h2d, d2h = run_e2e(wl, f0_fortran, y, args.steps, local, variant, sums)
+        e_ms, h2d, d2h = run_e2e(wl, f0_fortran, y, args.steps, local, variant, sums,
+                                 overlap=not args.no_overlap)
         e_rate, _ = rep.rate(N * args.steps, e_ms / 1e3)
         line["e2e"] = {"value": e_rate / 1e6, "unit": "MLUPS",
                        "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
@@ -513,8 +536,7 @@ def main():
     if dtype == "f64" and args.sums != "float" and not args.no_fp64_float:
         msf, lf, phf, _, _, vf = run_device(wl, u, y, args.steps, args.warmup, local,
                                             variant=variant, sums=capi.LBM_SUMS_FLOAT)
-        scf, nf = phf["stream_collide"]
-        achf = alg_bytes / (scf / nf / 1e3) / 1e9 if nf else None
+        achf = sc_achieved(phf, alg_bytes)
         ratef, _ = rep.rate(N * args.steps, msf / 1e3)
         line["fp64_all_float"] = {
             "value": ratef / 1e6, "unit": "MLUPS", "ms_per_step": msf / args.steps,
@@ -531,8 +553,7 @@ def main():
         if wl32.cfg.precision != capi.LBM_PREC_F32:
             wl32.cfg.precision = capi.LBM_PREC_F32
         ms32, l32, ph32, f32, p32, variant32 = run_device(wl32, u, y, args.steps, args.warmup, local, want_f=True)
-        sc32, n32 = ph32["stream_collide"]
-        ach32 = 2 * 19 * 4 * N / (sc32 / n32 / 1e3) / 1e9 if n32 else None
+        ach32 = sc_achieved(ph32, 2 * 19 * 4 * N)
         err = float(np.abs(f32 - f64).max() / np.abs(f64).max())
         ferr = None
         if p64 is not None and p32 is not None and wl.npart:
@@ -569,7 +590,8 @@ def main():
 
     if args.serve_seconds > 0 and rank == 0 and args.workload == "box256_p1000_f64":
         from multiphase_flow_codes_gb300 import serving
-        sv = serving.poisson_run(rate=args.serve_rate, duration=args.serve_seconds)
+        sv = serving.poisson_run(rate=args.serve_rate, duration=args.serve_seconds,
+                                 window=args.serve_window)
         sv["how"] = ("native lbm_server loop: Poisson arrivals, admission by lbm_footprint within a "
                      "96 GiB budget, up to 96 resident solves, continuous batching of the FP32 channel "
                      "solves into batched stream+collide launches, 50-step chunks; latency = done - "
