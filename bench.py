@@ -151,14 +151,12 @@ def initial_f(u):
     return f
 
 
-def run_device(wl, u, y, steps, warmup, device, want_f=False, variant=None, sums=None,
-               overlap=True):
+def run_device(wl, u, y, steps, warmup, device, want_f=False, variant=None, sums=None):
     """Device-resident timing of `steps` C-ABI step calls."""
     import torch
     from multiphase_flow_codes_gb300 import _capi as capi
     from multiphase_flow_codes_gb300.engine import LBMBox
     box = LBMBox(wl.cfg)
-    box.set_overlap(overlap)
     if sums is not None and wl.cfg.precision == capi.LBM_PREC_F64:
         box.set_sums(sums)
     stream = torch.cuda.Stream(device=device)
@@ -197,16 +195,12 @@ def run_device(wl, u, y, steps, warmup, device, want_f=False, variant=None, sums
 
 
 def sc_achieved(phases, alg_bytes):
-    """Algorithmic GB/s of the stream + collide kernel from the per-phase
-    CUDA-event times.  With the overlap of the particle phases, a step's
-    stream + collide is two launches (the far nodes, beside the previous
-    step's particle kernels on their own stream, then the near segments): the
-    step's bytes over the sum of the two launches' durations."""
+    """Algorithmic GB/s of the stream + collide kernel: its bytes per launch
+    over the mean CUDA-event duration of its launches in the timed region."""
     sc_ms, sc_n = phases["stream_collide"]
-    far_ms, _ = phases.get("stream_collide_far", (0.0, 0))
     if not sc_n:
         return None
-    return alg_bytes * sc_n / ((sc_ms + far_ms) / 1e3) / 1e9
+    return alg_bytes / (sc_ms / sc_n / 1e3) / 1e9
 
 
 def kernel_name(variant, fixed=False, integer=False):
@@ -225,13 +219,12 @@ def kernel_name(variant, fixed=False, integer=False):
     return "k_fused (stream + MRT collide + forcing; direct)"
 
 
-def run_e2e(wl, f0_fortran, y, steps, device, variant=None, sums=None, overlap=True):
+def run_e2e(wl, f0_fortran, y, steps, device, variant=None, sums=None):
     """End to end through the C ABI with host buffers (see module doc)."""
     import torch
     from multiphase_flow_codes_gb300 import _capi as capi
     from multiphase_flow_codes_gb300.engine import LBMBox
     box = LBMBox(wl.cfg)
-    box.set_overlap(overlap)
     if sums is not None and wl.cfg.precision == capi.LBM_PREC_F64:
         box.set_sums(sums)
     if variant is not None:
@@ -404,9 +397,6 @@ def main():
                          "over 600 s; 20: the overload case)")
     ap.add_argument("--serve-window", type=float, default=10.0,
                     help="seconds per latency window of the serving run")
-    ap.add_argument("--no-overlap", action="store_true",
-                    help="FP64: run each step's stream + collide whole, after the previous "
-                         "step's particle phases (lbm_set_overlap 0)")
     ap.add_argument("--no-fp64-float", action="store_true",
                     help="skip the all-FP64 (--sums float) comparison run of the FP64 workload")
     ap.add_argument("--sums", choices=["fixed", "float", "integer"], default="integer",
@@ -458,7 +448,7 @@ def main():
             "integer": capi.LBM_SUMS_INTEGER}[args.sums]
     ms, launches, phases, f64, p64, variant = run_device(wl, u, y, args.steps, args.warmup, local,
                                                          want_f=not args.no_fp32, variant=fixed,
-                                                         sums=sums, overlap=not args.no_overlap)
+                                                         sums=sums)
     clocks = sampler.stop()
     rate, t_s = rep.rate(N * args.steps, ms / 1e3)
     t_ms = t_s * 1e3
@@ -523,8 +513,7 @@ def main():
         f0 = initial_f(u)
         f0_fortran = np.asfortranarray(np.transpose(f0, (0, 3, 2, 1)))
         del f0
-        e_ms, h2d, d2h = run_e2e(wl, f0_fortran, y, args.steps, local, variant, sums,
-                                 overlap=not args.no_overlap)
+        e_ms, h2d, d2h = run_e2e(wl, f0_fortran, y, args.steps, local, variant, sums)
         e_rate, _ = rep.rate(N * args.steps, e_ms / 1e3)
         line["e2e"] = {"value": e_rate / 1e6, "unit": "MLUPS",
                        "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
