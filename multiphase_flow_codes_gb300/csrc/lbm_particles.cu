@@ -665,11 +665,12 @@ __device__ __forceinline__ T read_post(const Geometry& g, const T* f, int pushed
   return ld_pop(g, f, q * N + it + g.nx * (jt + g.ny * kt));
 }
 
-// threads per particle block of the bounce-back: FP64 links are FP64-pipe
-// bound, and 128 threads leave fewer idle lanes in the last pass over a
-// particle's ~1000 links than 256
+// threads per particle block of the bounce-back: 128 threads leave fewer
+// idle lanes in the last pass over a particle's ~1000 links than 256, and
+// eight such blocks fit an SM (the batched kernel uses the same count, so a
+// box's force sums run in the same order alone and in a batch)
 template <typename T>
-constexpr int bounce_threads() { return sizeof(T) == 8 ? 128 : PB; }
+constexpr int bounce_threads() { return 128; }
 
 // beads_collision for one particle per block of NT threads: every link
 // computes the bounced population f9 (stored per link) and its momentum
@@ -887,9 +888,9 @@ __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, Partic
   }
 }
 template <typename T>
-// (64 registers: FP64 eight 128-thread blocks per SM, FP32 four 256-thread
-// blocks, so that the 1000 particle blocks of the workload take fewer waves)
-__global__ void __launch_bounds__(bounce_threads<T>(), (sizeof(T) == 8 ? 8 : 4)) k_bounce(Geometry g, ParticleView pv, const T* f, int pushed,
+// (64 registers: eight 128-thread blocks per SM, so that the 1000 particle
+// blocks of the workload take one wave)
+__global__ void __launch_bounds__(bounce_threads<T>(), 8) k_bounce(Geometry g, ParticleView pv, const T* f, int pushed,
                                                const int32_t* __restrict__ isnodes, LinkSlab ls,
                                                double* fHIp, double* torqp) {
   k_bounce_body<T, bounce_threads<T>()>(blockIdx.x, gridDim.x, g, pv, f, pushed, isnodes, ls, fHIp, torqp);
@@ -1516,9 +1517,10 @@ namespace {
   const int nblk = (nblocks_expr);                   \
   if ((int)blockIdx.x >= nblk) return;
 
-__global__ void __launch_bounds__(PB, 4) k_bounce_multi(const BoxParticles* boxes) {
+__global__ void __launch_bounds__(bounce_threads<float>(), 8) k_bounce_multi(const BoxParticles* boxes) {
   BOX_OR_RETURN(B.pv.npart)
-  k_bounce_body<float, PB>(blockIdx.x, nblk, B.g, B.pv, B.f, 1, B.flags_cur, B.ls, B.ms.fHIp, B.ms.torqp);
+  k_bounce_body<float, bounce_threads<float>()>(blockIdx.x, nblk, B.g, B.pv, B.f, 1, B.flags_cur, B.ls,
+                                                B.ms.fHIp, B.ms.torqp);
 }
 __global__ void __launch_bounds__(PB) k_bounce_store_multi(const BoxParticles* boxes) {
   BOX_OR_RETURN(B.pv.npart)
@@ -1580,7 +1582,7 @@ void launch_particle_step_multi(const BoxParticles* boxes, int nb, int max_npart
                                 long long max_reset, cudaStream_t s) {
   if (nb <= 0 || max_npart <= 0) return;
   auto grid = [&](long long blocks) { return dim3((unsigned)(blocks > 0 ? blocks : 1), nb); };
-  k_bounce_multi<<<grid(max_npart), PB, 0, s>>>(boxes); count_launch();
+  k_bounce_multi<<<grid(max_npart), bounce_threads<float>(), 0, s>>>(boxes); count_launch();
   k_bounce_store_multi<<<grid(max_npart), PB, 0, s>>>(boxes); count_launch();
   k_lubforce_multi<<<grid((max_npart * 32 + 127) / 128), 128, 0, s>>>(boxes); count_launch();
   k_move_wrap_multi<<<grid((max_npart + kSmallBlock - 1) / kSmallBlock), kSmallBlock, 0, s>>>(boxes); count_launch();
