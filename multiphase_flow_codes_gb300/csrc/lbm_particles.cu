@@ -238,6 +238,22 @@ __global__ void k_link_sweeps(Geometry g, ParticleView pv, LinkSlab ls) {
   k_link_sweeps_body(blockIdx.x, gridDim.x, g, pv, ls);
 }
 
+// The reference's FP64 tests of beads_links (partlib.f90:990, 1012), taken
+// where the FP32 test is within kDecide of the boundary (rarely).  Out of
+// line, so that the compiler keeps them behind their branches: this GPU
+// issues FP64 at 2 lanes per clock per SM, and an FP64 instruction costs a
+// warp the same whatever its active lanes.  (i, j, k) 1-based, node at
+// (i - 1/2, j - 1/2, k - 1/2); the reference's "+ 0.0" offsets are exact
+// no-ops here (the point coordinates are positive, and only squares follow).
+__device__ __noinline__ bool inside_fp64(int i, int j, int k, double xc, double yc, double zc,
+                                         double rad2) {
+  const double xx = ((double)i - 0.5) - xc;
+  const double yy = ((double)j - 0.5) - yc;
+  const double zz = ((double)k - 0.5) - zc;
+  const double rr = xx * xx + yy * yy + zz * zz;
+  return (rr - rad2) <= 0.0;
+}
+
 __device__ __forceinline__ void k_links_body(int bx, int gx, Geometry g, ParticleView pv, int32_t* isnodes,
                                               LinkSlab ls, DevStatus* st, int alpha_fp32) {
   using Scan = cub::BlockScan<int, PB>;
@@ -259,21 +275,29 @@ __device__ __forceinline__ void k_links_body(int bx, int gx, Geometry g, Particl
 
   const int p = bx;
   if (p >= pv.npart) return;
-  const double rad = pv.rad;
-  const double radp2 = rad * 1.0 + 2.0;
-  const double rad2 = (rad * 1.0) * (rad * 1.0);
-  const float rad2f = (float)rad2;
-  // only nodes within rad + sqrt(2) of the centre can be solid or own a link
-  const float reachf = (float)((rad + 1.5) * (rad + 1.5)) + 0.05f;
   const bool channel = g.channel != 0;
-  const double x0 = pv.ypglb[3 * p] * 1.0, y0 = pv.ypglb[3 * p + 1] * 1.0,
-               z0 = pv.ypglb[3 * p + 2] * 1.0;
   const int tid = threadIdx.x;
-
+  // the block's FP64 constants, formed once (by thread 0) rather than by
+  // every warp: FP64 instructions are the scarce issue slots of this GPU
+  __shared__ double s_par[5];  // radp2, rad2, x0, y0, z0
+  __shared__ float s_parf[2];  // rad2 and the squared reach in FP32
+  __shared__ int s_finite;
   if (tid == 0) {
     nplanes = 0; nrows = 0; base = 0; fixed_ok = 1; nnear = 0;
+    const double rad = pv.rad;
+    s_par[0] = rad * 1.0 + 2.0;
+    s_par[1] = (rad * 1.0) * (rad * 1.0);
+    s_parf[0] = (float)s_par[1];
+    // only nodes within rad + sqrt(2) of the centre can be solid or own a link
+    s_parf[1] = (float)((rad + 1.5) * (rad + 1.5)) + 0.05f;
+    for (int a = 0; a < 3; ++a) s_par[2 + a] = pv.ypglb[3 * p + a] * 1.0;
+    s_finite = isfinite(s_par[2]) && isfinite(s_par[3]) && isfinite(s_par[4]);
   }
-  if (!(isfinite(x0) && isfinite(y0) && isfinite(z0))) {
+  __syncthreads();
+  const double radp2 = s_par[0], rad2 = s_par[1];
+  const float rad2f = s_parf[0], reachf = s_parf[1];
+  const double x0 = s_par[2], y0 = s_par[3], z0 = s_par[4];
+  if (!s_finite) {
     if (tid == 0) {
       ls.count[p] = 0;
       raise_error(st, LBM_ERR_NONFINITE, p);
@@ -324,7 +348,7 @@ __device__ __forceinline__ void k_links_body(int bx, int gx, Geometry g, Particl
     if (t < tz) {
       k = cz.at(t);
       zc = sweep_value(sev[6], k);
-      double zpnt = (double)k - 0.5 + 0.0;
+      double zpnt = (double)k - 0.5;
       double zz0 = zpnt - zc;
       take = fabs(zz0) <= radp2;
     }
@@ -351,8 +375,8 @@ __device__ __forceinline__ void k_links_body(int bx, int gx, Geometry g, Particl
       k = plane_k[pi];
       zc = plane_z[pi];
       yc = yval[min(pi, 2)][c];
-      zz0 = ((double)k - 0.5 + 0.0) - zc;
-      yy0 = ((double)j - 0.5 + 0.0) - yc;
+      zz0 = ((double)k - 0.5) - zc;
+      yy0 = ((double)j - 0.5) - yc;
       take = channel ? (sqrt(yy0 * yy0 + zz0 * zz0) <= radp2) : (fabs(yy0) <= radp2);
     }
     int pos, tot;
@@ -382,13 +406,8 @@ __device__ __forceinline__ void k_links_body(int bx, int gx, Geometry g, Particl
     const float d0 = rr0f - rad2f;
     if (d0 < -kDecide) return 1;
     if (d0 > kDecide) return 2;
-    const double xc = xval[min(r, 2)][ci], yc = row_y[r], zc = row_z[r];
-    const int j = row_j[r], k = row_k[r];
-    double xx0 = ((double)i - 0.5) - xc;
-    double yy0 = ((double)j - 0.5 + 0.0) - yc;
-    double zz0 = ((double)k - 0.5 + 0.0) - zc;
-    double rr0 = xx0 * xx0 + yy0 * yy0 + zz0 * zz0;
-    return (rr0 - rad2) <= 0.0 ? 1 : 2;
+    return inside_fp64(i, row_j[r], row_k[r], xval[min(r, 2)][ci], row_y[r], row_z[r], rad2) ? 1
+                                                                                             : 2;
   };
   for (int r0 = 0; r0 < nrows; r0 += PB) {
     const int r = r0 + tid;
@@ -464,15 +483,9 @@ __device__ __forceinline__ void k_links_body(int bx, int gx, Geometry g, Particl
         bool link;
         if (d1 < -kDecide) link = true;
         else if (d1 > kDecide) link = false;
-        else {
-          const int j = row_j[r], k = row_k[r];
-          const double xc = xval[min(r, 2)][ci], yc = row_y[r], zc = row_z[r];
-          double xx1 = (double)(i + cix(ipop)) - 0.5 - xc;
-          double yy1 = (double)(j + ciy(ipop)) - 0.5 - yc + 0.0;
-          double zz1 = (double)(k + ciz(ipop)) - 0.5 - zc + 0.0;
-          double rr1 = xx1 * xx1 + yy1 * yy1 + zz1 * zz1;
-          link = (rr1 - rad2) <= 0.0;
-        }
+        else
+          link = inside_fp64(i + cix(ipop), row_j[r] + ciy(ipop), row_k[r] + ciz(ipop),
+                             xval[min(r, 2)][ci], row_y[r], row_z[r], rad2);
         if (link) mask |= 1u << ipop;
       }
     }
@@ -692,9 +705,24 @@ __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, Partic
   // compensated (FP32) or plain FP64, the block sums are FP64
   using R = T;
   Acc<T> acc6[6];
-  const R w1 = R(pv.wp[3 * p]), w2 = R(pv.wp[3 * p + 1]), w3 = R(pv.wp[3 * p + 2]);
-  const R omg1 = R(pv.omgp[3 * p]), omg2 = R(pv.omgp[3 * p + 1]), omg3 = R(pv.omgp[3 * p + 2]);
-  const R xc0 = R(pv.ypglb[3 * p]), yc0 = R(pv.ypglb[3 * p + 1]), zc0 = R(pv.ypglb[3 * p + 2]);
+  // the particle's velocities in the arithmetic precision and the first
+  // tabulated coordinate per axis, formed once by thread 0 (conversions and
+  // roundings of FP64 values issue on the FP64 pipe, and cost a warp the same
+  // whatever its active lanes)
+  __shared__ R s_wo[6];
+  __shared__ int s_lo[3];
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      s_wo[a] = R(pv.wp[3 * p + a]);
+      s_wo[3 + a] = R(pv.omgp[3 * p + a]);
+      s_lo[a] = (int)floor((double)pv.ypglb[3 * p + a]) - (kBounceSpan / 2);
+    }
+  }
+  __syncthreads();
+  const R w1 = s_wo[0], w2 = s_wo[1], w3 = s_wo[2];
+  const R omg1 = s_wo[3], omg2 = s_wo[4], omg3 = s_wo[5];
+  const R xc0 = R(0), yc0 = R(0), zc0 = R(0);  // (unused by delta)
   const bool channel = g.channel != 0;
   const uint32_t* mask = solid_mask(isnodes, g);
   // Per axis, the offset d = pnt - c of the link point pnt = i + 1/2 from the
@@ -706,9 +734,7 @@ __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, Partic
   __shared__ R tcw[NPOP];
   // c_a v with c_a in {-1, 0, 1}: exact, so selected rather than multiplied
   auto sel = [](int c, R v) { return c == 0 ? R(0) : flip_if(c < 0, v); };
-  int lo[3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) lo[a] = (int)floor((double)pv.ypglb[3 * p + a]) - (kBounceSpan / 2);
+  const int lo[3] = {s_lo[0], s_lo[1], s_lo[2]};
   {
     // selects rather than arrays indexed by a, which would live in local memory
     for (int t = threadIdx.x; t < 3 * kBounceSpan; t += NT) {
@@ -1167,13 +1193,24 @@ __device__ __forceinline__ void k_fill_detect_body(int bx, int gx, Geometry g, P
   const int id = bx;
   if (id >= pv.npart) return;
   const bool channel = g.channel != 0;
-  const double cx0 = ypglbp[3 * id], cy0 = ypglbp[3 * id + 1], cz0 = ypglbp[3 * id + 2];
-  if (!(isfinite(cx0) && isfinite(cy0) && isfinite(cz0))) return;
   // bounding box of the nodes covered at the previous step (0-based node i
-  // has centre i + 0.5)
-  const int r = (int)ceil(pp.rad) + 2;
-  const int bx0 = (int)floor(cx0 - 0.5) - r, by0 = (int)floor(cy0 - 0.5) - r,
-            bz0 = (int)floor(cz0 - 0.5) - r;
+  // has centre i + 0.5), formed once by thread 0 (FP64 instructions cost a
+  // warp the same whatever its active lanes)
+  __shared__ int s_box[5];  // finite, r, bx0, by0, bz0
+  if (threadIdx.x == 0) {
+    const double cx0 = ypglbp[3 * id], cy0 = ypglbp[3 * id + 1], cz0 = ypglbp[3 * id + 2];
+    s_box[0] = isfinite(cx0) && isfinite(cy0) && isfinite(cz0);
+    if (s_box[0]) {
+      const int r = (int)ceil(pp.rad) + 2;
+      s_box[1] = r;
+      s_box[2] = (int)floor(cx0 - 0.5) - r;
+      s_box[3] = (int)floor(cy0 - 0.5) - r;
+      s_box[4] = (int)floor(cz0 - 0.5) - r;
+    }
+  }
+  __syncthreads();
+  if (!s_box[0]) return;
+  const int r = s_box[1], bx0 = s_box[2], by0 = s_box[3], bz0 = s_box[4];
   const int w = 2 * r + 2;
   const int wx = min(w, g.nx), wy = min(w, g.ny), wz = min(w, g.nz);
   // One thread per row of the box: the nodes solid last step and fluid now
