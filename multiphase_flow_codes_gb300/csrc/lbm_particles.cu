@@ -260,7 +260,10 @@ __device__ __forceinline__ void k_links_body(int bx, int gx, Geometry g, Particl
   __shared__ typename Scan::TempStorage scan_tmp;
   __shared__ int plane_k[MAXPLANES];
   __shared__ double plane_z[MAXPLANES];
+  __shared__ double plane_zz[MAXPLANES];  // (k - 1/2) - zc of each plane
   __shared__ double yval[3][MAXC];
+  __shared__ double yyv[3][MAXC];         // (j - 1/2) - yc per y candidate and start state
+  __shared__ float yyvf[3][MAXC];
   __shared__ double xval[3][MAXC];
   __shared__ float xofff[3][MAXC];  // (i - 1/2) - x centre per x candidate, FP64 then rounded
   __shared__ int nplanes;
@@ -327,7 +330,13 @@ __device__ __forceinline__ void k_links_body(int bx, int gx, Geometry g, Particl
   const int tx = min(cx.total(), MAXC);
   for (int t = tid; t < 3 * MAXC; t += PB) {
     int s = t / MAXC, c = t % MAXC;
-    if (c < ty) yval[s][c] = sweep_value(sev[s], cy.at(c));
+    if (c < ty) {
+      const double yc = sweep_value(sev[s], cy.at(c));
+      yval[s][c] = yc;
+      const double yy0 = ((double)cy.at(c) - 0.5) - yc;
+      yyv[s][c] = yy0;
+      yyvf[s][c] = (float)yy0;
+    }
     if (c < tx) {
       double v = channel ? x0 : sweep_value(sev[3 + s], cx.at(c));
       xval[s][c] = v;
@@ -343,19 +352,23 @@ __device__ __forceinline__ void k_links_body(int bx, int gx, Geometry g, Particl
   for (int c0 = 0; c0 < tz; c0 += PB) {
     int t = c0 + tid;
     int k = -1;
-    double zc = 0.0;
+    double zc = 0.0, zz0 = 0.0;
     bool take = false;
     if (t < tz) {
       k = cz.at(t);
       zc = sweep_value(sev[6], k);
       double zpnt = (double)k - 0.5;
-      double zz0 = zpnt - zc;
+      zz0 = zpnt - zc;
       take = fabs(zz0) <= radp2;
     }
     int pos, tot;
     Scan(scan_tmp).ExclusiveSum(take ? 1 : 0, pos, tot);
     __syncthreads();
-    if (take && nplanes + pos < MAXPLANES) { plane_k[nplanes + pos] = k; plane_z[nplanes + pos] = zc; }
+    if (take && nplanes + pos < MAXPLANES) {
+      plane_k[nplanes + pos] = k;
+      plane_z[nplanes + pos] = zc;
+      plane_zz[nplanes + pos] = zz0;
+    }
     __syncthreads();
     if (tid == 0) nplanes = min(nplanes + tot, MAXPLANES);
     __syncthreads();
@@ -366,17 +379,16 @@ __device__ __forceinline__ void k_links_body(int bx, int gx, Geometry g, Particl
   for (int c0 = 0; c0 < tpairs; c0 += PB) {
     int t = c0 + tid;
     bool take = false;
-    int k = 0, j = 0;
-    double zc = 0.0, yc = 0.0, zz0 = 0.0, yy0 = 0.0;
+    int k = 0, j = 0, pi = 0, c = 0;
     if (t < tpairs) {
-      int pi = t / ty;
-      int c = t - pi * ty;
+      // the offsets of the row's plane and y candidate come from the tables
+      // above (the same values; the FP64 work done once per plane and
+      // candidate rather than per pair)
+      pi = t / ty;
+      c = t - pi * ty;
       j = cy.at(c);
       k = plane_k[pi];
-      zc = plane_z[pi];
-      yc = yval[min(pi, 2)][c];
-      zz0 = ((double)k - 0.5) - zc;
-      yy0 = ((double)j - 0.5) - yc;
+      const double zz0 = plane_zz[pi], yy0 = yyv[min(pi, 2)][c];
       take = channel ? (sqrt(yy0 * yy0 + zz0 * zz0) <= radp2) : (fabs(yy0) <= radp2);
     }
     int pos, tot;
@@ -384,8 +396,8 @@ __device__ __forceinline__ void k_links_body(int bx, int gx, Geometry g, Particl
     __syncthreads();
     if (take && nrows + pos < MAXROWS) {
       int w = nrows + pos;
-      row_k[w] = k; row_j[w] = j; row_z[w] = zc; row_y[w] = yc;
-      row_yy[w] = (float)yy0; row_zz[w] = (float)zz0;
+      row_k[w] = k; row_j[w] = j; row_z[w] = plane_z[pi]; row_y[w] = yval[min(pi, 2)][c];
+      row_yy[w] = yyvf[min(pi, 2)][c]; row_zz[w] = (float)plane_zz[pi];
     }
     __syncthreads();
     if (tid == 0) nrows = min(nrows + tot, MAXROWS);
@@ -710,7 +722,7 @@ __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, Partic
   // roundings of FP64 values issue on the FP64 pipe, and cost a warp the same
   // whatever its active lanes)
   __shared__ R s_wo[6];
-  __shared__ int s_lo[3];
+  __shared__ int s_lo[4];
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -718,6 +730,9 @@ __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, Partic
       s_wo[3 + a] = R(pv.omgp[3 * p + a]);
       s_lo[a] = (int)floor((double)pv.ypglb[3 * p + a]) - (kBounceSpan / 2);
     }
+    // the link nodes lie within rad + sqrt(2) of the centre: the entries
+    // kBounceSpan / 2 +- (ceil(rad) + 3) of the table cover them
+    s_lo[3] = min((int)ceil(pv.rad) + 3, kBounceSpan / 2 - 1);
   }
   __syncthreads();
   const R w1 = s_wo[0], w2 = s_wo[1], w3 = s_wo[2];
@@ -727,18 +742,21 @@ __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, Partic
   const uint32_t* mask = solid_mask(isnodes, g);
   // Per axis, the offset d = pnt - c of the link point pnt = i + 1/2 from the
   // image c of the centre nearest to it depends on the node's coordinate i
-  // alone: tabulate it once per particle for the kBounceSpan coordinates
-  // around the centre (same operations as per link, so the same values);
-  // links outside the table compute it directly.  Per direction, c_q . w.
+  // alone: tabulate it once per particle for the coordinates around the
+  // centre that links reach (same operations as per link, so the same
+  // values); links outside the table compute it directly.  Per direction,
+  // c_q . w.
   __shared__ R tdel[3][kBounceSpan];
   __shared__ R tcw[NPOP];
   // c_a v with c_a in {-1, 0, 1}: exact, so selected rather than multiplied
   auto sel = [](int c, R v) { return c == 0 ? R(0) : flip_if(c < 0, v); };
   const int lo[3] = {s_lo[0], s_lo[1], s_lo[2]};
+  const int dlo = kBounceSpan / 2 - s_lo[3], dhi = kBounceSpan / 2 + s_lo[3];
   {
     // selects rather than arrays indexed by a, which would live in local memory
-    for (int t = threadIdx.x; t < 3 * kBounceSpan; t += NT) {
-      const int a = t / kBounceSpan, d = t - a * kBounceSpan;
+    const int span = dhi - dlo + 1;
+    for (int t = threadIdx.x; t < 3 * span; t += NT) {
+      const int a = t / span, d = dlo + (t - a * span);
       const bool periodic = !(channel && a == 0);
       // in FP64 whatever R: an FP32 centre near x = 256 is off by 1.5e-5
       const double cen = pv.ypglb[3 * p + a];
@@ -758,7 +776,7 @@ __device__ __forceinline__ void k_bounce_body(int bx, int gx, Geometry g, Partic
   auto delta = [&](int a, int i, R, int n, int nhalf, bool periodic) -> R {
     int d = i - lo[a];
     if (periodic) d = d < 0 ? d + n : (d >= n ? d - n : d);
-    if (d >= 0 && d < kBounceSpan) return tdel[a][d];
+    if (d >= dlo && d <= dhi) return tdel[a][d];
     const double cen = pv.ypglb[3 * p + a];
     const double pnt = (double)(i + 1) - 0.5;
     return R(pnt - (periodic ? near_img_t<double>(cen, pnt, n, nhalf) : cen));
