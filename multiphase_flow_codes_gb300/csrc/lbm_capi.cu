@@ -457,15 +457,17 @@ void do_forcing(lbm_ctx* c) {
   }
 }
 
-// Launch the next step's FORCING on the side stream once the fused kernel
-// just enqueued (the last reader of the table slot it overwrites) is done;
-// it then overlaps the particle kernels of the current step.  The forcing
-// state is backed up first so that cancel_prefetch can undo it.
+// Launch the next step's FORCING on the side stream, right after this step's
+// FORCING was taken (do_forcing): it runs beside this step's stream +
+// collide, whose FP64 fixed-point and FP32 kernels leave the FP64 pipe idle,
+// rather than beside the particle kernels, which need that pipe (this GPU
+// issues FP64 at 2 lanes per clock per SM).  The forcing state is backed up
+// first so that cancel_prefetch can undo it.
 void prefetch_forcing(lbm_ctx* c) {
   if (c->cfg.forcing != LBM_FORCING_STOCHASTIC || c->prefetched) return;
-  int slot = 0;
-  for (int s = 0; s < 3; ++s)
-    if (s != c->latest.slot) { slot = s; break; }
+  // the slot neither this step's force nor the previous one's (macrovar's)
+  // occupies: its last reader is the previous step's stream + collide
+  const int slot = pick_slot(c);
   cudaEventRecord(c->ev_main, c->stream);
   cudaStreamWaitEvent(c->side, c->ev_main, 0);
   cudaMemcpyAsync(c->d_forcing_backup, c->d_forcing, sizeof(ForcingDev), cudaMemcpyDeviceToDevice,
@@ -618,6 +620,7 @@ bool plan_staged(lbm_ctx* c, int variant, int stages, int ctas_per_sm, StagedPla
 template <typename T>
 void fused_step_t(lbm_ctx* c) {
   do_forcing(c);
+  prefetch_forcing(c);
   const bool fixed = fixed_path(c);
   if (fixed) pop_format(c, true);
   T* fin = fixed ? fraw<T>(c, c->cur) : fbuf<T>(c, c->cur);
@@ -625,7 +628,6 @@ void fused_step_t(lbm_ctx* c) {
   prof_begin(c);
   launch_stream_collide<T>(c, fin, fout, true);
   prof_end(c, LBM_PHASE_STREAM_COLLIDE);
-  prefetch_forcing(c);
   particle_prelude(c);
   if (c->particles_on) {
     prof_begin(c);

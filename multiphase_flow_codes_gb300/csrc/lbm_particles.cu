@@ -985,11 +985,28 @@ __global__ void __launch_bounds__(PB) k_bounce_store(Geometry g, ParticleView pv
 // the lubrication range contribute exact zeros in the reference; the warp
 // finds the near partners with a single-precision range test (wide margin)
 // and lane 0 adds their FP64 contributions in id order.
+// An FP64 value as FP32, truncated (relative error below 2^-23), by integer
+// operations on its bits: a double-to-float conversion issues on the FP64
+// pipe, which this GPU runs at 2 lanes per clock per SM, and the pair
+// prefilters below convert every pair's coordinates.  Magnitudes below
+// 2^-126 give 0 (only coordinates within a box are converted, |v| < 2^30).
+__device__ __forceinline__ float f32_trunc(double v) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+  if (e <= 0) return 0.0f;
+  return __uint_as_float((hi & 0x80000000u) | ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) |
+                         (lo >> 29));
+}
+
+// FP32 prefilter of a particle pair: the centres within lim per axis and in
+// distance, nearest image (a margin of a lattice unit over the exact FP64
+// test that follows, far above the FP32 error of the coordinates)
 __device__ __forceinline__ bool near_pair(const Geometry& g, const double* y, int p, int q,
                                           float lim) {
-  float dx = fabsf((float)y[3 * q] - (float)y[3 * p]);
-  float dy = fabsf((float)y[3 * q + 1] - (float)y[3 * p + 1]);
-  float dz = fabsf((float)y[3 * q + 2] - (float)y[3 * p + 2]);
+  float dx = fabsf(f32_trunc(y[3 * q]) - f32_trunc(y[3 * p]));
+  float dy = fabsf(f32_trunc(y[3 * q + 1]) - f32_trunc(y[3 * p + 1]));
+  float dz = fabsf(f32_trunc(y[3 * q + 2]) - f32_trunc(y[3 * p + 2]));
   if (!g.channel) dx = fminf(dx, (float)g.nx - dx);
   dy = fminf(dy, (float)g.ny - dy);
   dz = fminf(dz, (float)g.nz - dz);
