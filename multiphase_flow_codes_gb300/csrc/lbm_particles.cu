@@ -212,25 +212,37 @@ __device__ __forceinline__ void k_link_sweeps_body(int bx, int gx, Geometry g, P
   int ok = 1;
   if (!isfinite(c0)) {
     ok = 0;
-  } else if (axis == 2) {
-    out[6] = sweep_events(c0, g.nz, g.nzh);
-    ok = out[6].ok;
-  } else if (axis == 1 && g.channel) {
-    // no x sweep in the channel (walls in x)
-    SweepEv e;
-    e.nev = 0; e.ok = 1; e.v0 = c0;
-    out[3] = e; out[4] = e; out[5] = e;
   } else {
-    const int n = axis == 0 ? g.ny : g.nx, nh = axis == 0 ? g.nyh : g.nxh;
-    SweepEv* o = out + (axis == 0 ? 0 : 3);
+    // The three axes in one instruction stream: y and x take three start
+    // states and the fixed-point check (four sweeps), z one sweep; the z
+    // lanes run the y and x lanes' four rounds with them and keep only the
+    // first, so that a warp pays for four serial sweeps rather than five
+    // (FP64 issues at 2 lanes per clock per SM whatever the active lanes).
+    const bool xwall = axis == 1 && g.channel;  // no x sweep in the channel
+    const int n = axis == 0 ? g.ny : (axis == 1 ? g.nx : g.nz);
+    const int nh = axis == 0 ? g.nyh : (axis == 1 ? g.nxh : g.nzh);
+    SweepEv* o = out + 3 * axis;
     double c = c0;
-    for (int s = 0; s < 3; ++s) {
-      o[s] = sweep_events(c, n, nh);
-      ok &= o[s].ok;
-      c = sweep_value(o[s], n);
+    for (int s = 0; s < 4; ++s) {
+      const SweepEv e = sweep_events(c, n, nh);
+      const double next = sweep_value(e, n);
+      if (!xwall) {
+        if (axis == 2) {
+          if (s == 0) { o[0] = e; ok = e.ok; }
+        } else if (s < 3) {
+          o[s] = e;
+          ok &= e.ok;
+        } else if (next != c) {
+          ok = 0;
+        }
+      }
+      c = next;
     }
-    SweepEv last = sweep_events(c, n, nh);
-    if (sweep_value(last, n) != c) ok = 0;
+    if (xwall) {
+      SweepEv e;
+      e.nev = 0; e.ok = 1; e.v0 = c0;
+      out[3] = e; out[4] = e; out[5] = e;
+    }
   }
   ls.sweep_ok[3 * p + axis] = ok;
 }
