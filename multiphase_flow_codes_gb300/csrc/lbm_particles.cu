@@ -1001,12 +1001,14 @@ __global__ void __launch_bounds__(PB) k_bounce_store(Geometry g, ParticleView pv
 // operations on its bits: a double-to-float conversion issues on the FP64
 // pipe, which this GPU runs at 2 lanes per clock per SM, and the pair
 // prefilters below convert every pair's coordinates.  Magnitudes below
-// 2^-126 give 0 (only coordinates within a box are converted, |v| < 2^30).
+// 2^-126 give 0, magnitudes beyond the FP32 range the largest float (only
+// coordinates within a box are converted, |v| < 2^30).
 __device__ __forceinline__ float f32_trunc(double v) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(v);
   const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
   const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
   if (e <= 0) return 0.0f;
+  if (e >= 255) return __uint_as_float((hi & 0x80000000u) | 0x7f7fffffu);  // (not a box coordinate)
   return __uint_as_float((hi & 0x80000000u) | ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) |
                          (lo >> 29));
 }
