@@ -754,8 +754,19 @@ int upload_soa_t(lbm_ctx* ctx, const double* h, bool aos) {
 template <typename T>
 int download_soa_t(lbm_ctx* ctx, double* h, bool aos) {
   const long long N = ctx->g.N;
-  T* f = fbuf<T>(ctx, ctx->cur);
   double* hm = aos ? static_cast<double*>(const_cast<void*>(mapped_host(h))) : nullptr;
+  if constexpr (sizeof(T) == 8) {
+    if (hm && ctx->g.pop_fixed) {
+      // page-locked host array: convert from the fixed point on the way out,
+      // leaving the stored populations (and the next fused step) as they are
+      launch_soa_fixed_to_aos_host(reinterpret_cast<const long long*>(fraw<T>(ctx, ctx->cur)), hm,
+                                   N, sm_count(), ctx->stream);
+      CK(cudaGetLastError());
+      CK(cudaStreamSynchronize(ctx->stream));
+      return 0;
+    }
+  }
+  T* f = fbuf<T>(ctx, ctx->cur);
   if (hm) {
     launch_soa_to_aos_host<T>(f, hm, N, sm_count(), ctx->stream);
   } else if (aos) {

@@ -610,7 +610,9 @@ __global__ void __launch_bounds__(256) k_aos_host_to_soa(const double* __restric
     __syncthreads();
   }
 }
-template <typename T>
+// FIXED: soa holds the 64-bit fixed-point populations of the FP64 plain path
+// (g.pop_fixed), converted here on the way out rather than in place first
+template <typename T, bool FIXED = false>
 __global__ void __launch_bounds__(256) k_soa_to_aos_host(const T* __restrict__ soa,
                                                          double* __restrict__ aos, long long N) {
   extern __shared__ double tile[];
@@ -622,7 +624,10 @@ __global__ void __launch_bounds__(256) k_soa_to_aos_host(const T* __restrict__ s
     const int total = nn * NPOP;
     for (int i = threadIdx.x; i < total; i += blockDim.x) {
       const int q = i / nn, n = i - q * nn;
-      tile[n * NPOP + q] = (double)soa[(long long)q * N + a0 + n];
+      if constexpr (FIXED)
+        tile[n * NPOP + q] = pop_from_fixed(soa[(long long)q * N + a0 + n]);
+      else
+        tile[n * NPOP + q] = (double)soa[(long long)q * N + a0 + n];
     }
     __syncthreads();
     if ((reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
@@ -903,6 +908,13 @@ void launch_soa_to_aos_host(const T* soa, double* aos_mapped, long long N, int s
   const long long ntiles = (N + kXTile - 1) / kXTile;
   const unsigned grid = (unsigned)std::min<long long>(ntiles, 5LL * sms);
   { k_soa_to_aos_host<T><<<grid, 256, smem, s>>>(soa, aos_mapped, N); count_launch(); }
+}
+void launch_soa_fixed_to_aos_host(const long long* soa, double* aos_mapped, long long N, int sms,
+                                  cudaStream_t s) {
+  const size_t smem = (size_t)kXTile * NPOP * sizeof(double);
+  const long long ntiles = (N + kXTile - 1) / kXTile;
+  const unsigned grid = (unsigned)std::min<long long>(ntiles, 5LL * sms);
+  { k_soa_to_aos_host<long long, true><<<grid, 256, smem, s>>>(soa, aos_mapped, N); count_launch(); }
 }
 template <typename T>
 void launch_convert(const double* in, T* out, long long n, cudaStream_t s) {

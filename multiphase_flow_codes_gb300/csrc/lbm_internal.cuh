@@ -240,6 +240,9 @@ void launch_aos_host_to_soa(const double* aos_mapped, T* soa, long long N, int s
 template <typename T>
 void launch_soa_to_aos_host(const T* soa, double* aos_mapped, long long N, int sms,
                             cudaStream_t s);
+// the same from the FP64 plain path's fixed-point storage (g.pop_fixed)
+void launch_soa_fixed_to_aos_host(const long long* soa, double* aos_mapped, long long N, int sms,
+                                  cudaStream_t s);
 template <typename T>
 void launch_convert(const double* in, T* out, long long n, cudaStream_t s);
 template <typename T>

@@ -294,6 +294,31 @@ def test_fortran_layout_page_locked(require_gpu, oracle_mod, precision):
     box.close()
 
 
+def test_page_locked_download_between_fused_steps(require_gpu, oracle_mod):
+    """Between the FP64 plain path's fused steps the populations are stored
+    in fixed point; a download to page-locked memory converts them on the way
+    out (the same values as the staged download, which converts the buffer in
+    place) and leaves the stored state alone, so steps with downloads in
+    between follow the trajectory of steps without, bit for bit."""
+    import torch
+    from multiphase_flow_codes_gb300._capi import dptr
+    _, a = make_pair(oracle_mod, shape=(40, 24, 16), npart=2, rad=4.0, rhopart=2.5)
+    _, b = make_pair(oracle_mod, shape=(40, 24, 16), npart=2, rad=4.0, rhopart=2.5)
+    a.set_variant(capi.LBM_VARIANT_DIRECT)
+    b.set_variant(capi.LBM_VARIANT_DIRECT)
+    n = 19 * 40 * 24 * 16
+    pin = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+    hp = np.ndarray((19, 40, 24, 16), dtype=np.float64, buffer=pin, order="F")
+    for _ in range(4):
+        a.step(1)
+        b.step(1)
+        a._ck(a._L.lbm_download_f(a.handle, dptr(hp)), "download_f")
+    assert np.array_equal(a.get_f(), b.get_f())
+    assert np.array_equal(hp, b.get_f_fortran())
+    a.close()
+    b.close()
+
+
 def test_mass_momentum(require_gpu, oracle_mod):
     o, box = make_pair(oracle_mod, shape=(16, 16, 16))
     box.step(3)
