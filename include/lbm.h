@@ -138,6 +138,22 @@ int lbm_download_force(lbm_ctx* ctx, double* fx, double* fy, double* fz);
  * (beads_links) and marks the next beads_move as the first one. */
 int lbm_upload_particles(lbm_ctx* ctx, int npart, const double* ypglb,
                          const double* wp, const double* omgp);
+/* initpartvel (3DBox.../partlib.f90:177-263 with trilinear, 320-831;
+ * 3DChannel.../partlib.f90:182-268, 325-836): the fluid velocity at each of
+ * `npart` centres ypglb (3, npart) by trilinear interpolation of the last
+ * macrovar's u between the eight surrounding nodes, into wp (3, npart).
+ * Periodic images along the open axes, as the reference's halo planes give
+ * them; FP64 contexts reproduce the reference's rounding bit for bit.
+ * LBM_ERR_ARG for a centre whose cell leaves the grid (x + 0.5 outside
+ * [0, n + 1) along an open axis; in a channel, x + 0.5 outside [1, nx),
+ * where the reference reads outside ux).  The context's particles are not
+ * changed. */
+int lbm_initpartvel(lbm_ctx* ctx, int npart, const double* ypglb, double* wp);
+/* The release block of the reference's main loop (3DBox.../main.f90:149-165,
+ * 3DChannel.../main.f90:163-175) with given centres: initpartvel, then
+ * initpartomg, whose interpolated spin the reference discards (omgp = 0,
+ * partlib.f90:927-929), then lbm_upload_particles (beads_links). */
+int lbm_release_particles(lbm_ctx* ctx, int npart, const double* ypglb);
 /* any pointer may be NULL; each is a (3, npart) array */
 int lbm_download_particles(lbm_ctx* ctx, double* ypglb, double* wp, double* omgp,
                            double* fHIp, double* flubp, double* torqp);

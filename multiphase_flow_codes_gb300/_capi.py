@@ -84,6 +84,8 @@ SIGNATURES = {
     "lbm_download_macro": (C.c_int, [_P, _D, _D, _D, _D]),
     "lbm_download_force": (C.c_int, [_P, _D, _D, _D]),
     "lbm_upload_particles": (C.c_int, [_P, C.c_int, _D, _D, _D]),
+    "lbm_initpartvel": (C.c_int, [_P, C.c_int, _D, _D]),
+    "lbm_release_particles": (C.c_int, [_P, C.c_int, _D]),
     "lbm_download_particles": (C.c_int, [_P, _D, _D, _D, _D, _D, _D]),
     "lbm_download_flags": (C.c_int, [_P, _I, _I]),
     "lbm_download_links": (C.c_int, [_P, C.c_int64, C.POINTER(C.c_int64), _I, _I, _I, _D]),

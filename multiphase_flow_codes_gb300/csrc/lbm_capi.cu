@@ -1564,6 +1564,41 @@ int lbm_upload_particles(lbm_ctx* ctx, int npart, const double* ypglb, const dou
   return check_status(ctx);
 }
 
+int lbm_initpartvel(lbm_ctx* ctx, int npart, const double* ypglb, double* wp) {
+  if (!ctx || npart < 0 || (npart > 0 && (!ypglb || !wp))) return LBM_ERR_ARG;
+  if (npart == 0) return LBM_OK;
+  materialize_macro(ctx);
+  const size_t b = 3 * (size_t)npart * sizeof(double);
+  char* scratch = nullptr;
+  CK(cudaMallocAsync(reinterpret_cast<void**>(&scratch), 2 * b + 16, ctx->stream));
+  double* dy = reinterpret_cast<double*>(scratch);
+  double* dw = reinterpret_cast<double*>(scratch + b);
+  int* dbad = reinterpret_cast<int*>(scratch + 2 * b);
+  int bad = npart;
+  CK(cudaMemcpyAsync(dy, ypglb, b, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(dbad, &bad, sizeof bad, cudaMemcpyHostToDevice, ctx->stream));
+  if (ctx->f32)
+    launch_initpartvel<float>(ctx->g, mbuf<float>(ctx, 1), mbuf<float>(ctx, 2), mbuf<float>(ctx, 3),
+                              dy, npart, dw, dbad, ctx->stream);
+  else
+    launch_initpartvel<double>(ctx->g, mbuf<double>(ctx, 1), mbuf<double>(ctx, 2),
+                               mbuf<double>(ctx, 3), dy, npart, dw, dbad, ctx->stream);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(wp, dw, b, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(&bad, dbad, sizeof bad, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaFreeAsync(scratch, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (bad < npart) return fail(ctx, LBM_ERR_ARG, "initpartvel: a centre's cell leaves the grid");
+  return LBM_OK;
+}
+
+int lbm_release_particles(lbm_ctx* ctx, int npart, const double* ypglb) {
+  if (!ctx || npart < 0 || npart > ctx->npmax || (npart > 0 && !ypglb)) return LBM_ERR_ARG;
+  std::vector<double> wp(3 * (size_t)npart), omgp(3 * (size_t)npart, 0.0);
+  if (int rc = lbm_initpartvel(ctx, npart, ypglb, wp.data())) return rc;
+  return lbm_upload_particles(ctx, npart, ypglb, wp.data(), omgp.data());
+}
+
 int lbm_particle_state(lbm_ctx* ctx, int dir, int npart, double* state, int32_t* first_move) {
   if (!ctx || (dir != 0 && dir != 1) || npart < 0 || (npart > 0 && !state)) return LBM_ERR_ARG;
   if (ctx->in_batch && dir != 0)

@@ -410,4 +410,11 @@ void launch_filling(const Geometry& g, const ParticleView& pv, const PartParams&
                     const int32_t* isnodes, const int32_t* isnodes0, T* f, FillList fl,
                     DevStatus* st, cudaStream_t s);
 
+// initpartvel: wp (3, npart) at the centres y (3, npart) from the velocity
+// fields; *bad (set to npart by the caller) becomes the smallest index of a
+// centre outside the interpolation range
+template <typename T>
+void launch_initpartvel(const Geometry& g, const T* ux, const T* uy, const T* uz,
+                        const double* y, int npart, double* wp, int* bad, cudaStream_t s);
+
 }  // namespace lbm

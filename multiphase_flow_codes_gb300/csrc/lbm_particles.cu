@@ -1700,4 +1700,76 @@ template void launch_filling<float>(const Geometry&, const ParticleView&, const 
                                     const int32_t*, const int32_t*, float*, FillList,
                                     DevStatus*, cudaStream_t);
 
+// initpartvel with trilinear (iflag = 1), 3DBox.../partlib.f90:177-263 and
+// 320-831; the channel's (3DChannel.../partlib.f90:182-268, 325-836) has no
+// x image.  One thread per centre and component.  The cell is formed as the
+// reference forms it (1-based node i at i - 0.5, i = int(x + 0.5)); on one
+// domain the halo planes trilinear reads are the periodic images, so the
+// eight nodes wrap into 1..n along the open axes.  Weights and sum are
+// rounded in the reference's order with no fused multiply-add: FP64 fields
+// give the reference's wp bit for bit.  A centre whose cell leaves the grid
+// (x + 0.5 outside [0, n + 1) along an open axis, where the reference reads
+// outside its halo planes; x + 0.5 outside [1, nx) in a channel, where it
+// reads outside ux) is reported in *bad and gets wp = 0.
+template <typename T>
+__global__ void k_initpartvel(Geometry g, const T* __restrict__ ux, const T* __restrict__ uy,
+                              const T* __restrict__ uz, const double* __restrict__ y, int npart,
+                              double* __restrict__ wp, int* __restrict__ bad) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 3 * npart) return;
+  const int ip = t / 3, d = t - 3 * ip;
+  const double xc = y[3 * ip], yc = y[3 * ip + 1], zc = y[3 * ip + 2];
+  const double sx = __dadd_rn(xc, 0.5), sy = __dadd_rn(yc, 0.5), sz = __dadd_rn(zc, 0.5);
+  const bool ok = (g.channel ? (sx >= 1.0 && sx < g.nx) : (sx >= 0.0 && sx < g.nx + 1.0)) &&
+                  sy >= 0.0 && sy < g.ny + 1.0 && sz >= 0.0 && sz < g.nz + 1.0;
+  if (!ok) {
+    wp[t] = 0.0;
+    atomicMin(bad, ip);
+    return;
+  }
+  int i = (int)sx, j = (int)sy, k = (int)sz;
+  const double tx = __dsub_rn(sx, (double)i), ty = __dsub_rn(sy, (double)j),
+               tz = __dsub_rn(sz, (double)k);
+  const double tx0 = __dsub_rn(1.0, tx), ty0 = __dsub_rn(1.0, ty), tz0 = __dsub_rn(1.0, tz);
+  int ip1 = i + 1, jp1 = j + 1, kp1 = k + 1;
+  if (i == 0) i = g.nx;
+  if (ip1 > g.nx) ip1 = 1;
+  if (j == 0) j = g.ny;
+  if (jp1 > g.ny) jp1 = 1;
+  if (k == 0) k = g.nz;
+  if (kp1 > g.nz) kp1 = 1;
+  const T* u = d == 0 ? ux : (d == 1 ? uy : uz);
+  auto at = [&](int a, int b, int c) {
+    return (double)u[((long long)(c - 1) * g.ny + (b - 1)) * g.nx + (a - 1)];
+  };
+  auto w3 = [](double a, double b, double c, double v) {
+    return __dmul_rn(__dmul_rn(__dmul_rn(a, b), c), v);
+  };
+  double v0 = w3(tx0, ty0, tz0, at(i, j, k));
+  v0 = __dadd_rn(v0, w3(tx, ty0, tz0, at(ip1, j, k)));
+  v0 = __dadd_rn(v0, w3(tx, ty, tz0, at(ip1, jp1, k)));
+  v0 = __dadd_rn(v0, w3(tx0, ty, tz0, at(i, jp1, k)));
+  v0 = __dadd_rn(v0, w3(tx0, ty0, tz, at(i, j, kp1)));
+  v0 = __dadd_rn(v0, w3(tx, ty0, tz, at(ip1, j, kp1)));
+  v0 = __dadd_rn(v0, w3(tx, ty, tz, at(ip1, jp1, kp1)));
+  v0 = __dadd_rn(v0, w3(tx0, ty, tz, at(i, jp1, kp1)));
+  wp[t] = v0;
+}
+
+template <typename T>
+void launch_initpartvel(const Geometry& g, const T* ux, const T* uy, const T* uz,
+                        const double* y, int npart, double* wp, int* bad, cudaStream_t s) {
+  if (npart <= 0) return;
+  const int n = 3 * npart;
+  k_initpartvel<T><<<(n + 127) / 128, 128, 0, s>>>(g, ux, uy, uz, y, npart, wp, bad);
+  count_launch();
+}
+
+template void launch_initpartvel<double>(const Geometry&, const double*, const double*,
+                                         const double*, const double*, int, double*, int*,
+                                         cudaStream_t);
+template void launch_initpartvel<float>(const Geometry&, const float*, const float*,
+                                        const float*, const double*, int, double*, int*,
+                                        cudaStream_t);
+
 }  // namespace lbm

@@ -229,10 +229,28 @@ class LBMBox:
                 "omgpmax": out[4]}
 
     # ---- particles -------------------------------------------------------
-    def release_particles(self, ypglb: np.ndarray, wp: np.ndarray | None = None,
+    def initpartvel(self, ypglb: np.ndarray) -> np.ndarray:
+        """The fluid velocity at the centres (npart, 3) by trilinear
+        interpolation of u (initpartvel, partlib.f90:177-263); the context's
+        particles are not changed."""
+        y = np.ascontiguousarray(ypglb, dtype=np.float64).reshape(-1, 3)
+        w = np.zeros_like(y)
+        self._ck(self._L.lbm_initpartvel(self._h, y.shape[0], dptr(y), dptr(w)), "initpartvel")
+        return w
+
+    def release_particles(self, ypglb: np.ndarray, wp: np.ndarray | str | None = None,
                           omgp: np.ndarray | None = None):
+        """Release spheres at the centres (npart, 3): with wp = "fluid" the
+        reference's release block (initpartvel, omgp = 0, beads_links),
+        otherwise the given velocities (None: at rest)."""
         y = np.ascontiguousarray(ypglb, dtype=np.float64).reshape(-1, 3)
         n = y.shape[0]
+        if isinstance(wp, str):
+            if wp != "fluid" or omgp is not None:
+                raise ValueError('wp is an array, None or "fluid" (with omgp None)')
+            self._ck(self._L.lbm_release_particles(self._h, n, dptr(y)), "release_particles")
+            self.npart = n
+            return
         w = np.zeros_like(y) if wp is None else np.ascontiguousarray(wp, dtype=np.float64).reshape(n, 3)
         o = np.zeros_like(y) if omgp is None else np.ascontiguousarray(omgp, dtype=np.float64).reshape(n, 3)
         self._ck(self._L.lbm_upload_particles(self._h, n, dptr(y), dptr(w), dptr(o)),

@@ -61,6 +61,8 @@ def lib() -> C.CDLL:
         L.orc_error.argtypes = [P]
         L.orc_npart.argtypes = [P]
         L.orc_initpartpos.argtypes = [P, C.c_int]
+        L.orc_initpartvel.argtypes = [P, C.c_int]
+        L.orc_initpartvel.restype = C.c_int
         L.orc_release.argtypes = [P, C.c_int]
         L.orc_release.restype = None
         L.orc_restore.argtypes = [P, C.c_int]
@@ -180,6 +182,19 @@ class OracleBox:
 
     def initpartpos(self, npart: int) -> int:
         return self._L.orc_initpartpos(self._h, npart)
+
+    def initpartvel(self, ypglb) -> np.ndarray:
+        """wp at the given centres from the current ux, uy, uz (initpartvel,
+        B/partlib.f90:177-263); returns wp (npart, 3).  ValueError for a
+        centre whose cell leaves the grid (a channel's: within 0.5 of a
+        wall)."""
+        y = np.asarray(ypglb, dtype=np.float64).reshape(-1, 3)
+        n = y.shape[0]
+        self.ypglb[:n] = y
+        bad = self._L.orc_initpartvel(self._h, n)
+        if bad >= 0:
+            raise ValueError(f"particle {bad}: centre outside the interpolation range")
+        return self.wp[:n].copy()
 
     def release_particles(self, ypglb, wp=None, omgp=None):
         y = np.asarray(ypglb, dtype=np.float64).reshape(-1, 3)

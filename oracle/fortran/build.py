@@ -36,12 +36,12 @@ REF_ROOT = Path(os.environ.get("LBM_REFERENCE_ROOT", "/root/reference"))
 BOX_ROOTS = ["para", "allocarray", "wave", "set_plan1d_rc", "set_plan1d_cc", "initpop",
              "collision_mrt", "macrovar", "rhoupdat", "streaming", "forcing", "beads_links",
              "beads_collision", "beads_lubforce", "beads_move", "beads_redistribute",
-             "beads_filling", "initpartpos"]
+             "beads_filling", "initpartpos", "initpartvel"]
 
 CHANNEL_ROOTS = ["para", "allocarray", "initpop", "initvel", "collision_mrt", "macrovar",
                  "rhoupdat", "streaming", "forcing", "beads_links", "beads_collision",
                  "beads_lubforce", "beads_move", "beads_redistribute", "beads_filling",
-                 "initpartpos"]
+                 "initpartpos", "initpartvel"]
 
 PROGRAMS = {
     "box": {
@@ -92,6 +92,7 @@ def generate(prog: str) -> Path:
         units += parse_units(text, f, spec["patches"].get(f, ()))
     for f in ("fparse.py", "funits.py", "fgen.py"):
         h.update((HERE / f).read_bytes())
+    h.update(",".join(spec["roots"]).encode())
     tag = h.hexdigest()[:16]
     out = cpp_path(prog)
     if out.exists() and f"source-hash {tag}" in out.read_text().split("\n", 2)[1]:

@@ -638,6 +638,57 @@ struct Oracle {
     return LBM_ERR_OVERLAP;
   }
 
+  // initpartvel, B/partlib.f90:177-263 with trilinear (iflag = 1),
+  // B/partlib.f90:320-831 (channel: C/partlib.f90:182-268, 325-836, the same
+  // but with the x wrap of 356-358 commented out).  One process holds the
+  // whole domain, so the halo planes exchng1 brings in (tmpL = plane nz,
+  // tmpR = plane 1, tmpU = row 1, tmpD = row ny, with their corners) are the
+  // periodic images, and every case of trilinear reads u at the nodes
+  // (i|ip1, j|jp1, k|kp1) wrapped into 1..n.  Node i (1-based) sits at
+  // i - 0.5.  The weights and the sum are formed in the reference's order.
+  // Returns the 0-based index of the first centre whose cell leaves the grid
+  // (x + 0.5 outside [0, n + 1) along an open axis, outside [1, nx) along a
+  // channel's walls: the reference reads outside its arrays there), else -1.
+  int initpartvel(int np) {
+    const double* uv[3] = {ux.data(), uy.data(), uz.data()};
+    for (int ip = 0; ip < np; ++ip) {
+      const double xc = ypglb[3 * ip], yc = ypglb[3 * ip + 1], zc = ypglb[3 * ip + 2];
+      const double sx = (xc + 0.5) / 1.0, sy = (yc - 0.0 + 0.5) / 1.0, sz = (zc - 0.0 + 0.5) / 1.0;
+      if (!((channel ? (sx >= 1.0 && sx < nx) : (sx >= 0.0 && sx < nx + 1.0)) && sy >= 0.0 &&
+            sy < ny + 1.0 && sz >= 0.0 && sz < nz + 1.0))
+        return ip;
+      int i = (int)((xc + 0.5) / 1.0);
+      int j = (int)((yc - 0.0 + 0.5) / 1.0);
+      int k = (int)((zc - 0.0 + 0.5) / 1.0);
+      int ip1 = i + 1, jp1 = j + 1, kp1 = k + 1;
+      const double tx = (xc + 0.5 - (double)i) / 1.0;
+      const double ty = (yc - 0.0 + 0.5 - (double)j) / 1.0;
+      const double tz = (zc - 0.0 + 0.5 - (double)k) / 1.0;
+      const double tx0 = 1.0 - tx, ty0 = 1.0 - ty, tz0 = 1.0 - tz;
+      if (!channel) {
+        if (i == 0) i = nx;
+        if (ip1 > nx) ip1 = 1;
+      }
+      if (j == 0) j = ny;
+      if (jp1 > ny) jp1 = 1;
+      if (k == 0) k = nz;
+      if (kp1 > nz) kp1 = 1;
+      auto at = [&](const double* u, int a, int b, int c) {
+        return u[((int64_t)(c - 1) * ny + (b - 1)) * nx + (a - 1)];
+      };
+      for (int d = 0; d < 3; ++d) {
+        const double* u = uv[d];
+        const double v1 = at(u, i, j, k), v2 = at(u, ip1, j, k), v3 = at(u, ip1, jp1, k),
+                     v4 = at(u, i, jp1, k), v5 = at(u, i, j, kp1), v6 = at(u, ip1, j, kp1),
+                     v7 = at(u, ip1, jp1, kp1), v8 = at(u, i, jp1, kp1);
+        wp[3 * ip + d] = tx0 * ty0 * tz0 * v1 + tx * ty0 * tz0 * v2 + tx * ty * tz0 * v3 +
+                         tx0 * ty * tz0 * v4 + tx0 * ty0 * tz * v5 + tx * ty0 * tz * v6 +
+                         tx * ty * tz * v7 + tx0 * ty * tz * v8;
+      }
+    }
+    return -1;
+  }
+
   // Release particles at given positions and velocities: the irelease block
   // of B/main.f90:149-165 with initpartvel/initpartomg replaced by inputs.
   void release(int np) {
@@ -1130,6 +1181,7 @@ void orc_macrovar(void* h) { static_cast<Oracle*>(h)->macrovar(); }
 void orc_rhoupdat(void* h) { static_cast<Oracle*>(h)->rhoupdat(); }
 void orc_initpop(void* h) { static_cast<Oracle*>(h)->initpop(); }
 int orc_initpartpos(void* h, int np) { return static_cast<Oracle*>(h)->initpartpos(np); }
+int orc_initpartvel(void* h, int np) { return static_cast<Oracle*>(h)->initpartvel(np); }
 // positions already in ypglb (set through orc_field), velocities in wp/omgp
 void orc_release(void* h, int np) { static_cast<Oracle*>(h)->release(np); }
 // host threads of the parallel loops (the CPU baseline's core count)

@@ -13,11 +13,16 @@ sources are absent:
                               velocities, 5 full steps
   reference_channel24_p2.npz  3DChannel...: 24 x 28 x 20, walls at x = 0 and
                               x = 24, 2 spheres R = 4, 5 full steps
+  reference_initpartvel.npz   initpartvel of both programs on a 24 x 20 x 16
+                              grid: the seeded velocity (spectral_velocity,
+                              seed 54321, k0 3, u_rms 0.04) interpolated at
+                              13 centres in every halo case of trilinear
 
 Each holds the particle vectors, the solid-node ids (isnodes, 1-based as
 the reference), the number of links, the forcing generator's state (box),
 and the populations at 4096 seeded positions.
-Run: python tests/golden/make_reference_golden.py   (needs the reference)
+Run: python tests/golden/make_reference_golden.py [name ...]   (needs the
+reference; with names, only those fixtures)
 """
 
 import sys
@@ -55,7 +60,46 @@ def record(R, name, box: bool):
     np.savez_compressed(HERE / name, **out)
 
 
-def main():
+INTERP = np.array([
+    [10.3, 9.7, 7.2], [0.2, 5.3, 6.6], [23.8, 6.1, 3.3], [7.7, 0.3, 8.1], [11.1, 19.6, 9.9],
+    [3.3, 4.4, 0.1], [5.5, 7.5, 15.7], [0.1, 0.2, 0.3], [23.9, 19.9, 15.9], [12.0, 0.4, 15.6],
+    [6.0, 19.7, 0.2], [2.2, 19.8, 15.8], [4.5, 5.5, 6.5]])
+
+
+def interp_centres(channel: bool, nx: int = 24):
+    pos = INTERP.copy()
+    if channel:  # x cells inside the walls
+        pos[:, 0] = np.clip(pos[:, 0], 0.6, nx - 0.6)
+    return pos
+
+
+def record_initpartvel():
+    shape = (24, 20, 16)
+    u = inputs.spectral_velocity(shape[0], 3.0, 0.04, seed=54321, ny=shape[1], nz=shape[2])
+    out = {}
+    for prog in ("box", "channel"):
+        pos = interp_centres(prog == "channel", shape[0])
+        n = pos.shape[0]
+        if prog == "box":
+            R = refrun.box_program(shape[0], n, 1.0, 1.0, ny=shape[1], nz=shape[2])
+        else:
+            R = refrun.channel_program(*shape, n, 1.0, 1.0)
+        refrun.set_velocity(R, *u)
+        R["istep"] = 1
+        R.call("initpartpos")
+        R["ypglb"] = pos.T
+        R["yp"][:, :n] = pos.T
+        R.call("initpartvel")
+        out[f"pos_{prog}"] = pos
+        out[f"wp_{prog}"] = R["wp"].T.copy()
+    np.savez_compressed(HERE / "reference_initpartvel.npz", **out)
+
+
+def main(only=()):
+    if not only or "initpartvel" in only:
+        record_initpartvel()
+    if only and "runs" not in only:
+        return
     n = 24
     R = refrun.box_program(n, 2, 4.0, 2.5)
     refrun.set_velocity(R, *inputs.spectral_velocity(n, 4.0, 0.03, seed=54321))
@@ -80,4 +124,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))

@@ -11,6 +11,12 @@
   energy exactly on the workload's spectrum k^4 exp(-2 (k/k0)^2).
 * ``lbm_init_channel``: initvel of the channel program (the log-law mean
   flow, 3DChannel.../initial.f90:57-126) against its numpy restatement.
+* ``lbm_initpartvel`` / ``lbm_release_particles``: initpartvel's trilinear
+  interpolation of u at the centres (3DBox.../partlib.f90:177-263, 320-831)
+  bit for bit against the oracle's restatement (itself pinned bit for bit to
+  the reference's Fortran) on the engine's own velocity field, with centres
+  in every halo case; the release block (initpartvel, omgp = 0, links) and
+  the rejection of centres whose cell leaves the grid.
 """
 
 import numpy as np
@@ -107,3 +113,81 @@ def test_init_channel_loglaw(require_gpu):
         ref = np.stack(initial.channel_loglaw(*shape, cfg.visc))
         assert np.abs(u - ref).max() <= 1e-15 * np.abs(ref).max() + 1e-18, shape
         assert ref[1].max() > 0.0
+
+
+# centres in every halo case of trilinear on a 24 x 20 x 16 grid: below the
+# first and above the last node along each axis, corners, a centre on a node
+INTERP = np.array([
+    [10.3, 9.7, 7.2], [0.2, 5.3, 6.6], [23.8, 6.1, 3.3], [7.7, 0.3, 8.1], [11.1, 19.6, 9.9],
+    [3.3, 4.4, 0.1], [5.5, 7.5, 15.7], [0.1, 0.2, 0.3], [23.9, 19.9, 15.9], [12.0, 0.4, 15.6],
+    [6.0, 19.7, 0.2], [2.2, 19.8, 15.8], [4.5, 5.5, 6.5]])
+
+
+def _interp_box(oracle_mod, preset, precision):
+    from multiphase_flow_codes_gb300.engine import LBMBox
+    shape = (24, 20, 16)
+    cfg = capi.config_init(preset, *shape, len(INTERP), 1.0, 2.5)
+    cfg.precision = precision
+    box = LBMBox(cfg)
+    u = inputs.spectral_velocity(shape[0], 3.0, 0.04, ny=shape[1], nz=shape[2])
+    box.initpop(*u)
+    box.macrovar()
+    _, ux, uy, uz = box.get_macro()
+    o = oracle_mod.OracleBox(cfg)
+    o.ux[...] = ux
+    o.uy[...] = uy
+    o.uz[...] = uz
+    pos = INTERP.copy()
+    if preset == capi.LBM_PRESET_CHANNEL:
+        pos[:, 0] = np.clip(pos[:, 0], 0.6, shape[0] - 0.6)
+    return box, o, pos
+
+
+@pytest.mark.parametrize("preset", [capi.LBM_PRESET_BOX, capi.LBM_PRESET_CHANNEL])
+@pytest.mark.parametrize("precision", [capi.LBM_PREC_F64, capi.LBM_PREC_F32])
+def test_initpartvel_bit_exact(require_gpu, oracle_mod, preset, precision):
+    box, o, pos = _interp_box(oracle_mod, preset, precision)
+    got = box.initpartvel(pos)
+    ref = o.initpartvel(pos)
+    assert np.abs(ref).max() > 0
+    assert np.array_equal(got, ref), np.abs(got - ref).max()
+    assert box.npart == 0  # the context's particles are not changed
+    box.close()
+
+
+def test_release_particles_in_the_flow(require_gpu, oracle_mod):
+    """The reference's release block: wp interpolated, omgp = 0, flags and
+    links as the oracle builds them for those centres and velocities."""
+    from conftest import gpu_links, oracle_links
+    box, o, pos = _interp_box(oracle_mod, capi.LBM_PRESET_BOX, capi.LBM_PREC_F64)
+    pos = pos[[0, 4, 8]]  # three spheres of radius 1 far apart
+    box.release_particles(pos, wp="fluid")
+    p = box.get_particles()
+    wp = o.initpartvel(pos)
+    assert np.array_equal(p["ypglb"], pos)
+    assert np.array_equal(p["wp"], wp)
+    assert not p["omgp"].any()
+    o.release_particles(pos, wp)
+    po, no, qo, _ = oracle_links(o)
+    pg, ng, qg, _ = gpu_links(box)
+    assert np.array_equal(po, pg) and np.array_equal(no, ng) and np.array_equal(qo, qg)
+    box.close()
+
+
+@pytest.mark.parametrize("preset,centre", [
+    (capi.LBM_PRESET_CHANNEL, [0.4, 5.0, 5.0]),
+    (capi.LBM_PRESET_CHANNEL, [23.5, 5.0, 5.0]),
+    (capi.LBM_PRESET_BOX, [24.6, 5.0, 5.0]),
+    (capi.LBM_PRESET_BOX, [5.0, -0.6, 5.0]),
+    (capi.LBM_PRESET_BOX, [5.0, 5.0, float("nan")]),
+])
+def test_initpartvel_rejects_cells_off_the_grid(require_gpu, oracle_mod, preset, centre):
+    box, o, _ = _interp_box(oracle_mod, preset, capi.LBM_PREC_F64)
+    pos = np.array([[5.0, 5.0, 5.0], centre])
+    with pytest.raises(capi.LBMError) as e:
+        box.initpartvel(pos)
+    assert e.value.code == capi.LBM_ERR_ARG
+    with pytest.raises(ValueError):
+        o.initpartvel(pos)
+    assert box.initpartvel(pos[:1]).shape == (1, 3)  # the context stays usable
+    box.close()

@@ -55,3 +55,20 @@ def test_oracle_matches_reference_golden(oracle_mod, kind):
         assert o.iseedf == int(g["iseedf"]) and o.iyf == int(g["iyf"])
         assert np.array_equal(o.ivf, g["ivf"])
     check(o, g, 1e-13 if kind == "box" else 0.0)
+
+
+@pytest.mark.parametrize("kind", ["box", "channel"])
+def test_oracle_initpartvel_matches_reference_golden(oracle_mod, kind):
+    """initpartvel's trilinear interpolation, bit for bit, at centres in
+    every halo case (reference_initpartvel.npz)."""
+    from oracle import config as ocfg
+    g = np.load(GOLDEN / "reference_initpartvel.npz")
+    pos = g[f"pos_{kind}"]
+    shape = (24, 20, 16)
+    preset = ocfg.PRESET_BOX if kind == "box" else ocfg.PRESET_CHANNEL
+    cfg = ocfg.config_init(preset, *shape, pos.shape[0], 1.0, 1.0)
+    o = oracle_mod.OracleBox(cfg)
+    u = inputs.spectral_velocity(shape[0], 3.0, 0.04, seed=54321, ny=shape[1], nz=shape[2])
+    for c, a in zip(("ux", "uy", "uz"), u):
+        getattr(o, c)[...] = a
+    assert np.array_equal(o.initpartvel(pos), g[f"wp_{kind}"])

@@ -193,3 +193,63 @@ def test_box_rhoupdat(oracle_mod):
     F = refrun.fields(R)
     assert np.array_equal(o.rho, F["rho"])
     assert relerr(o.f, F["f"]) == 0.0
+
+
+INTERP_BOX = np.array([
+    [10.3, 9.7, 7.2], [0.2, 5.3, 6.6], [23.8, 6.1, 3.3], [7.7, 0.3, 8.1], [11.1, 19.6, 9.9],
+    [3.3, 4.4, 0.1], [5.5, 7.5, 15.7], [0.1, 0.2, 0.3], [23.9, 19.9, 15.9], [12.0, 0.4, 15.6],
+    [6.0, 19.7, 0.2], [2.2, 19.8, 15.8], [4.5, 5.5, 6.5]])
+
+
+def interp_pair(oracle_mod, prog, shape, positions):
+    """The reference program and the restatement with a random velocity
+    field and the given centres after initpartpos's local lists."""
+    from oracle import config as ocfg
+    nx, ny, nz = shape
+    n = positions.shape[0]
+    if prog == "box":
+        R = refrun.box_program(nx, n, 1.0, 1.0, ny=ny, nz=nz)
+        cfg = ocfg.config_init(ocfg.PRESET_BOX, nx, ny, nz, n, 1.0, 1.0)
+    else:
+        R = refrun.channel_program(nx, ny, nz, n, 1.0, 1.0)
+        cfg = ocfg.config_init(ocfg.PRESET_CHANNEL, nx, ny, nz, n, 1.0, 1.0)
+    o = oracle_mod.OracleBox(cfg)
+    rng = np.random.default_rng(nx * 7 + ny)
+    u = [rng.standard_normal((nz, ny, nx)) * 0.05 for _ in range(3)]
+    refrun.set_velocity(R, *u)
+    for c, a in zip(("ux", "uy", "uz"), u):
+        getattr(o, c)[...] = a
+    R["istep"] = 1
+    R.call("initpartpos")
+    assert np.array_equal(R["ipglb"][:R["nps"]], np.arange(1, n + 1))
+    R["ypglb"] = positions.T
+    R["yp"][:, :n] = positions.T
+    return R, o
+
+
+@pytest.mark.parametrize("prog", ["box", "channel"])
+def test_initpartvel(oracle_mod, prog):
+    """initpartvel (trilinear interpolation of u at the centres,
+    3DBox.../partlib.f90:177-263, 320-831; channel 182-268, 325-836) bit for
+    bit, with centres in every halo case of trilinear: below the first and
+    above the last node along each axis, the corners, a centre on a node."""
+    need(prog)
+    shape = (24, 20, 16)
+    pos = INTERP_BOX.copy()
+    if prog == "channel":  # x cells inside the walls (the reference has no x image there)
+        pos[:, 0] = np.clip(pos[:, 0], 0.6, shape[0] - 0.6)
+    R, o = interp_pair(oracle_mod, prog, shape, pos)
+    R.call("initpartvel")
+    got = o.initpartvel(pos)
+    assert np.array_equal(got, R["wp"].T)
+    assert np.abs(got).max() > 0
+
+
+def test_initpartvel_channel_rejects_wall_cells(oracle_mod):
+    from oracle import config as ocfg
+    cfg = ocfg.config_init(ocfg.PRESET_CHANNEL, 24, 20, 16, 2, 1.0, 1.0)
+    o = oracle_mod.OracleBox(cfg)
+    with pytest.raises(ValueError):
+        o.initpartvel(np.array([[5.0, 5.0, 5.0], [0.4, 5.0, 5.0]]))
+    with pytest.raises(ValueError):
+        o.initpartvel(np.array([[23.6, 5.0, 5.0]]))
