@@ -430,7 +430,8 @@ def main():
         cfg_desc["collision_sums"] = {
             "fixed": "integer-coefficient moment sums exact in 64-bit fixed point, products FP64",
             "integer": "moment sums exact in 64-bit fixed point, velocity and force products as "
-                       "exact 128-bit integer products (no FP64 instruction per in-range node)",
+                       "exact 128-bit integer products; body-force series in FP64, rounded once to "
+                       "fixed point",
             "float": "all FP64"}[args.sums]
 
     import torch
@@ -473,13 +474,14 @@ def main():
             "alg_bytes_per_launch": alg_bytes, "peak_source": peak_src}
     fp64 = {}
     if dtype == "f64" and key in figs and figs[key].get("pipes"):
-        # the all-integer core issues no FP64 instruction: its compute roofline
-        # is the integer pipes, from the ncu capture
-        fp64 = {"fp64_inst_per_node": 0.0, "pipes_pct_of_peak": figs[key]["pipes"],
-                "capture": figs[key].get("capture"),
-                "note": "all-integer collision core: bound by the ALU pipe (fixed-point sums, "
-                        "128-bit products, range tests), not by FP64 or HBM"}
-    elif dtype == "f64" and key in figs and figs[key].get("fp64_flop_per_node") and sc_n:
+        # the integer collision core's compute roofline is the integer pipes,
+        # from the ncu capture (FP64 only in the body-force series)
+        fp64 = {"fp64_inst_per_node": figs[key].get("fp64_inst_per_node", 0.0),
+                "pipes_pct_of_peak": figs[key]["pipes"], "capture": figs[key].get("capture"),
+                "note": "integer collision core, FP64 body-force series: bound by the ALU pipe "
+                        "(fixed-point sums, 128-bit products, range tests), not by FP64 or HBM"}
+    elif dtype == "f64" and key in figs and figs[key].get("fp64_flop_per_node") and phases["stream_collide"][1]:
+        sc_ms, sc_n = phases["stream_collide"]
         import ctypes as C
         peak = C.c_double(0.0)
         rc = capi.lib().lbm_fma_throughput(capi.LBM_PREC_F64, C.byref(peak))

@@ -322,8 +322,10 @@ int lbm_get_variant(lbm_ctx* ctx, int* variant, int* stages, int* groups, int* c
  * LBM_SUMS_INTEGER (FP64 contexts, their default): LBM_SUMS_FIXED with the
  * velocity and force terms as exact 128-bit integer products of fixed-point
  * values too (products rounded once to 2^-64 or 2^-70, each term of a moment
- * once to 2^-61), so the direct kernel issues no FP64 instruction on a node
- * that stays in range (|u| < 1/4, |F| < 2^-9; others take the FP64 path).
+ * once to 2^-61), so the collision issues no FP64 instruction on a node
+ * that stays in range (|u| < 1/4, |F| < 2^-9; others take the FP64 path);
+ * the body-force series is evaluated in FP64 beside it and rounded once to
+ * its fixed point.
  * FP32 contexts accept LBM_SUMS_FLOAT only.  The unfused per-subroutine
  * entries always use LBM_SUMS_FLOAT.  No counterpart in the reference. */
 enum { LBM_SUMS_FLOAT = 0, LBM_SUMS_FIXED = 1, LBM_SUMS_INTEGER = 2 };

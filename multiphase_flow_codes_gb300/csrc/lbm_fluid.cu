@@ -317,6 +317,22 @@ __device__ __forceinline__ void body_force_fx(const ForceView<double>& fv, const
   }
 }
 
+// The body force as body_force evaluates it in FP64 (the series of the row
+// table, as k_macrovar takes it), then in fixed point at 2^-kFxF: beside the
+// all-integer collision core, which leaves the FP64 pipe idle, this costs less
+// issue than body_force_fx's twelve 128-bit products.  |F| >= 2^-7 (outside
+// the fixed point) raises LBM_ERR_STATE.
+__device__ __forceinline__ void body_force_fxd(const ForceView<double>& fv, const Geometry& g,
+                                               int x, int y, int z, long long (&o)[3],
+                                               DevStatus* st, int n) {
+  double v[3];
+  body_force(fv, g, x, y, z, v[0], v[1], v[2]);
+  int e = 0;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) o[c] = fx_from<kFxF>(v[c], e);
+  if (e >= 1023 + (63 - kFxF)) raise_error(st, LBM_ERR_STATE, n);
+}
+
 // k_fused's FX path on populations stored in fixed point (collide_fx_fixed):
 // the FP64 plain path's kernel between fused steps.  Loads and stores are the
 // 64-bit integers themselves; a node collide_fx_fixed declines is converted
@@ -350,14 +366,18 @@ __global__ void __launch_bounds__(128, 5) k_fused_fixed(Geometry g, RatesT<doubl
 #pragma unroll
   for (int q = 0; q < NPOP; ++q) f[q] = fin[(size_t)q * N + n];
   const bool solid = is_solid(solid_mask(isnodes, g), g, z * g.ny + y, x);
+  auto force = [&](const ForceView<double>& fv, long long (&o)[3]) {
+    if constexpr (INTCORE) body_force_fxd(fv, g, x, y, z, o, st, n);
+    else body_force_fx(fv, g, x, y, z, o);
+  };
   if (fcache_mode != 0) {
-    body_force_fx(fnew, g, x, y, z, fc);
-    if (!solid && fcache_mode != 2) body_force_fx(fprev, g, x, y, z, fp);
+    force(fnew, fc);
+    if (!solid && fcache_mode != 2) force(fprev, fp);
 #pragma unroll
     for (int c = 0; c < 3; ++c) fcache[(size_t)c * N + n] = fc[c];
   } else if (!solid) {
-    body_force_fx(fprev, g, x, y, z, fp);
-    body_force_fx(fnew, g, x, y, z, fc);
+    force(fprev, fp);
+    force(fnew, fc);
   }
   if (!solid) {
     bool done;
