@@ -1,10 +1,11 @@
 """One small run of every kernel the library launches, for profiling.
 
-Runs, on cuda:0: the FP64 plain path and the FP32-shifted path of a 128^3
-box with 150 spheres (three full steps each, then the macroscopic fields,
-the statistics and the mass/momentum diagnostics), a batch of three boxes
-of uneven sizes (two steps), the per-subroutine entries once, and the
-allocation-free reduction.  ``python -m multiphase_flow_codes_gb300.kernels_tour``
+Runs, on cuda:0: the FP64 plain path (the collision arithmetic given on the
+command line, default integer) and the FP32-shifted path of a 128^3 box
+with 150 spheres (three full steps each, then the macroscopic fields, the
+statistics, the mass/momentum diagnostics and initpartvel at the centres),
+a batch of three boxes of uneven sizes (two steps), the per-subroutine
+entries once, and the allocation-free reduction.  ``python -m multiphase_flow_codes_gb300.kernels_tour``
 under a profiler gives one launch list covering lbm_step, lbm_batch_step,
 lbm_statistics and the rest.  Inputs are seeded; nothing is checked here.
 """
@@ -20,7 +21,7 @@ from . import config, inputs
 from .engine import LBMBatch, LBMBox
 
 
-def main(n: int = 128, npart: int = 150, steps: int = 3, sums: int = capi.LBM_SUMS_FIXED):
+def main(n: int = 128, npart: int = 150, steps: int = 3, sums: int = capi.LBM_SUMS_INTEGER):
     u = inputs.spectral_velocity(n, 4.0, 0.03)
     y = inputs.initpartpos(n, n, n, npart, 4.0)
     for prec in (capi.LBM_PREC_F64, capi.LBM_PREC_F32):
@@ -37,6 +38,7 @@ def main(n: int = 128, npart: int = 150, steps: int = 3, sums: int = capi.LBM_SU
         box.rmsstat()
         box.mass_momentum()
         box.particle_slip(5.0, 7.0)
+        box.initpartvel(y)
         box.step_unfused(1)
         box.synchronize()
         if prec == capi.LBM_PREC_F64:
@@ -70,4 +72,4 @@ if __name__ == "__main__":
     import sys
     modes = {"fixed": capi.LBM_SUMS_FIXED, "integer": capi.LBM_SUMS_INTEGER,
              "float": capi.LBM_SUMS_FLOAT}
-    main(sums=modes[sys.argv[1]] if len(sys.argv) > 1 else capi.LBM_SUMS_FIXED)
+    main(sums=modes[sys.argv[1]] if len(sys.argv) > 1 else capi.LBM_SUMS_INTEGER)
