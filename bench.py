@@ -212,7 +212,7 @@ def kernel_name(variant, fixed=False, integer=False):
         return f"k_fused_staged (stream + MRT collide + forcing; {st} stages, {per_sm} CTAs/SM)"
     if fixed and integer:
         return ("k_fused_fixed (stream + MRT collide + forcing; direct, populations and forces in "
-                "64-bit fixed point, all-integer collision core)")
+                "64-bit fixed point, integer collision core, FP64 body-force series)")
     if fixed:
         return ("k_fused_fixed (stream + MRT collide + forcing; direct, populations and forces in "
                 "64-bit fixed point)")

@@ -338,9 +338,10 @@ __device__ __forceinline__ void body_force_fxd(const ForceView<double>& fv, cons
 // 64-bit integers themselves; a node collide_fx_fixed declines is converted
 // to FP64, collided by collide_fast and converted back (a value beyond the
 // fixed-point range, |f| >= 32 or not finite, raises LBM_ERR_NONFINITE).
-// The body forces are fixed point too (body_force_fx): the previous step's
-// enters the velocity as an exact integer add; the force cache (fcache_mode
-// as in k_fused) holds them as 64-bit integers at 2^-kFxF.
+// The body forces are fixed point too (INTCORE: the series in FP64, rounded
+// once, body_force_fxd; otherwise exact integer products, body_force_fx): the
+// previous step's enters the velocity as an exact integer add; the force
+// cache (fcache_mode as in k_fused) holds them as 64-bit integers at 2^-kFxF.
 // Five CTAs of 128 threads per SM (96 registers; the 19 populations spill to
 // L1) measured 3 % faster than four without spills, six slower.
 template <bool CHANNEL, bool INTCORE>
