@@ -342,10 +342,13 @@ __device__ __forceinline__ void body_force_fxd(const ForceView<double>& fv, cons
 // once, body_force_fxd; otherwise exact integer products, body_force_fx): the
 // previous step's enters the velocity as an exact integer add; the force
 // cache (fcache_mode as in k_fused) holds them as 64-bit integers at 2^-kFxF.
-// Five CTAs of 128 threads per SM (96 registers; the 19 populations spill to
-// L1) measured 3 % faster than four without spills, six slower.
+// CTAs of 128 threads per SM: four with the integer core (128 registers;
+// with the force series on the FP64 pipe 3.4 % faster at 256^3 than five at
+// 96 registers, twice the spills, and 2.6 % faster than three at 168, no
+// spills); five with the FP64-product core (96 registers, 3 % faster than
+// four there).
 template <bool CHANNEL, bool INTCORE>
-__global__ void __launch_bounds__(128, 5) k_fused_fixed(Geometry g, RatesT<double> r,
+__global__ void __launch_bounds__(128, INTCORE ? 4 : 5) k_fused_fixed(Geometry g, RatesT<double> r,
                                                          const long long* __restrict__ fin,
                                                          long long* __restrict__ fout,
                                                          const int32_t* __restrict__ isnodes,
