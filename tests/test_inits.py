@@ -191,3 +191,23 @@ def test_initpartvel_rejects_cells_off_the_grid(require_gpu, oracle_mod, preset,
         o.initpartvel(pos)
     assert box.initpartvel(pos[:1]).shape == (1, 3)  # the context stays usable
     box.close()
+
+
+def test_initpartvel_at_a_released_sphere_gives_its_velocity(require_gpu, oracle_mod):
+    """Inside a resolved sphere macrovar sets u = w_p + omega x r
+    (3DBox.../collision.f90:278-329), a linear field that trilinear
+    interpolation reproduces: u at the centre is w_p."""
+    from multiphase_flow_codes_gb300.engine import LBMBox
+    cfg = capi.config_init(capi.LBM_PRESET_BOX, 32, 32, 32, 2, 4.0, 2.5)
+    box = LBMBox(cfg)
+    u = inputs.spectral_velocity(32, 4.0, 0.03)
+    box.initpop(*u)
+    box.macrovar()
+    pos = np.array([[8.3, 9.1, 20.6], [24.2, 22.7, 7.4]])
+    wp = np.array([[0.01, -0.02, 0.005], [-0.015, 0.004, 0.02]])
+    om = np.array([[0.002, -0.001, 0.003], [0.0, 0.004, -0.002]])
+    box.release_particles(pos, wp, om)
+    box.macrovar()
+    got = box.initpartvel(pos)
+    assert np.abs(got - wp).max() <= 1e-15, np.abs(got - wp).max()
+    box.close()
