@@ -316,8 +316,10 @@ __host__ __device__ __forceinline__ long long fx_mul(long long v, long long m, i
 
 // |x| < 2^(kFxOutMax) at scale 2^-kFxOut
 __host__ __device__ __forceinline__ unsigned fx_out_of_range(long long x) {
-  const unsigned long long lim = 1ULL << (kFxOut + kFxOutMax);
-  return (unsigned)((unsigned long long)(x + (long long)lim) >= 2 * lim);
+  // |x| >= 2^(kFxOut + kFxOutMax) = 2^56, on the high word: the bound's low
+  // word is zero, so x + 2^56 >= 2^57 is (hi + 2^24) >= 2^25 in 32 bits
+  constexpr unsigned hlim = 1u << (kFxOut + kFxOutMax - 32);
+  return ((unsigned)((unsigned long long)x >> 32) + hlim) & ~(2 * hlim - 1);
 }
 
 // The collision of collide_fast with the integer-coefficient sums of both
@@ -493,11 +495,14 @@ __host__ __device__ __forceinline__ long long mul_round(long long a, long long b
 // is one whose moments leave their ranges).  The roundings (2^-62 per term)
 // are those of fx_core's conversions from FP64.
 constexpr int kFxUU = 64;  // u_a u_b
+//
+// bias is added to every output (through tl1, which each of them holds once):
+// the caller's rounding constant costs one add instead of nineteen.
 __host__ __device__ __forceinline__ bool fx_core_int(const long long (&g)[NPOP], long long fpx,
                                                      long long fpy, long long fpz, long long Fx,
                                                      long long Fy, long long Fz,
                                                      const RatesT<double>& r,
-                                                     long long (&h)[NPOP]) {
+                                                     long long (&h)[NPOP], long long bias = 0) {
   typedef long long I;
   const I a1 = g[1] + g[2], d1 = g[1] - g[2];
   const I a3 = g[3] + g[4], d3 = g[3] - g[4];
@@ -587,9 +592,10 @@ __host__ __device__ __forceinline__ bool fx_core_int(const long long (&g)[NPOP],
   if (out) return false;
 
   // inverse transform, exact (collision.f90:160-200)
-  h[0] = tl1 - 30 * M[1] + 12 * M[2];
-  const I suma = tl1 - 11 * M[1] - 4 * M[2];
-  const I sumb = tl1 + 8 * M[1] + M[2];
+  const I tlb = tl1 + bias;
+  h[0] = tlb - 30 * M[1] + 12 * M[2];
+  const I suma = tlb - 11 * M[1] - 4 * M[2];
+  const I sumb = tlb + 8 * M[1] + M[2];
   const I sumc = tl6 - 4 * M[3];
   const I sumd = 2 * M[6] - 4 * M[7];
   const I sume = tl8 - 4 * M[4];
@@ -693,16 +699,19 @@ __host__ __device__ __forceinline__ bool collide_fx_fixed_int(long long (&g)[NPO
                                                               long long Fx, long long Fy,
                                                               long long Fz,
                                                               const RatesT<double>& r) {
-  constexpr unsigned long long lim = 1ULL << (kFxIn + kFxInMax);
-  unsigned long long out = 0;
+  // |g| < 2^(kFxIn + kFxInMax) = 2^55, tested on the high words: the bound's
+  // low word is zero, so g + 2^55 < 2^56 is (hi + 2^23) < 2^24 in 32 bits
+  constexpr unsigned hlim = 1u << (kFxIn + kFxInMax - 32);
+  unsigned out = 0;
 #pragma unroll
-  for (int q = 0; q < NPOP; ++q) out |= ((unsigned long long)g[q] + lim) & ~(2 * lim - 1);
+  for (int q = 0; q < NPOP; ++q)
+    out |= ((unsigned)((unsigned long long)g[q] >> 32) + hlim) & ~(2 * hlim - 1);
   if (out) return false;
   long long h[NPOP];
-  if (!fx_core_int(g, fpx, fpy, fpz, Fx, Fy, Fz, r, h)) return false;
   constexpr int sh = kFxOut - kFxIn;
+  if (!fx_core_int(g, fpx, fpy, fpz, Fx, Fy, Fz, r, h, 1LL << (sh - 1))) return false;
 #pragma unroll
-  for (int q = 0; q < NPOP; ++q) g[q] = (h[q] + (1LL << (sh - 1))) >> sh;
+  for (int q = 0; q < NPOP; ++q) g[q] = h[q] >> sh;
   return true;
 }
 
