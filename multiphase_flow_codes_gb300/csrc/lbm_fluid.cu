@@ -317,6 +317,14 @@ __device__ __forceinline__ void body_force_fx(const ForceView<double>& fv, const
   }
 }
 
+// a population read once per step: not kept in L1, which holds the kernel's
+// spilled registers and the force tables
+__device__ __forceinline__ long long ld_once(const long long* p) {
+  long long v;
+  asm("ld.global.nc.L1::no_allocate.b64 %0, [%1];" : "=l"(v) : "l"(p));
+  return v;
+}
+
 // The body force as body_force evaluates it in FP64 (the series of the row
 // table, as k_macrovar takes it), then in fixed point at 2^-kFxF: beside the
 // all-integer collision core, which leaves the FP64 pipe idle, this costs less
@@ -368,7 +376,7 @@ __global__ void __launch_bounds__(128, INTCORE ? 4 : 5) k_fused_fixed(Geometry g
     for (int c = 0; c < 3; ++c) fp[c] = fcache[(size_t)c * N + n];
   }
 #pragma unroll
-  for (int q = 0; q < NPOP; ++q) f[q] = fin[(size_t)q * N + n];
+  for (int q = 0; q < NPOP; ++q) f[q] = ld_once(fin + (size_t)q * N + n);
   const bool solid = is_solid(solid_mask(isnodes, g), g, z * g.ny + y, x);
   auto force = [&](const ForceView<double>& fv, long long (&o)[3]) {
     if constexpr (INTCORE) body_force_fxd(fv, g, x, y, z, o, st, n);
