@@ -13,8 +13,31 @@
 
 using namespace lbm;
 
+// fx_out_of_range tests |x| >= 2^56 on the high word; the 64-bit form of
+// the same test, for comparison
+static bool out_of_range_64(long long x) {
+  const unsigned long long lim = 1ULL << (kFxOut + kFxOutMax);
+  return (unsigned long long)x + lim >= 2 * lim;
+}
+
 int main(int argc, char** argv) {
   const int n_states = argc > 1 ? std::atoi(argv[1]) : 100000;
+  {
+    long long bad = 0, n = 0;
+    std::mt19937_64 rng(77);
+    const long long lim = 1LL << (kFxOut + kFxOutMax);
+    const long long edges[] = {0, 1, -1, lim - 1, lim, lim + 1, -lim + 1, -lim, -lim - 1,
+                               (1LL << 62), -(1LL << 62), 0x7fffffffffffffffLL,
+                               (long long)0x8000000000000000ULL, lim - (1LL << 32),
+                               -lim + (1LL << 32), lim + (1LL << 32) - 1};
+    for (long long x : edges) { ++n; bad += (fx_out_of_range(x) != 0) != out_of_range_64(x); }
+    for (int i = 0; i < 2000000; ++i) {
+      const long long x = (long long)rng() >> (i % 10);
+      ++n;
+      bad += (fx_out_of_range(x) != 0) != out_of_range_64(x);
+    }
+    std::printf("range %lld %lld\n", bad, n);
+  }
   for (int mrt = 1; mrt <= 2; ++mrt) {
     Rates rr;
     const double tau = 3 * 0.0036 + 0.5;

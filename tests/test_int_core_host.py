@@ -35,6 +35,8 @@ def test_integer_core_matches_fp64_product_core(tmp_path):
     out = subprocess.run([str(exe), "60000"], check=True, capture_output=True, text=True,
                          timeout=600).stdout.split("\n")
     rows = [ln.split() for ln in out if ln.strip()]
+    rng_row = rows.pop(0)
+    assert rng_row[0] == "range" and int(rng_row[1]) == 0, rng_row  # high-word test == 64-bit test
     assert len(rows) == 2
     for mrt, maxd, dec_int, dec_fp, int_only, fp_only, n in rows:
         assert float(maxd) <= 16 * 2.0 ** -58, (mrt, maxd)
