@@ -44,7 +44,9 @@ enum {
   LBM_ERR_CUDA = -2,      /* a CUDA runtime call failed                      */
   LBM_ERR_OVERLAP = -3,   /* particles overlap after a move (partlib.f90:2641) */
   LBM_ERR_CAPACITY = -4,  /* a fixed-capacity device list overflowed         */
-  LBM_ERR_ALPHA = -5,     /* link fraction outside [0,1] (partlib.f90:1026)  */
+  LBM_ERR_ALPHA = -5,     /* link fraction outside [0,1] (partlib.f90:1026):
+                           * the reference prints and continues there, and so
+                           * do the engine's link kernels; reserved          */
   LBM_ERR_NONFINITE = -6, /* non-finite value detected in the state          */
   LBM_ERR_TIMEOUT = -7,   /* a bounded device-side wait ran out              */
   LBM_ERR_STATE = -8,     /* call out of order (e.g. no particles uploaded)  */
